@@ -1,0 +1,205 @@
+// Internal declarations shared by the translation units of libcov3d_gb300.so.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cufft.h>
+
+#include <cstdint>
+#include <map>
+#include <vector>
+#include <string>
+
+#include "cov3d_gb300.h"
+
+namespace cov3d {
+
+constexpr float kPiF = 3.14159265358979323846f;
+constexpr double kPi = 3.14159265358979323846;
+
+// ----------------------------------------------------------------------------- errors
+
+void set_error(const char *fmt, ...);
+int check_cuda(cudaError_t e, const char *what);
+int check_cufft(cufftResult r, const char *what);
+
+#define COV3D_TRY(expr)                 \
+  do {                                  \
+    int _st = (expr);                   \
+    if (_st != COV3D_OK) return _st;    \
+  } while (0)
+
+#define COV3D_CUDA(expr) COV3D_TRY(::cov3d::check_cuda((expr), #expr))
+// Counts one kernel launch of this library and checks the launch error.
+int launched(const char *name);
+#define COV3D_LAUNCHED(name) COV3D_TRY(::cov3d::launched(name))
+
+// ----------------------------------------------------------------------------- geometry
+
+// How a nonuniform point's fine-grid fractional index is obtained.
+enum PointKind { kPointsNone = 0, kPointsExplicit = 1, kPointsRotations = 2 };
+// How a frequency maps to a fractional centered-grid index.
+enum Mapping { kMapES = 0, kMapGridSample = 1 };
+
+struct PointGeom {
+  int kind;           // PointKind
+  const float *pts;   // explicit: contiguous (N, 3, P) frequencies
+  const float *rot;   // rotations: (N, 9) row-major
+  int Lp;             // image edge (points per image = Lp*Lp)
+  int P;              // Lp*Lp
+  int n;              // fine grid edge
+  int mapping;        // Mapping
+  int wrap;           // wrap explicit points to [-pi, pi)
+  float s_es;         // n / (2 pi)
+  float half_n;       // n / 2 (integer division) as float
+  float gs_scale;     // float32((n/(n-1))/pi)
+  float gs_off;       // float32(1/(n-1)) for even n, else 0
+  float plane_half;   // Lp / 2 (may be .5) as float
+};
+
+// Interpolation kernel descriptor.
+struct KernelSpec {
+  int type;     // cov3d_kernel
+  int width;    // taps per axis
+  float beta;   // ES shape
+  int periodic; // 1 = wrap cell indices mod n, 0 = zero padding
+};
+
+// Bin grid used for point sorting / spreading tiles.
+struct Bins {
+  int bs[3];   // bin edge per axis
+  int nb[3];   // bins per axis
+  int64_t nbins;
+};
+
+// ----------------------------------------------------------------------------- plan
+}  // namespace cov3d
+
+namespace cov3d {
+// Grow-only device buffer owned by a plan.
+struct DevBuf {
+  void *ptr = nullptr;
+  int64_t cap = 0;  // bytes
+  template <typename T>
+  T *as() const {
+    return static_cast<T *>(ptr);
+  }
+};
+int grow(DevBuf &b, int64_t bytes);
+void release(DevBuf &b);
+}  // namespace cov3d
+
+struct cov3d_plan {
+  int L = 0, n = 0, upsample = 2, kernel = COV3D_KERNEL_ES, width = 6;
+  double beta = 0.0;
+  int compensated = 1;
+  int n_trans = 1;
+  cudaStream_t stream = nullptr;
+  int device = 0;
+
+  cov3d::DevBuf gc1d;          // float deapodisation factors per axis (L)
+  double *h_gc1d = nullptr;    // host copy (double)
+
+  // points
+  int point_kind = cov3d::kPointsNone;
+  int wrap = 0;
+  int64_t n_images = 0;
+  int points_L = 0;
+  int64_t n_points = 0;
+  cov3d::DevBuf pts;           // explicit points copy (N, 3, P) float
+  cov3d::DevBuf rot;           // rotations (N, 9) float
+
+  // sort / subproblems
+  cov3d::Bins bins{};
+  int max_sub = 2048;
+  cov3d::DevBuf bin_count;     // int (nbins + 1), last = dead points
+  cov3d::DevBuf bin_off;       // int (nbins + 2)
+  cov3d::DevBuf sub_off;       // int (nbins + 1)
+  cov3d::DevBuf pt_bin, pt_rank, perm;        // int (M)
+  cov3d::DevBuf sub_bin, sub_first, sub_count;  // int (max subproblems)
+  cov3d::DevBuf nsub;          // int scalar
+
+  // workspaces
+  cov3d::DevBuf fine, fine2;   // complex fine grids (n^3 * channels)
+  cov3d::DevBuf q;             // per-point values (points * r) complex
+  cov3d::DevBuf small;         // per-image small matrices
+  cov3d::DevBuf acc;           // double accumulators
+  double *h_acc = nullptr;     // pinned host mirror of acc (64 doubles)
+  std::map<int, cufftHandle> *ffts = nullptr;  // cuFFT plans by channel count
+
+  // phase timing (CUDA events on the plan's stream), see cov3d_plan_timing
+  int timing = 0;
+  std::vector<cudaEvent_t> *ev_pool = nullptr;
+  size_t ev_next = 0;
+  std::vector<int> *ev_phase = nullptr;  // phase of each recorded (start, stop) pair
+};
+
+namespace cov3d {
+
+// ----------------------------------------------------------------------------- phases
+enum Phase {
+  kPhaseSort = 0, kPhasePack, kPhaseFftFwd, kPhaseInterp, kPhaseGram, kPhaseSolve, kPhaseWpass, kPhaseSpread,
+  kPhaseReg, kPhaseFftInv, kPhaseUnpack, kNumPhases
+};
+
+// Records CUDA events around a phase when the plan's timing is enabled.
+class PhaseScope {
+ public:
+  PhaseScope(cov3d_plan *p, int phase);
+  ~PhaseScope();
+ private:
+  cov3d_plan *p_;
+  cudaEvent_t stop_ = nullptr;
+};
+
+// ----------------------------------------------------------------------------- helpers
+
+PointGeom make_geom(const cov3d_plan *p);
+KernelSpec make_kernel(const cov3d_plan *p);
+int get_fft(cov3d_plan *p, int nchan, cufftHandle *out);
+
+// points_sort.cu
+int sort_points(cov3d_plan *p);
+
+// interp.cu
+struct GridArgs {
+  const void *grid;
+  int64_t cell_stride, chan_stride;
+  int shift;  // storage = (centered + shift) mod n
+};
+struct EpilogueArgs {
+  const float *ctf;  // (n_images, P) or null
+  int nyquist;       // zero row/col 0 when Lp even
+  float scale;
+};
+int launch_interp(cov3d_plan *p, const GridArgs &g, int nchan, void *out, int64_t out_ps, int64_t out_cs,
+                  const EpilogueArgs &e);
+
+// spread.cu
+int launch_spread(cov3d_plan *p, const void *values, int64_t in_ps, int64_t in_cs, int nchan, const EpilogueArgs &e,
+                  void *grid, int64_t cell_stride, int64_t chan_stride, int shift);
+int launch_spread_unaggregated(cov3d_plan *p, const void *values, int64_t in_ps, const EpilogueArgs &e,
+                               void *grids);
+
+// grid_ops.cu
+int launch_pack(cov3d_plan *p, const float *vol_real, const void *vol_cplx, const float *log_scale, int use_gc,
+                int nchan, void *fine);
+int launch_unpack_complex(cov3d_plan *p, const void *fine, int nchan, int use_gc, void *out);
+int launch_unpack_grad(cov3d_plan *p, const void *fine, const float *vectors, const float *log_scale, int use_gc,
+                       int nchan, float *grad_vec, double *grad_log_acc);
+int launch_ml_reg(cov3d_plan *p, const void *grid, void *ggrid, const float *fr, int nchan, double coef,
+                  double *cost_acc);
+int launch_gc_volume(const cov3d_plan *p, float *out);
+int launch_zero(cov3d_plan *p, void *ptr, int64_t bytes);
+
+// gram_solve.cu
+int launch_gram(cudaStream_t st, int B, int P, int r, const void *q, int64_t is, int64_t ps, int64_t cs,
+                const void *images, void *gram, void *h, float *yy);
+int launch_wpass(cudaStream_t st, int B, int P, int r, const void *q, int64_t is, int64_t ps, int64_t cs,
+                 const void *images, const void *C, const void *u, void *w, int64_t wis, int64_t wps, int64_t wcs);
+int launch_solve(cudaStream_t st, int B, int r, int objective, const void *gram, const void *h, double s2,
+                 const double *linv, double wscale, double cscale, void *C, void *u, double *cost_b, double *cost_sum,
+                 void *z, void *m, int *bad);
+int covar_cost_grad(cov3d_plan *p, const cov3d_cost_args *a, double *h_cost, double *d_cost, float *d_grad_vectors,
+                    float *d_grad_log_sqrt, double *d_per_image_cost);
+
+}  // namespace cov3d

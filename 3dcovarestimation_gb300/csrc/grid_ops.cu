@@ -1,0 +1,208 @@
+// Fine-grid packing around cuFFT: deapodisation + zero padding + centering as one pass
+// before the forward FFT, and crop + deapodisation after the inverse (reference
+// Covar.get_vectors_fourier_domain covar.py:440-446 / pad_tensor + centered_fft3
+// projection_funcs.py:11-165, whose fftshift/ifftshift/pad copies are folded into index maps).
+//
+// Storage order of the fine grid is the raw FFT order: voxel offset k = j - L/2 sits at
+// storage index k mod n, so no shift pass is needed on either side of the FFT.
+#include "cov3d_device.cuh"
+
+namespace cov3d {
+
+namespace {
+
+// storage coordinate -> voxel index j in [0, L), or -1 when the cell is zero padding
+__device__ __forceinline__ int storage_to_voxel(int s, int L, int n) {
+  const int half = L / 2;
+  if (s < L - half) return s + half;
+  if (s >= n - half) return s - n + half;
+  return -1;
+}
+
+__device__ __forceinline__ int voxel_to_storage(int j, int L, int n) {
+  const int k = j - L / 2;
+  return k < 0 ? k + n : k;
+}
+
+__global__ void pack_kernel(const float *__restrict__ vr, const float2 *__restrict__ vc,
+                            const float *__restrict__ logs, const float *__restrict__ gc, int nchan, int L, int n,
+                            float2 *__restrict__ fine) {
+  const int64_t n3 = (int64_t)n * n * n;
+  const int64_t cell = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (cell >= n3) return;
+  const int s2 = (int)(cell % n);
+  const int s1 = (int)((cell / n) % n);
+  const int s0 = (int)(cell / ((int64_t)n * n));
+  const int j0 = storage_to_voxel(s0, L, n), j1 = storage_to_voxel(s1, L, n), j2 = storage_to_voxel(s2, L, n);
+  float2 *out = fine + cell * nchan;
+  if (j0 < 0 || j1 < 0 || j2 < 0) {
+    for (int c = 0; c < nchan; ++c) out[c] = make_float2(0.f, 0.f);
+    return;
+  }
+  const int64_t L3 = (int64_t)L * L * L;
+  const int64_t v = ((int64_t)j0 * L + j1) * L + j2;
+  const float g = gc ? 1.0f / (__ldg(gc + j0) * __ldg(gc + j1) * __ldg(gc + j2)) : 1.0f;
+  for (int c = 0; c < nchan; ++c) {
+    const float sc = logs ? g * expf(__ldg(logs + c)) : g;
+    float2 x = vr ? make_float2(__ldg(vr + c * L3 + v), 0.f) : vc[c * L3 + v];
+    out[c] = make_float2(x.x * sc, x.y * sc);
+  }
+}
+
+__global__ void unpack_complex_kernel(const float2 *__restrict__ fine, const float *__restrict__ gc, int nchan, int L,
+                                      int n, float2 *__restrict__ out) {
+  const int64_t L3 = (int64_t)L * L * L;
+  const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= L3) return;
+  const int j2 = (int)(v % L), j1 = (int)((v / L) % L), j0 = (int)(v / ((int64_t)L * L));
+  const int64_t cell =
+      ((int64_t)voxel_to_storage(j0, L, n) * n + voxel_to_storage(j1, L, n)) * n + voxel_to_storage(j2, L, n);
+  const float g = gc ? 1.0f / (__ldg(gc + j0) * __ldg(gc + j1) * __ldg(gc + j2)) : 1.0f;
+  for (int c = 0; c < nchan; ++c) {
+    const float2 x = fine[cell * nchan + c];
+    out[c * L3 + v] = make_float2(x.x * g, x.y * g);
+  }
+}
+
+// Gradient w.r.t. the Covar parameters from the inverse-FFT'd fine-grid gradient:
+// dcost/dV = 2 Re(.) / gc on the cropped voxels; d/dvectors = dV * exp(s);
+// d/dlog_sqrt = sum dV * V (accumulated in double).
+__global__ void unpack_grad_kernel(const float2 *__restrict__ fine, const float *__restrict__ vectors,
+                                   const float *__restrict__ logs, const float *__restrict__ gc, int nchan, int L,
+                                   int n, float *__restrict__ gvec, double *__restrict__ glog) {
+  const int64_t L3 = (int64_t)L * L * L;
+  const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool live = v < L3;
+  int64_t cell = 0;
+  float g = 1.0f;
+  if (live) {
+    const int j2 = (int)(v % L), j1 = (int)((v / L) % L), j0 = (int)(v / ((int64_t)L * L));
+    cell = ((int64_t)voxel_to_storage(j0, L, n) * n + voxel_to_storage(j1, L, n)) * n + voxel_to_storage(j2, L, n);
+    if (gc) g = 1.0f / (__ldg(gc + j0) * __ldg(gc + j1) * __ldg(gc + j2));
+  }
+  for (int c = 0; c < nchan; ++c) {
+    double part = 0.0;
+    if (live) {
+      const float e = expf(__ldg(logs + c));
+      const float dV = 2.0f * fine[cell * nchan + c].x * g;
+      const float vec = __ldg(vectors + c * L3 + v);
+      gvec[c * L3 + v] = dV * e;
+      part = (double)dV * (double)(vec * e);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+    if ((threadIdx.x & 31) == 0 && part != 0.0) atomicAdd(glog + c, part);
+  }
+}
+
+// ML Fourier regulariser reg_scale * sum |G|^2 fr / (2 s2) (covar_sgd.py:1373-1376): adds its
+// conjugate-Wirtinger derivative coef * fr * G to the fine-grid gradient, accumulates its value.
+__global__ void ml_reg_kernel(const float2 *__restrict__ grid, float2 *__restrict__ gg, const float *__restrict__ fr,
+                              int nchan, int n, double coef, double *__restrict__ cost) {
+  const int64_t n3 = (int64_t)n * n * n;
+  const int64_t cell = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double part = 0.0;
+  if (cell < n3) {
+    const int half = n / 2;
+    int s2 = (int)(cell % n), s1 = (int)((cell / n) % n), s0 = (int)(cell / ((int64_t)n * n));
+    s0 += half;
+    s1 += half;
+    s2 += half;
+    s0 = s0 >= n ? s0 - n : s0;
+    s1 = s1 >= n ? s1 - n : s1;
+    s2 = s2 >= n ? s2 - n : s2;
+    const float w = __ldg(fr + ((int64_t)s0 * n + s1) * n + s2);
+    const float cf = (float)coef * w;
+    for (int c = 0; c < nchan; ++c) {
+      const float2 x = grid[cell * nchan + c];
+      float2 y = gg[cell * nchan + c];
+      y.x = fmaf(cf, x.x, y.x);
+      y.y = fmaf(cf, x.y, y.y);
+      gg[cell * nchan + c] = y;
+      part += (double)w * ((double)x.x * x.x + (double)x.y * x.y);
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+  __shared__ double warp_part[32];
+  if ((threadIdx.x & 31) == 0) warp_part[threadIdx.x >> 5] = part;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s += warp_part[i];
+    if (s != 0.0) atomicAdd(cost, s * coef);
+  }
+}
+
+__global__ void gc_volume_kernel(const float *__restrict__ gc, int L, float *__restrict__ out) {
+  const int64_t L3 = (int64_t)L * L * L;
+  const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= L3) return;
+  const int j2 = (int)(v % L), j1 = (int)((v / L) % L), j0 = (int)(v / ((int64_t)L * L));
+  out[v] = gc[j0] * gc[j1] * gc[j2];
+}
+
+inline unsigned nblocks(int64_t n, int bs = 256) { return (unsigned)((n + bs - 1) / bs); }
+
+}  // namespace
+
+int launch_pack(cov3d_plan *p, const float *vol_real, const void *vol_cplx, const float *log_scale, int use_gc,
+                int nchan, void *fine) {
+  const int64_t n3 = (int64_t)p->n * p->n * p->n;
+  pack_kernel<<<nblocks(n3), 256, 0, p->stream>>>(vol_real, static_cast<const float2 *>(vol_cplx), log_scale,
+                                                  use_gc ? p->gc1d.as<float>() : nullptr, nchan, p->L, p->n,
+                                                  static_cast<float2 *>(fine));
+  return launched("pack_kernel");
+}
+
+int launch_unpack_complex(cov3d_plan *p, const void *fine, int nchan, int use_gc, void *out) {
+  const int64_t L3 = (int64_t)p->L * p->L * p->L;
+  unpack_complex_kernel<<<nblocks(L3), 256, 0, p->stream>>>(static_cast<const float2 *>(fine),
+                                                            use_gc ? p->gc1d.as<float>() : nullptr, nchan, p->L,
+                                                            p->n, static_cast<float2 *>(out));
+  return launched("unpack_complex_kernel");
+}
+
+int launch_unpack_grad(cov3d_plan *p, const void *fine, const float *vectors, const float *log_scale, int use_gc,
+                       int nchan, float *grad_vec, double *grad_log_acc) {
+  const int64_t L3 = (int64_t)p->L * p->L * p->L;
+  unpack_grad_kernel<<<nblocks(L3), 256, 0, p->stream>>>(static_cast<const float2 *>(fine), vectors, log_scale,
+                                                         use_gc ? p->gc1d.as<float>() : nullptr, nchan, p->L, p->n,
+                                                         grad_vec, grad_log_acc);
+  return launched("unpack_grad_kernel");
+}
+
+int launch_ml_reg(cov3d_plan *p, const void *grid, void *ggrid, const float *fr, int nchan, double coef,
+                  double *cost_acc) {
+  const int64_t n3 = (int64_t)p->n * p->n * p->n;
+  ml_reg_kernel<<<nblocks(n3), 256, 0, p->stream>>>(static_cast<const float2 *>(grid), static_cast<float2 *>(ggrid),
+                                                    fr, nchan, p->n, coef, cost_acc);
+  return launched("ml_reg_kernel");
+}
+
+int launch_gc_volume(const cov3d_plan *p, float *out) {
+  const int64_t L3 = (int64_t)p->L * p->L * p->L;
+  gc_volume_kernel<<<nblocks(L3), 256, 0, p->stream>>>(p->gc1d.as<float>(), p->L, out);
+  return launched("gc_volume_kernel");
+}
+
+int launch_zero(cov3d_plan *p, void *ptr, int64_t bytes) {
+  return check_cuda(cudaMemsetAsync(ptr, 0, (size_t)bytes, p->stream), "cudaMemsetAsync");
+}
+
+int get_fft(cov3d_plan *p, int nchan, cufftHandle *out) {
+  auto it = p->ffts->find(nchan);
+  if (it != p->ffts->end()) {
+    *out = it->second;
+    return check_cufft(cufftSetStream(it->second, p->stream), "cufftSetStream");
+  }
+  cufftHandle h;
+  int dims[3] = {p->n, p->n, p->n};
+  COV3D_TRY(check_cufft(cufftPlanMany(&h, 3, dims, dims, nchan, 1, dims, nchan, 1, CUFFT_C2C, nchan),
+                        "cufftPlanMany"));
+  (*p->ffts)[nchan] = h;
+  *out = h;
+  return check_cufft(cufftSetStream(h, p->stream), "cufftSetStream");
+}
+
+}  // namespace cov3d

@@ -1,0 +1,64 @@
+"""Seeded synthetic cryo-EM data on the GPU (stands in for the reference's ``SimulatedSource``,
+``source.py:312-542``, and its ASPIRE/cryoDRGN CTF code, which are not part of this library).
+
+Volumes are sums of isotropic 3D Gaussians; rotations are uniform on SO(3) (normalised
+Gaussian quaternions); the CTF is the standard weak-phase form
+``-(sqrt(1-A^2) sin chi + A cos chi)``, ``chi = pi*lambda*df*k^2 - pi/2*Cs*lambda^3*k^4`` with
+the relativistic electron wavelength.  CTF values are therefore not bit-identical to ASPIRE's
+``RadialCTFFilter``; every parity test feeds the same CTF array to both sides.
+"""
+
+import math
+
+import torch
+
+
+def gaussian_blob_volumes(count, L, blobs=50, radius=0.35, width=(1.0, 3.0), amp=(0.5, 1.0), generator=None,
+                          device="cuda"):
+    """(count, L, L, L) float32 sums of ``blobs`` Gaussians, centres uniform in a ball."""
+    g = generator
+    dev = torch.device(device)
+    ax = torch.arange(L, device=dev, dtype=torch.float32) - L // 2
+    z, y, x = torch.meshgrid(ax, ax, ax, indexing="ij")
+    out = torch.zeros((count, L, L, L), device=dev)
+    for c in range(count):
+        d = torch.randn((blobs, 3), generator=g, device=dev)
+        d = d / d.norm(dim=1, keepdim=True)
+        rr = torch.rand((blobs, 1), generator=g, device=dev) ** (1.0 / 3.0) * radius * L
+        centres = d * rr
+        sig = torch.rand((blobs,), generator=g, device=dev) * (width[1] - width[0]) + width[0]
+        a = torch.rand((blobs,), generator=g, device=dev) * (amp[1] - amp[0]) + amp[0]
+        for i in range(blobs):
+            r2 = (z - centres[i, 0]) ** 2 + (y - centres[i, 1]) ** 2 + (x - centres[i, 2]) ** 2
+            out[c] += a[i] * torch.exp(-r2 / (2 * sig[i] ** 2))
+    return out
+
+
+def uniform_rotations(n, generator=None, device="cuda"):
+    """(n, 3, 3) rotation matrices from normalised Gaussian quaternions."""
+    q = torch.randn((n, 4), generator=generator, device=device, dtype=torch.float64)
+    q = q / q.norm(dim=1, keepdim=True)
+    w, x, y, z = q.unbind(1)
+    R = torch.stack([1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w),
+                     2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w),
+                     2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)], dim=1)
+    return R.reshape(n, 3, 3).to(torch.float32)
+
+
+def electron_wavelength(voltage_kv):
+    v = voltage_kv * 1e3
+    return 12.2643247 / math.sqrt(v * (1 + 0.978466e-6 * v))  # Angstrom
+
+
+def ctf_images(defocus_um, L, pixel_size, voltage_kv=300.0, cs_mm=2.7, amplitude_contrast=0.1, device="cuda"):
+    """(n, L, L) float32 CTFs on the centered Fourier grid of an L x L image."""
+    dev = torch.device(device)
+    lam = electron_wavelength(voltage_kv)
+    f = (torch.arange(L, device=dev, dtype=torch.float64) - L // 2) / (L * pixel_size)
+    ky, kx = torch.meshgrid(f, f, indexing="ij")
+    k2 = kx * kx + ky * ky
+    df = defocus_um.to(dev, torch.float64).reshape(-1, 1, 1) * 1e4  # Angstrom
+    cs = cs_mm * 1e7
+    chi = math.pi * lam * df * k2 - 0.5 * math.pi * cs * lam**3 * k2 * k2
+    A = amplitude_contrast
+    return (-(math.sqrt(1 - A * A) * torch.sin(chi) + A * torch.cos(chi))).to(torch.float32)

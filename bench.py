@@ -1,0 +1,364 @@
+"""Covariance-SGD throughput on GB300 (the reference's headline path).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+One step = one covariance-SGD iteration over a batch of 1024 synthetic L=128 images with
+r=10 eigenvolumes (the config of the GPU drop-in workload: ES kernel width 6 at tol 1e-6,
+upsampling 2, ML objective): on-the-fly points + bin sort, deapodise/pad + FFT3, ES
+interpolation with the fused projection epilogue, per-image Gram + FP64 solve, hand-written
+adjoint, compensated spreading, inverse FFT3, crop, Adam update.  Prints one JSON line.
+
+``--impl reference`` times the CPU port of the same step (oracle/cpu_step.py: float32 C
+loops with OpenMP + scipy FFT) on the host cores.
+"""
+
+import argparse
+import importlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "cov-SGD images/s (L=128,r=10)"
+WORKLOAD = ("cov-SGD step, GPU drop-in plain FP32 config: L=128, pixel 1.5 A, r=10 Gaussian-blob eigenvolumes, "
+            "batch 1024, uniform SO(3) poses, CTF 300 kV / Cs 2.7 mm / AC 0.1 / defocus U[1,3] um, SNR 0.05, "
+            "NUFFT upsampling 2, ES width 6 (tol 1e-6), ML objective + Fourier regulariser, Adam")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--L", type=int, default=128)
+    ap.add_argument("--rank", type=int, default=10)
+    ap.add_argument("--batch", type=int, default=1024)
+    ap.add_argument("--width", type=int, default=6)
+    ap.add_argument("--resident-batches", type=int, default=16)
+    ap.add_argument("--e2e-steps", type=int, default=0, help="0 = same as --steps")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--seed", type=int, default=2000)
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def cpu_baseline(args):
+    from oracle import cpu_step
+
+    threads = os.cpu_count()
+    # size the sample so the per-image part takes about cpu_seconds
+    _, probe = cpu_step.time_baseline(args.L, args.rank, args.batch, 2, args.width, real="float", threads=threads)
+    sample = int(max(2, min(256, args.cpu_seconds / max(probe["t_image_s"], 1e-6))))
+    ips, det = cpu_step.time_baseline(args.L, args.rank, args.batch, sample, args.width, real="float",
+                                      seed=args.seed, threads=threads)
+    return {"value": ips, "unit": "images/s", "cores": threads, "kind": "port",
+            "sample": (f"per-step part (pad + FFT3 + iFFT3 + crop, {det['t_step_s']:.2f} s) timed once and the "
+                       f"per-image part (points, ES interp, Gram/solve, adjoint, ES spread) on {sample} images "
+                       f"({det['t_image_s'] * 1e3:.1f} ms/image); images/s = {args.batch} / (t_step + "
+                       f"{args.batch} * t_image); float32 C + OpenMP, scipy.fft workers={threads}")}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    t0 = time.perf_counter()
+    cb = cpu_baseline(args)
+    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "images/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": args.batch / cb["value"] * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "global_batch": args.batch, "L": args.L, "rank": args.rank},
+            "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": "images/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "wall_s": time.perf_counter() - t0}
+    print(json.dumps(line), flush=True)
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = [r.split(",") for r in open(self.path).read().strip().splitlines() if r.count(",") >= 8]
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if "Active" in r[5 + i] and "Not" not in r[5 + i]})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def load_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+def load_traffic(kernel):
+    """dram bytes per launch of `kernel` recorded from an ncu capture in profiles/ (or None)."""
+    path = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        parts = line.split()
+        if len(parts) >= 2 and parts[0] == kernel:
+            try:
+                return float(parts[1])
+            except ValueError:
+                return None
+    return None
+
+
+def make_dataset(pkg, args, dev, n_images):
+    import torch
+
+    from importlib import import_module
+
+    syn = import_module("3dcovarestimation_gb300.synthetic")
+    g = torch.Generator(device=dev).manual_seed(args.seed)
+    L, r = args.L, args.rank
+    eig = syn.gaussian_blob_volumes(r, L, generator=g, device=dev)
+    eig = torch.linalg.qr(eig.reshape(r, -1).T)[0].T.reshape(r, L, L, L).contiguous()
+    sqrt_lam = torch.linspace(1.0, 0.3, r, device=dev) * L**1.5
+    rot = syn.uniform_rotations(n_images, generator=g, device=dev)
+    defocus = torch.rand((n_images,), generator=g, device=dev) * 2.0 + 1.0
+    ctf = syn.ctf_images(defocus, L, 1.5, device=dev)
+    images = torch.empty((n_images, L * L), dtype=torch.complex64, device=dev)
+    plan = pkg.NufftPlan((L,) * 3, batch_size=r, device=dev, width=args.width)
+    B = args.batch
+    for i in range(0, n_images, B):
+        plan.setrot(rot[i:i + B])
+        proj = pkg.vol_forward(eig, plan, ctf[i:i + B], fourier_domain=True)  # (b, r, L, L)
+        z = torch.randn((proj.shape[0], r, 1, 1), generator=g, device=dev) * sqrt_lam.reshape(1, r, 1, 1)
+        images[i:i + B] = (proj * z).sum(1).reshape(-1, L * L)
+    signal_var = float((images.abs() ** 2).mean())
+    noise_var = signal_var / 0.05
+    images += torch.randn(images.shape, generator=g, device=dev, dtype=torch.complex64) * (noise_var ** 0.5)
+    return images, rot, ctf.reshape(n_images, -1), noise_var
+
+
+def run_gb300(args):
+    import torch
+
+    rank, world, local = dist_env()
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+    pkg = importlib.import_module("3dcovarestimation_gb300")
+    from importlib import import_module
+
+    L, r, B = args.L, args.rank, args.batch
+    nb = max(2, args.resident_batches)
+    images, rot, ctf, noise_var = make_dataset(pkg, args, dev, nb * B)
+    images = images.reshape(nb, B, -1)
+    rot = rot.reshape(nb, B, 3, 3).contiguous()
+    ctf = ctf.reshape(nb, B, -1)
+    covar = pkg.Covar(L, r, upsampling_factor=2).to(dev)
+    step_fn = pkg.FusedCovarStep(L, r, "nufft", 2, width=args.width, device=dev)
+    covar.vectors.grad = torch.zeros_like(covar.vectors)
+    covar.log_sqrt_eigenvals.grad = torch.zeros_like(covar.log_sqrt_eigenvals)
+    groups = covar.grad_lr_factor()
+    for gp in groups:
+        gp["lr"] *= 1e-6 * B
+    opt = torch.optim.Adam(groups)
+    n = 2 * L
+    shell = torch.fft.fftshift(torch.fft.fftfreq(n, device=dev)) * n
+    rr = torch.sqrt(shell[:, None, None] ** 2 + shell[None, :, None] ** 2 + shell[None, None, :] ** 2)
+    fourier_reg = (1.0 + rr) ** 2 / (n**3)
+    reg_scale = 1.0 / 100000  # reg / N with N = 100,000 images
+    cost_acc = torch.zeros((), dtype=torch.float64, device=dev)
+
+    def grads_allreduce():
+        if world > 1:
+            import torch.distributed as dist
+
+            for t in (covar.vectors.grad, covar.log_sqrt_eigenvals.grad):
+                dist.all_reduce(t)
+                t /= world
+
+    def step(k, imgs=None, ctfs=None, rots=None):
+        b = (k * world + rank) % nb
+        step_fn.set_rotations(rot[b] if rots is None else rots)
+        c, _, _ = step_fn(covar.vectors.detach(), covar.log_sqrt_eigenvals.detach(),
+                          images[b] if imgs is None else imgs, ctf[b] if ctfs is None else ctfs, noise_var,
+                          reg_scale, fourier_reg, grad_vectors=covar.vectors.grad,
+                          grad_log_sqrt=covar.log_sqrt_eigenvals.grad)
+        grads_allreduce()
+        opt.step()
+        return c
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for k in range(args.warmup):
+        cost_acc += step(k)
+    barrier()
+    lib = pkg._lib
+    launches0 = lib.launch_count()
+    step_fn.plan.timing(True)
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        barrier()
+        e0.record(stream)
+        for k in range(args.steps):
+            cost_acc += step(args.warmup + k)
+        e1.record(stream)
+        barrier()
+    ms_total = e0.elapsed_time(e1)
+    launches = lib.launch_count() - launches0
+    phases = step_fn.plan.timing_read()
+    step_fn.plan.timing(False)
+    clocks = clk.summary()
+    ms_max = ms_total
+    if world > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([ms_total], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_max = float(t)
+    ms_step = ms_max / args.steps
+    value = world * B * args.steps / (ms_max / 1e3)
+
+    # end to end through the same C-ABI call with host (pinned) buffers: H2D of the batch's
+    # images, CTF and rotations + the step + D2H of the cost, every step
+    e2e_steps = args.e2e_steps or args.steps
+    nhost = min(nb, 4)
+    h_images = images[:nhost].cpu().pin_memory()
+    h_ctf = ctf[:nhost].cpu().pin_memory()
+    h_rot = rot[:nhost].cpu().pin_memory()
+    d_img = torch.empty_like(images[0])
+    d_ctf = torch.empty_like(ctf[0])
+    d_rot = torch.empty_like(rot[0])
+    h_cost = torch.zeros((e2e_steps,), dtype=torch.float64).pin_memory()
+    barrier()
+    t0 = time.perf_counter()
+    for k in range(e2e_steps):
+        j = k % nhost
+        d_img.copy_(h_images[j], non_blocking=True)
+        d_ctf.copy_(h_ctf[j], non_blocking=True)
+        d_rot.copy_(h_rot[j], non_blocking=True)
+        c = step(k, d_img, d_ctf, d_rot)
+        h_cost[k:k + 1].copy_(c.reshape(1), non_blocking=True)
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t)
+    e2e_value = world * B * e2e_steps / e2e_s
+    h2d = d_img.numel() * 8 + d_ctf.numel() * 4 + d_rot.numel() * 4
+
+    if rank != 0:
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.destroy_process_group()
+        return
+
+    # roofline of the dominant kernel (interp or spread), per step = per launch group
+    M = B * L * L
+    n3 = n**3
+    alg = {"interp": r * n3 * 8 + r * M * 8 + B * 9 * 4 + M * 4,
+           "spread": r * M * 8 + 2 * r * n3 * 8 + M * 4}
+    dom = max(("interp", "spread"), key=lambda k: phases[k][0])
+    dom_ms = phases[dom][0] / max(1, args.steps)
+    peak, peak_kind = load_peaks()
+    achieved = alg[dom] / (dom_ms / 1e3) / 1e9
+    flops = M * (args.width**3) * r * 4
+    sm_mhz = clocks.get("sm_mhz") or 1900.0
+    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+    kernel_name = "interp_kernel" if dom == "interp" else "spread_kernel"
+    line = {
+        "metric": METRIC, "value": value, "unit": "images/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "global_batch": B * world, "L": L, "rank": r, "upsample": 2,
+                   "es_width": args.width, "resident_images": nb * B,
+                   "l2": "inputs larger than L2: each step reads a distinct resident 1024-image batch "
+                         "(134 MB images + 67 MB CTF) and 1.34 GB fine grids",
+                   "parallelism": f"dp{world}", "seed": args.seed},
+        "roofline": {"bound": "hbm", "kernel": kernel_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind, "traffic": load_traffic(kernel_name),
+                     "algorithmic_bytes_per_launch": alg[dom], "ms_per_launch": dom_ms,
+                     "fp32_tflops": flops / (phases["interp"][0] / args.steps / 1e3) / 1e12,
+                     "fp32_frac_interp": flops / (phases["interp"][0] / args.steps / 1e3) / 1e12 / fp32_peak},
+        "e2e": {"value": e2e_value, "unit": "images/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 8},
+        "gpu_launches": launches,
+        "clocks": clocks,
+        "phases_ms_per_step": {k: v[0] / args.steps for k, v in phases.items() if v[1]},
+        "final_cost": float(cost_acc) / (args.warmup + args.steps),
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(args)
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

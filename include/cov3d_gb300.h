@@ -1,0 +1,228 @@
+/*
+ * cov3d_gb300.h -- C ABI of the GB300-native COV3D hot path.
+ *
+ * Plain C: every argument is a scalar, a plain struct of scalars, or a raw pointer.
+ * Pointers named d_* are device pointers; the library never allocates or frees caller
+ * memory.  Every entry point returns a cov3d_status code (0 on success); the text of
+ * the last error of the calling thread is available from cov3d_last_error().
+ *
+ * Geometry and conventions (identical to the reference COV3D package):
+ *  - volumes are L^3, C order, indexed [axis0][axis1][axis2] (axis 2 fastest);
+ *  - images are L^2 pixels, row-major; pixel p of image b is nonuniform point b*L^2 + p;
+ *  - a point's coordinate row d pairs with volume axis d (reference nufft_plan.py:326,335);
+ *  - the fine (upsampled) Fourier grid has n = upsample*L points per axis.  A "centered"
+ *    grid holds frequency 2*pi*(m - n/2)/n at index m (reference projection_funcs.py:148-165);
+ *    an "fft-native" grid is the raw FFT output, index s = (m - n/2) mod n.
+ *
+ * Kernels (interpolation / spreading weights):
+ *  - COV3D_KERNEL_ES:      exponential of semicircle, width w, periodic wrap (the exact
+ *                          NUFFT of reference nufft_plan.py:245-392, cuFINUFFT semantics);
+ *  - COV3D_KERNEL_LINEAR:  trilinear with zero padding, align_corners (grid_sample, the
+ *                          reference's NufftPlanDiscretized mode="bilinear", nufft_plan.py:67-242);
+ *  - COV3D_KERNEL_NEAREST: nearest neighbour with zero padding (mode="nearest").
+ *
+ * Threading: a plan is not thread safe; all work is enqueued on the plan's stream.
+ */
+#ifndef COV3D_GB300_H
+#define COV3D_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define COV3D_ABI_VERSION 1
+
+typedef enum {
+  COV3D_OK = 0,
+  COV3D_EINVAL = 1,     /* bad argument: shape, pointer, option (reference: assert / ValueError) */
+  COV3D_ENOMEM = 2,     /* device allocation failed */
+  COV3D_ECUDA = 3,      /* CUDA runtime error */
+  COV3D_ECUFFT = 4,     /* cuFFT error */
+  COV3D_ENONFINITE = 5, /* non-finite value detected in an input or a reduction */
+  COV3D_EMAXITER = 6,   /* iterative solve stopped at maxiter without reaching rtol */
+  COV3D_ESTATE = 7      /* call out of order (e.g. execute before setpts) */
+} cov3d_status;
+
+typedef enum { COV3D_KERNEL_ES = 0, COV3D_KERNEL_LINEAR = 1, COV3D_KERNEL_NEAREST = 2 } cov3d_kernel;
+
+typedef enum { COV3D_GRID_CENTERED = 0, COV3D_GRID_FFT_NATIVE = 1 } cov3d_grid_order;
+
+typedef struct cov3d_plan cov3d_plan;
+
+/* Plan options.  Replaces the keyword arguments the reference passes to cuFINUFFT / FINUFFT
+ * (nufft_plan.py:296-316: eps, gpu_method, gpu_sort) and to NufftPlanDiscretized
+ * (nufft_plan.py:84-92: upsample_factor, mode). */
+typedef struct {
+  int kernel;        /* cov3d_kernel */
+  int upsample;      /* sigma; fine grid n = upsample * L (>= 1) */
+  int width;         /* ES width w in [2, 16]; 0 = from eps: ceil(-log10(eps/10)) */
+  double beta;       /* ES shape; 0 = 0.97*pi*(1 - 1/(2 sigma))*w */
+  int compensated;   /* 1 = TwoSum-compensated FP32 spreading in shared memory */
+  int bin_size;      /* spatial bin edge in fine-grid cells for point sorting; 0 = 8 */
+  void *stream;      /* cudaStream_t for all work of this plan (NULL = legacy default) */
+} cov3d_opts;
+
+/* Layout of a complex64 fine grid in device memory.  Element (cell, channel) lives at
+ * base + cell_index*cell_stride + channel*chan_stride (strides in complex elements), where
+ * cell_index = (s0*n + s1)*n + s2 and s_d is the storage coordinate given by `order`. */
+typedef struct {
+  int order;            /* cov3d_grid_order */
+  int64_t cell_stride;  /* 1 for channels-first (r, n, n, n); r for channels-last (n, n, n, r) */
+  int64_t chan_stride;  /* n^3 for channels-first; 1 for channels-last */
+} cov3d_grid_layout;
+
+/* Epilogue / prologue flags of the projection operators (reference projection_funcs.py:346-399). */
+#define COV3D_APPLY_NYQUIST 1 /* zero pixel row 0 and column 0 when L is even */
+#define COV3D_APPLY_CTF 2     /* multiply by a per-pixel real filter (B, L*L) */
+
+/* ------------------------------------------------------------------ library */
+
+int cov3d_abi_version(void);
+/* Copies the calling thread's last error message (NUL terminated, truncated to len). */
+int cov3d_last_error(char *buf, int len);
+/* Static description of a status code. */
+const char *cov3d_status_string(int status);
+
+/* ------------------------------------------------------------------ plans
+ * Mirrors the cuFINUFFT plan lifecycle the reference binds through cufinufft.Plan:
+ * construction nufft_plan.py:288-316, setpts :318-336, execute :338-392, destruction on GC.
+ */
+
+/* Create a plan for L^3 volumes.  eps is the requested accuracy for the ES kernel (the
+ * reference clamps it to max(eps, 10*machine eps), nufft_plan.py:286).  n_trans is the number
+ * of volumes transformed together (reference batch_size = rank r); it sizes the fine-grid
+ * workspace and cuFFT plan used by the type-1/type-2 and cost entry points. */
+int cov3d_plan_create(int L, int n_trans, double eps, const cov3d_opts *opts, cov3d_plan **plan);
+int cov3d_plan_destroy(cov3d_plan *plan);
+int cov3d_plan_set_stream(cov3d_plan *plan, void *stream);
+/* Reports n (fine grid edge), width and beta actually used. */
+int cov3d_plan_info(const cov3d_plan *plan, int *n, int *width, double *beta);
+
+/* Set nonuniform points.  d_pts holds n_images blocks of 3 rows of points_L^2 float32
+ * frequencies in radians, i.e. the reference's (N, 3, L^2) pts_rot tensor
+ * (NufftPlan.setpts nufft_plan.py:318-336; NufftPlanDiscretized.setpts :94-118).
+ * img_stride / row_stride are element strides (3*L^2 and L^2 for a contiguous tensor).
+ * wrap = 1 wraps to [-pi, pi) as NufftPlan.setpts does (:327).  The points are copied. */
+int cov3d_setpts(cov3d_plan *plan, const float *d_pts, int64_t n_images, int points_L, int64_t img_stride,
+                 int64_t row_stride, int wrap);
+
+/* Set points from per-image rotation matrices d_rot (n_images, 3, 3) row-major float32:
+ * the points of image b are flip_axis0(R_b @ pi*[x, y, 0]) wrapped to [-pi, pi), generated on
+ * the fly (reference PoseModule.forward poses.py:237-269, CovarDataset.compute_pts_rot
+ * dataset.py:146-164).  Nothing of size (N, 3, L^2) is materialised. */
+int cov3d_setrot(cov3d_plan *plan, const float *d_rot, int64_t n_images, int points_L);
+
+/* Interpolate nchan channels of a complex fine grid at the plan's points (type-2 spreading
+ * step; the reference's grid_sample forward nufft_plan.py:120-169 for LINEAR/NEAREST).
+ * Output element (point, channel) goes to d_out[point*out_point_stride + ch*out_chan_stride].
+ * flags: COV3D_APPLY_NYQUIST / COV3D_APPLY_CTF with d_ctf (n_images, L^2); every output is
+ * multiplied by `scale` (vol_forward's 1/L, projection_funcs.py:370). */
+int cov3d_interp(cov3d_plan *plan, const void *d_grid, const cov3d_grid_layout *layout, int nchan, void *d_out,
+                 int64_t out_point_stride, int64_t out_chan_stride, const float *d_ctf, int flags, float scale);
+
+/* Exact adjoint of cov3d_interp: spread nchan channels of point values into a fine grid
+ * (the reference's grid_sample backward, execute_adjoint nufft_plan.py:171-200).  The grid is
+ * zeroed first unless accumulate != 0.  flags / scale as in cov3d_interp (im_backward's
+ * CTF multiply, Nyquist zeroing and 1/L, projection_funcs.py:385-399). */
+int cov3d_spread(cov3d_plan *plan, const void *d_values, int64_t in_point_stride, int64_t in_chan_stride,
+                 int nchan, const float *d_ctf, int flags, float scale, void *d_grid, const cov3d_grid_layout *layout,
+                 int accumulate);
+
+/* Per-image adjoint without the sum over images (execute_adjoint_unaggregated,
+ * nufft_plan.py:202-242): d_grids is (n_images, n, n, n) centered complex64, one channel. */
+int cov3d_spread_unaggregated(cov3d_plan *plan, const void *d_values, int64_t in_point_stride, const float *d_ctf,
+                              int flags, float scale, void *d_grids);
+
+/* Type-2 NUFFT of nchan <= n_trans spatial volumes (real float32 if d_vol_real != NULL, else
+ * complex64 d_vol_complex), each L^3: deapodise + zero-pad + FFT + interpolate.  Output is
+ * (nchan, n_points) complex64 (NufftPlan.execute_forward, nufft_plan.py:338-364). */
+int cov3d_execute_type2(cov3d_plan *plan, const float *d_vol_real, const void *d_vol_complex, int nchan, void *d_out);
+
+/* Type-1 NUFFT (exact adjoint of type 2): (nchan, n_points) complex64 -> (nchan, L^3)
+ * complex64 (NufftPlan.execute_adjoint, nufft_plan.py:366-392). */
+int cov3d_execute_type1(cov3d_plan *plan, const void *d_values, int nchan, void *d_vol_out);
+
+/* Deapodisation factors of the plan's kernel on the L^3 voxel grid, float32 (the ES
+ * analogue of VolumeBase.init_grid_correction, covar.py:45-65). */
+int cov3d_grid_correction(const cov3d_plan *plan, float *d_out);
+
+/* ------------------------------------------------------------------ covariance SGD
+ * One fused evaluation of the covariance cost and its exact gradient with respect to the
+ * Covar parameters (vectors (r, L^3), log_sqrt_eigenvals (r)), replacing
+ * Covar.get_vectors_fourier_domain (covar.py:440-446) + cost_maximum_liklihood_fourier_domain
+ * (covar_sgd.py:1350-1399) / cost_fourier_domain (:1290-1347) + autograd backward as driven
+ * by CovarTrainer.run_batch (covar_sgd.py:199-229).  The gradient is the hand-written adjoint:
+ * per-image r x r Gram + FP64 Hermitian solve, then backprojection of the cost's derivative
+ * with respect to the projections through the exact adjoint of the interpolation.
+ * Points must be set (setpts/setrot) for n_images = B images of L^2 pixels. */
+typedef struct {
+  int objective;            /* 0 = maximum likelihood (default objective), 1 = least squares */
+  int rank;                 /* r <= n_trans */
+  const float *d_vectors;   /* (r, L^3) float32 */
+  const float *d_log_sqrt;  /* (r) float32 */
+  const void *d_images;     /* (B, L^2) complex64, Fourier domain (centered) */
+  const float *d_ctf;       /* (B, L^2) float32 or NULL */
+  double noise_var;         /* Fourier-domain noise variance (dataset noise_var * L^2) */
+  double reg_scale;         /* reg / N (covar_sgd.py:357) */
+  const float *d_fourier_reg; /* (n^3) float32 centered, or NULL (ML regulariser :1373-1376) */
+  int use_grid_correction;  /* divide by the kernel's deapodisation factors (init_grid_correction) */
+  double *d_cost;           /* optional device scalar receiving the cost (no host sync needed) */
+} cov3d_cost_args;
+
+/* Outputs: d_grad_vectors (r, L^3) float32, d_grad_log_sqrt (r) float32, optional
+ * d_per_image_cost (B) float64 (the mean_aggregate=False data term), optional args->d_cost.
+ * When `cost` (host) is not NULL the call synchronises the plan's stream and stores the
+ * cost there; otherwise it returns without waiting for the GPU. */
+int cov3d_covar_cost_grad(cov3d_plan *plan, const cov3d_cost_args *args, double *cost, float *d_grad_vectors,
+                          float *d_grad_log_sqrt, double *d_per_image_cost);
+
+/* ------------------------------------------------------------------ instrumentation
+ * No reference counterpart beyond its time.time() epoch timing (covar_sgd.py:386-389). */
+
+/* Number of kernels this library has launched since it was loaded (all threads). */
+long long cov3d_launch_count(void);
+/* Name of timing phase k (0 <= k < COV3D_NUM_PHASES), or NULL. */
+const char *cov3d_phase_name(int phase);
+#define COV3D_NUM_PHASES 11
+/* Enable (1) or disable (0) CUDA-event timing of the plan's phases; clears recorded events. */
+int cov3d_plan_timing(cov3d_plan *plan, int enable);
+/* Synchronise the plan's stream, sum the recorded durations per phase into ms[n_phases] and
+ * counts[n_phases] (n_phases >= COV3D_NUM_PHASES), and clear the record. */
+int cov3d_plan_timing_read(cov3d_plan *plan, double *ms, int *counts, int n_phases);
+
+/* ------------------------------------------------------------------ per-image r x r algebra
+ * Plan-independent building blocks of the covariance cost, its adjoint and the latent-MAP
+ * solve.  Image b's projections are r complex64 channels over P pixels: element (p, i) at
+ * d_q[b*img_stride + p*point_stride + i*chan_stride]; its Fourier image is d_images[b*P + p]. */
+
+/* gram (n_images, r, r) = conj(Q)^T Q, h (n_images, r) = conj(Q)^T y, yy (n_images) = |y|^2:
+ * the batched products of compute_latentMAP_batch (wiener_coords.py:192-194) and of
+ * raw_cost_fourier_domain (covar_sgd.py:1327-1328).  r <= 32. */
+int cov3d_gram(void *stream, int n_images, int P, int r, const void *d_q, int64_t img_stride, int64_t point_stride,
+               int64_t chan_stride, const void *d_images, void *d_gram, void *d_h, float *d_yy);
+
+/* Per-image FP64 solve of m = gram/noise_var + Linv (Linv = d_linv (r, r) float64, or the
+ * identity when NULL), b = h/noise_var, z = m^-1 b (compute_latentMAP_batch, wiener_coords.py:
+ * 168-203).  objective 0 (ML): cost_b = cscale*(-Re(b^H z) + logdet m)/2 and the adjoint
+ * coefficients C = wscale*(conj(m^-1) + conj(z) z^T)/(2 noise_var), u = -wscale*conj(z)/(2
+ * noise_var).  objective 1 (LS): cost_b = cscale*(-2|h|^2 + ||gram||_F^2 + 2 noise_var tr gram),
+ * C = wscale*(2 conj(gram) + 2 noise_var I), u = -2 wscale conj(h).  Every output pointer may
+ * be NULL.  d_bad is set to 1 when some m is not positive definite. */
+int cov3d_cost_solve(void *stream, int n_images, int r, int objective, const void *d_gram, const void *d_h,
+                     double noise_var, const double *d_linv, double wscale, double cscale, void *d_C, void *d_u,
+                     double *d_cost_b, double *d_cost_sum, void *d_z, void *d_m, int *d_bad);
+
+/* W = C Q + u y per image and pixel (the derivative of the per-image cost with respect to
+ * conj(Q)); W may alias Q when the strides are equal. */
+int cov3d_wpass(void *stream, int n_images, int P, int r, const void *d_q, int64_t img_stride, int64_t point_stride,
+                int64_t chan_stride, const void *d_images, const void *d_C, const void *d_u, void *d_w,
+                int64_t w_img_stride, int64_t w_point_stride, int64_t w_chan_stride);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* COV3D_GB300_H */

@@ -1,0 +1,268 @@
+"""Generate the golden fixtures under ``tests/golden/`` by running the reference COV3D code
+(pure PyTorch, CPU, float64) on small seeded inputs.
+
+Run in the development container only (the reference tree is not present on GPU machines):
+
+    python tests/golden/make_golden.py [/path/to/reference]
+
+The reference is imported unmodified through ``ref_shim`` (placeholder modules for its
+unused third-party dependencies).  Every fixture stores its inputs next to the reference's
+outputs, so the tests never need the reference itself.
+
+Cases (reference file:line of the function that produced each output):
+
+* ``poses.npz``          rotvec_to_rotmat (poses.py:44-67), PoseModule.forward
+                         (poses.py:237-269), offset_to_phase_shift (poses.py:92-125)
+* ``disc_*.npz``         NufftPlanDiscretized.setpts/execute_forward/execute_adjoint/
+                         execute_adjoint_unaggregated (nufft_plan.py:94-242), vol_forward /
+                         im_backward (projection_funcs.py:321-399)
+* ``cost_*.npz``         cost_maximum_liklihood_fourier_domain and cost_fourier_domain
+                         (covar_sgd.py:1290-1399) through Covar.get_vectors_fourier_domain
+                         (covar.py:440-446) with autograd gradients
+* ``latent_*.npz``       compute_latentMAP_batch (wiener_coords.py:168-203)
+* ``cg_*.npz``           regularize_lhs + correct_upsampling_padding +
+                         complex_conjugate_gradient (mean.py:43-142)
+* ``mean_*.npz``         reconstruct_mean (mean.py:145-259), whole pipeline
+"""
+
+import io
+import logging
+import os
+import re
+import sys
+
+import numpy as np
+import torch
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+
+sys.path.insert(0, HERE)
+import ref_shim  # noqa: E402
+
+ref_shim.install(REF)
+
+from cov3d import covar_sgd, mean, nufft_plan, poses, projection_funcs, wiener_coords  # noqa: E402
+from cov3d.covar import Covar  # noqa: E402
+
+torch.set_default_dtype(torch.float64)
+
+
+def save(name, **arrays):
+    path = os.path.join(HERE, name)
+    np.savez_compressed(path, **{k: np.asarray(v) for k, v in arrays.items()})
+    print(f"wrote {name}: {os.path.getsize(path) / 1024:.1f} KiB")
+
+
+def random_rotvecs(rng, n):
+    q = rng.standard_normal((n, 4))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    q[q[:, 0] < 0] *= -1
+    angle = 2 * np.arccos(np.clip(q[:, 0], -1, 1))
+    axis = q[:, 1:] / np.maximum(np.linalg.norm(q[:, 1:], axis=1, keepdims=True), 1e-12)
+    return (axis * angle[:, None]).astype(np.float32)
+
+
+def c32(rng, shape):
+    return (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)).astype(np.complex64)
+
+
+def ref_points(rotvecs, offsets, L):
+    pose = poses.PoseModule(torch.tensor(rotvecs, dtype=torch.float64), torch.tensor(offsets, dtype=torch.float64), L,
+                            dtype=torch.float64)
+    with torch.no_grad():
+        pts, phase = pose(torch.arange(len(rotvecs)))
+    return pts, phase
+
+
+def case_poses():
+    rng = np.random.default_rng(11)
+    out = {}
+    for L in (12, 15):
+        n = 7
+        rotvecs = random_rotvecs(rng, n)
+        offsets = (rng.uniform(-3, 3, (n, 2))).astype(np.float32)
+        rotmat = poses.rotvec_to_rotmat(torch.tensor(rotvecs, dtype=torch.float64))
+        pts, phase = ref_points(rotvecs, offsets, L)
+        out.update({f"L{L}_rotvecs": rotvecs, f"L{L}_offsets": offsets, f"L{L}_rotmat": rotmat.numpy(),
+                    f"L{L}_pts": pts.numpy(), f"L{L}_phase": phase.numpy()})
+    save("poses.npz", **out)
+
+
+def case_disc(L, us, mode, n_img, chans, seed, unaggregated=False):
+    rng = np.random.default_rng(seed)
+    n = L * us
+    rotvecs = random_rotvecs(rng, n_img)
+    pts, _ = ref_points(rotvecs, np.zeros((n_img, 2), np.float32), L)
+    vol = c32(rng, (chans, n, n, n))
+    sig = c32(rng, (n_img, L, L))
+    filters = rng.uniform(0.2, 1.5, (n_img, L, L)).astype(np.float32)
+
+    plan = nufft_plan.NufftPlanDiscretized((L,) * 3, upsample_factor=us, mode=mode)
+    plan.setpts(pts)
+    vol_t = torch.tensor(vol).to(torch.complex128)
+    sig_t = torch.tensor(sig).to(torch.complex128)
+    filt_t = torch.tensor(filters, dtype=torch.float64)
+    fwd = plan.execute_forward(vol_t)
+    adj = plan.execute_adjoint(sig_t)
+    vf = projection_funcs.vol_forward(vol_t, plan, filt_t, fourier_domain=True)
+    ib = projection_funcs.im_backward(sig_t, plan, filt_t, fourier_domain=True)
+    arrays = dict(L=L, us=us, pts=pts.numpy(), rotvecs=rotvecs, vol=vol, sig=sig, filters=filters,
+                  fwd=fwd.numpy(), adj=adj.numpy(), vol_forward=vf.numpy(), im_backward=ib.numpy())
+    if unaggregated:
+        arrays["adj_unagg"] = plan.execute_adjoint_unaggregated(sig_t).numpy()
+    save(f"disc_{mode}_L{L}_us{us}.npz", **arrays)
+
+
+def case_cost(L=10, r=3, B=6, us=2, seed=5):
+    rng = np.random.default_rng(seed)
+    n = L * us
+    vectors = rng.standard_normal((r, L, L, L)).astype(np.float32) * 0.1
+    rotvecs = random_rotvecs(rng, B)
+    pts, _ = ref_points(rotvecs, np.zeros((B, 2), np.float32), L)
+    images = c32(rng, (B, L, L)) * np.float32(3.0)
+    filters = rng.uniform(0.2, 1.5, (B, L, L)).astype(np.float32)
+    fourier_reg = rng.uniform(0.5, 2.0, (n, n, n)).astype(np.float32)
+    noise_var = 7.5
+    reg_scale = 0.3
+
+    out = dict(L=L, r=r, us=us, vectors=vectors, rotvecs=rotvecs, pts=pts.numpy(), images=images, filters=filters,
+               fourier_reg=fourier_reg, noise_var=noise_var, reg_scale=reg_scale)
+    plan = nufft_plan.NufftPlanDiscretized((L,) * 3, upsample_factor=us, mode="bilinear")
+    plan.setpts(pts)
+    ims = torch.tensor(images).to(torch.complex128)
+    filt = torch.tensor(filters, dtype=torch.float64)
+    freg = torch.tensor(fourier_reg, dtype=torch.float64)
+    for name, fn in (("ml", covar_sgd.cost_maximum_liklihood_fourier_domain), ("ls", covar_sgd.cost_fourier_domain)):
+        for with_reg in (False, True):
+            covar = Covar(L, r, dtype=torch.float64, upsampling_factor=us, vectors=torch.tensor(vectors, dtype=torch.float64))
+            covar.init_grid_correction("bilinear")
+            vols = covar.get_vectors_fourier_domain()
+            kw = dict(reg_scale=reg_scale, fourier_reg=freg) if with_reg else {}
+            cost = fn(vols, ims, plan, filt, noise_var, **kw)
+            cost.backward()
+            tag = f"{name}{'_reg' if with_reg else ''}"
+            out[f"{tag}_cost"] = cost.detach().numpy()
+            out[f"{tag}_grad_vectors"] = covar.vectors.grad.numpy()
+            out[f"{tag}_grad_logsqrt"] = covar.log_sqrt_eigenvals.grad.numpy()
+            # per-image (unaggregated) data term
+            covar.zero_grad()
+            vols = covar.get_vectors_fourier_domain()
+            per_img = fn(vols, ims, plan, filt, noise_var, mean_aggregate=False)
+            out[f"{tag}_per_image"] = per_img.detach().numpy()
+    out["log_sqrt_eigenvals"] = covar.log_sqrt_eigenvals.detach().numpy()
+    out["vectors_normalised"] = covar.vectors.detach().numpy()
+    out["grid_correction"] = covar.grid_correction.numpy()
+    save(f"cost_L{L}_r{r}.npz", **out)
+
+
+def case_latent(L=10, r=3, B=9, seed=9):
+    rng = np.random.default_rng(seed)
+    images = c32(rng, (B, L, L))
+    eig = c32(rng, (B, r, L, L)) * np.float32(0.5)
+    lam = np.diag(rng.uniform(0.5, 3.0, r))
+    lam_inv = np.linalg.inv(lam + 1e-6 * np.eye(r))
+    noise_var = 2.5
+    z, m, b = wiener_coords.compute_latentMAP_batch(
+        torch.tensor(images).to(torch.complex128), torch.tensor(eig).to(torch.complex128), noise_var,
+        torch.tensor(lam_inv).to(torch.complex128))
+    zr, mr, br = wiener_coords.compute_latentMAP_batch(
+        torch.tensor(images.real.astype(np.float64)), torch.tensor(eig.real.astype(np.float64)), noise_var,
+        torch.tensor(lam_inv))
+    z0, m0, b0 = wiener_coords.compute_latentMAP_batch(
+        torch.tensor(images).to(torch.complex128), torch.tensor(eig).to(torch.complex128), noise_var)
+    save(f"latent_L{L}_r{r}.npz", images=images, eigen_forward=eig, eigenvals=np.diag(lam), eigenvals_inv=lam_inv,
+         noise_var=noise_var, z=z.numpy(), m=m.numpy(), b=b.numpy(), z_real=zr.numpy(), m_real=mr.numpy(),
+         b_real=br.numpy(), z_identity=z0.numpy(), m_identity=m0.numpy(), b_identity=b0.numpy())
+
+
+class _CGCounter(logging.Handler):
+    def __init__(self):
+        super().__init__()
+        self.iters = []
+
+    def emit(self, record):
+        m = re.search(r"CG converged in (\d+) iterations", record.getMessage())
+        if m:
+            self.iters.append(int(m.group(1)))
+
+
+def case_cg(L=8, us=2, seed=3):
+    rng = np.random.default_rng(seed)
+    n = L * us
+    lhs = (rng.uniform(0.0, 4.0, (n, n, n)) ** 2).astype(np.float32)
+    lhs[rng.uniform(size=lhs.shape) < 0.05] = 0.0  # unobserved frequencies, exercised by regularize_lhs's floor
+    rhs = c32(rng, (n, n, n))
+    lhs_t = torch.tensor(lhs).to(torch.complex128)
+    rhs_t = torch.tensor(rhs).to(torch.complex128)
+    reg_lhs = mean.regularize_lhs(lhs_t)
+    init = projection_funcs.centered_ifft3(rhs_t / reg_lhs, cropping_size=(L,) * 3).real
+    handler = _CGCounter()
+    mean.logger.addHandler(handler)
+    mean.logger.setLevel(logging.DEBUG)
+    x = mean.correct_upsampling_padding(reg_lhs, rhs_t, init, L, us)
+    mean.logger.removeHandler(handler)
+    b = projection_funcs.centered_ifft3(rhs_t, cropping_size=(L,) * 3)
+    save(f"cg_L{L}.npz", L=L, us=us, lhs=lhs, rhs=rhs, reg_lhs=reg_lhs.numpy(), init=init.numpy(), x=x.numpy(),
+         b=b.numpy(), iters=np.array(handler.iters))
+
+
+class _MeanDataset(torch.utils.data.Dataset):
+    """Minimal stand-in for CovarDataset with the attributes reconstruct_mean reads."""
+
+    def __init__(self, images, pts, filters, offsets, contrasts, L):
+        self.images = images
+        self.pts_rot = pts
+        self.filters = filters
+        self.offsets = offsets
+        self.contrasts = contrasts
+        self.resolution = L
+        self._in_spatial_domain = False
+        self.dtype = images.real.dtype
+        self.noise_var = 1.0
+
+    def __len__(self):
+        return len(self.images)
+
+    def __getitem__(self, idx):
+        return self.images[idx], self.pts_rot[idx], self.filters[idx], idx
+
+    def to_fourier_domain(self):
+        pass
+
+    def to_spatial_domain(self):
+        pass
+
+
+def case_mean(L=10, us=2, N=96, seed=21):
+    rng = np.random.default_rng(seed)
+    rotvecs = random_rotvecs(rng, N)
+    offsets = rng.uniform(-2, 2, (N, 2)).astype(np.float32)
+    contrasts = rng.uniform(0.7, 1.3, N).astype(np.float32)
+    pts, _ = ref_points(rotvecs, np.zeros((N, 2), np.float32), L)
+    images = c32(rng, (N, L, L))
+    filters = rng.uniform(0.2, 1.5, (N, L, L)).astype(np.float32)
+    ds = _MeanDataset(torch.tensor(images).to(torch.complex128), pts, torch.tensor(filters, dtype=torch.float64),
+                      torch.tensor(offsets, dtype=torch.float64), torch.tensor(contrasts, dtype=torch.float64), L)
+    loader = torch.utils.data.DataLoader(ds, batch_size=32, shuffle=False)
+    handler = _CGCounter()
+    mean.logger.addHandler(handler)
+    mean.logger.setLevel(logging.DEBUG)
+    vol, rhs, lhs = mean.reconstruct_mean(loader, upsampling_factor=us, return_lhs_rhs=True)
+    mean.logger.removeHandler(handler)
+    save(f"mean_L{L}.npz", L=L, us=us, rotvecs=rotvecs, offsets=offsets, contrasts=contrasts, pts=pts.numpy(),
+         images=images, filters=filters, volume=vol.numpy(), rhs=rhs.numpy(), lhs=lhs.numpy(),
+         iters=np.array(handler.iters))
+
+
+if __name__ == "__main__":
+    case_poses()
+    case_disc(10, 2, "bilinear", 5, 2, seed=1)
+    case_disc(10, 2, "nearest", 5, 2, seed=2)
+    case_disc(9, 2, "bilinear", 4, 2, seed=3)
+    case_disc(10, 1, "nearest", 4, 1, seed=4, unaggregated=True)
+    case_disc(7, 1, "bilinear", 3, 1, seed=6, unaggregated=True)
+    case_cost()
+    case_latent()
+    case_cg()
+    case_mean()

@@ -1,0 +1,127 @@
+"""Import shim that lets the reference COV3D package (pure Python / PyTorch) import on a
+machine without its heavy third-party dependencies.
+
+Only used by ``make_golden.py`` in the development container, where the reference
+source tree is mounted read-only.  It is never imported by the product, the GPU tests,
+``smoke()`` or ``bench.py``.
+
+What it does:
+
+* serves placeholder modules for packages that the reference imports at module scope
+  but that the discretized hot path never calls (ASPIRE, cuFINUFFT/FINUFFT, cryoDRGN,
+  mrcfile, pandas, starfile, colorlog, matplotlib, umap, seaborn, recovar);
+* restates ``aspire.utils.grid_2d`` / ``grid_3d`` from their mathematical definition
+  (normalised grid ``ceil(arange(-n/2, n/2)) / (n/2)``), because ``poses.py:197-215``,
+  ``fsc_utils.py:43-47`` and ``mean.py:412-414`` do call them.
+"""
+
+import importlib.abc
+import importlib.machinery
+import sys
+import types
+
+import numpy as np
+
+STUB_ROOTS = {
+    "aspire",
+    "cufinufft",
+    "finufft",
+    "cryodrgn",
+    "mrcfile",
+    "pandas",
+    "starfile",
+    "colorlog",
+    "matplotlib",
+    "umap",
+    "seaborn",
+    "recovar",
+}
+
+
+def _grid_1d_values(n, shifted, normalized, dtype):
+    grid = np.ceil(np.arange(-n / 2, n / 2, dtype=dtype))
+    if shifted and n % 2 == 0:
+        grid = np.arange(-n / 2 + 1 / 2, n / 2 + 1 / 2, dtype=dtype)
+    if normalized:
+        if shifted and n % 2 == 0:
+            grid = grid / (n / 2 - 1 / 2)
+        else:
+            grid = grid / (n / 2)
+    return grid.astype(dtype)
+
+
+def grid_2d(n, shifted=False, normalized=True, indexing="yx", dtype=np.float32):
+    g = _grid_1d_values(n, shifted, normalized, dtype)
+    a, b = np.meshgrid(g, g, indexing="ij")
+    if indexing == "yx":
+        y, x = a, b
+    else:
+        x, y = a, b
+    r = np.sqrt(x * x + y * y)
+    phi = np.arctan2(y, x)
+    return {"x": x, "y": y, "r": r, "phi": phi}
+
+
+def grid_3d(n, shifted=False, normalized=True, indexing="zyx", dtype=np.float32):
+    g = _grid_1d_values(n, shifted, normalized, dtype)
+    a, b, c = np.meshgrid(g, g, g, indexing="ij")
+    if indexing == "zyx":
+        z, y, x = a, b, c
+    else:
+        x, y, z = a, b, c
+    r = np.sqrt(x * x + y * y + z * z)
+    phi = np.arctan2(y, x)
+    theta = np.arccos(np.divide(z, r, out=np.zeros_like(r), where=r > 0))
+    return {"x": x, "y": y, "z": z, "r": r, "phi": phi, "theta": theta}
+
+
+class _Placeholder:
+    """Stands in for any class or function of a missing package."""
+
+    def __init__(self, *args, **kwargs):
+        pass
+
+    def __call__(self, *args, **kwargs):
+        return _Placeholder()
+
+    def __getattr__(self, name):
+        return _Placeholder()
+
+    def __class_getitem__(cls, item):
+        return cls
+
+
+class _StubModule(types.ModuleType):
+    def __getattr__(self, name):
+        if name.startswith("__"):
+            raise AttributeError(name)
+        placeholder = type(name, (_Placeholder,), {})
+        setattr(self, name, placeholder)
+        return placeholder
+
+
+class _StubLoader(importlib.abc.Loader):
+    def create_module(self, spec):
+        mod = _StubModule(spec.name)
+        mod.__path__ = []
+        return mod
+
+    def exec_module(self, module):
+        if module.__name__ == "aspire.utils":
+            module.grid_2d = grid_2d
+            module.grid_3d = grid_3d
+
+
+class _StubFinder(importlib.abc.MetaPathFinder):
+    def find_spec(self, fullname, path, target=None):
+        if fullname.split(".")[0] in STUB_ROOTS:
+            return importlib.machinery.ModuleSpec(fullname, _StubLoader(), is_package=True)
+        return None
+
+
+def install(reference_root):
+    """Put the stub finder first on ``sys.meta_path`` and the reference on ``sys.path``."""
+    if not any(isinstance(f, _StubFinder) for f in sys.meta_path):
+        sys.meta_path.insert(0, _StubFinder())
+    if reference_root not in sys.path:
+        sys.path.insert(0, reference_root)

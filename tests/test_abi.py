@@ -1,0 +1,47 @@
+"""The C-ABI library loads, exports every entry point declared in include/*.h, and rejects bad
+arguments on the host (no GPU work)."""
+import ctypes
+import glob
+import os
+import re
+
+from conftest import ROOT
+
+
+def declared_symbols():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        text = open(h).read()
+        names |= set(re.findall(r"^\s*(?:const\s+)?(?:long\s+long|\w+)\s*\*?\s*(cov3d_\w+)\s*\(", text, flags=re.M))
+    return sorted(names)
+
+
+def test_header_declares_entry_points():
+    names = declared_symbols()
+    assert "cov3d_plan_create" in names and "cov3d_covar_cost_grad" in names and len(names) >= 15
+
+
+def test_library_exports_every_declared_symbol(pkg):
+    lib = ctypes.CDLL(pkg.LIB_PATH)
+    missing = [n for n in declared_symbols() if not hasattr(lib, n)]
+    assert not missing, missing
+    assert sorted(pkg._lib.exported_symbols()) == declared_symbols()
+
+
+def test_host_side_validation(pkg):
+    lib = pkg._lib.load()
+    assert lib.cov3d_abi_version() == 1
+    h = ctypes.c_void_p()
+    assert lib.cov3d_plan_create(0, 1, 1e-6, None, ctypes.byref(h)) == pkg._lib.EINVAL
+    assert "invalid plan size" in pkg._lib.last_error()
+    opts = pkg._lib.Opts(kernel=7, upsample=2)
+    assert lib.cov3d_plan_create(16, 1, 1e-6, ctypes.byref(opts), ctypes.byref(h)) == pkg._lib.EINVAL
+    assert lib.cov3d_plan_destroy(None) == 0
+    assert lib.cov3d_setpts(None, None, 1, 4, 48, 16, 0) == pkg._lib.EINVAL
+    assert lib.cov3d_status_string(pkg._lib.ENOMEM) == b"out of device memory"
+    try:
+        pkg._lib.check(pkg._lib.EINVAL)
+    except ValueError as e:
+        assert "invalid argument" in str(e)
+    else:
+        raise AssertionError("check() did not raise")

@@ -1,0 +1,128 @@
+"""GPU parity of the covariance cost and its hand-written gradient: the drop-in cost
+functions and the fused single-call step, against the reference's own outputs (golden
+fixture, float64 autograd) and the float64 oracle."""
+import numpy as np
+import pytest
+import torch
+
+from conftest import load_golden
+from oracle import nufft_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+TOL_COST = 1e-5   # FP32 path vs FP64 reference, relative
+TOL_GRAD = 1e-4   # gradient vs FP64, relative (spec bound)
+
+
+def rel(a, b):
+    a = a.detach().cpu().numpy() if torch.is_tensor(a) else np.asarray(a)
+    b = b.detach().cpu().numpy() if torch.is_tensor(b) else np.asarray(b)
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+@pytest.mark.parametrize("objective", ["ml", "ls"])
+@pytest.mark.parametrize("with_reg", [False, True])
+def test_dropin_cost_matches_reference(pkg, dev, objective, with_reg):
+    c = load_golden("cost_L10_r3.npz")
+    L, r, us = int(c["L"]), int(c["r"]), int(c["us"])
+    covar = pkg.Covar(L, r, upsampling_factor=us, vectors=torch.tensor(c["vectors"])).to(dev)
+    covar.init_grid_correction("bilinear")
+    plan = pkg.NufftPlanDiscretized((L,) * 3, upsample_factor=us, mode="bilinear")
+    plan.setpts(torch.tensor(c["pts"], dtype=torch.float32, device=dev))
+    fn = pkg.cost_maximum_liklihood_fourier_domain if objective == "ml" else pkg.cost_fourier_domain
+    kw = dict(reg_scale=float(c["reg_scale"]), fourier_reg=torch.tensor(c["fourier_reg"], device=dev)) if with_reg else {}
+    val = fn(covar.get_vectors_fourier_domain(), torch.tensor(c["images"], device=dev),
+             plan, torch.tensor(c["filters"], device=dev), float(c["noise_var"]), **kw)
+    val.backward()
+    tag = objective + ("_reg" if with_reg else "")
+    assert rel(val, c[tag + "_cost"]) < TOL_COST
+    assert rel(covar.vectors.grad, c[tag + "_grad_vectors"]) < TOL_GRAD
+    assert rel(covar.log_sqrt_eigenvals.grad, c[tag + "_grad_logsqrt"]) < TOL_GRAD
+    # per-image (mean_aggregate=False) data term
+    per = fn(covar.get_vectors_fourier_domain(), torch.tensor(c["images"], device=dev), plan,
+             torch.tensor(c["filters"], device=dev), float(c["noise_var"]), mean_aggregate=False)
+    if not with_reg:
+        assert rel(per, c[tag + "_per_image"]) < TOL_COST
+
+
+@pytest.mark.parametrize("objective", ["ml", "ls"])
+@pytest.mark.parametrize("with_reg", [False, True])
+def test_fused_step_matches_reference(pkg, dev, objective, with_reg):
+    if objective == "ls" and with_reg:
+        pytest.skip("the LS regulariser is evaluated outside the fused step")
+    c = load_golden("cost_L10_r3.npz")
+    L, r, us = int(c["L"]), int(c["r"]), int(c["us"])
+    step = pkg.FusedCovarStep(L, r, "bilinear", us, device=dev)
+    step.set_points(torch.tensor(c["pts"], dtype=torch.float32, device=dev))
+    B = c["images"].shape[0]
+    per = torch.empty((B,), dtype=torch.float64, device=dev)
+    val, gv, gl = step(torch.tensor(c["vectors_normalised"], device=dev), torch.tensor(c["log_sqrt_eigenvals"], device=dev),
+                       torch.tensor(c["images"], device=dev).reshape(B, -1),
+                       torch.tensor(c["filters"], device=dev).reshape(B, -1), float(c["noise_var"]),
+                       reg_scale=float(c["reg_scale"]) if with_reg else 0.0,
+                       fourier_reg=torch.tensor(c["fourier_reg"], device=dev) if with_reg else None,
+                       objective=0 if objective == "ml" else 1, per_image=per, sync_cost=True)
+    tag = objective + ("_reg" if with_reg else "")
+    assert rel(val, c[tag + "_cost"]) < TOL_COST
+    assert rel(gv, c[tag + "_grad_vectors"]) < TOL_GRAD
+    assert rel(gl, c[tag + "_grad_logsqrt"]) < TOL_GRAD
+
+
+@pytest.mark.parametrize("L,r,B", [(16, 3, 8), (24, 5, 12)])
+def test_fused_es_step_matches_fp64_oracle(pkg, dev, L, r, B):
+    rng = np.random.default_rng(L * r)
+    vec = rng.standard_normal((r, L, L, L))
+    vec /= np.linalg.norm(vec.reshape(r, -1), axis=1)[:, None, None, None]
+    vec = vec.astype(np.float32)
+    ls = np.log(rng.uniform(2.0, 6.0, r)).astype(np.float32)
+    R = O.rotvec_to_rotmat(rng.standard_normal((B, 3))).astype(np.float32)
+    imgs = ((rng.standard_normal((B, L, L)) + 1j * rng.standard_normal((B, L, L))) * 3).astype(np.complex64)
+    ctf = rng.uniform(0.2, 1.3, (B, L, L)).astype(np.float32)
+    fr = rng.uniform(0.5, 2.0, (2 * L,) * 3).astype(np.float32)
+    step = pkg.FusedCovarStep(L, r, "nufft", 2, width=6, device=dev)
+    step.set_rotations(torch.tensor(R, device=dev))
+    val, gv, gl = step(torch.tensor(vec, device=dev), torch.tensor(ls, device=dev),
+                       torch.tensor(imgs, device=dev).reshape(B, -1), torch.tensor(ctf, device=dev).reshape(B, -1),
+                       5.0, reg_scale=0.01, fourier_reg=torch.tensor(fr, device=dev), sync_cost=True)
+    pts = O.rotated_points(R.astype(np.float64), L)
+    ref = O.covar_cost_grad(vec, ls, imgs, pts, ctf, 5.0, kind="es", width=6, reg_scale=0.01, fourier_reg=fr)
+    assert rel(val, ref[0]) < TOL_COST
+    assert rel(gv, ref[1]) < TOL_GRAD
+    assert rel(gl, ref[2]) < TOL_GRAD
+
+
+def test_fused_step_equals_dropin_autograd_full_size(pkg, dev):
+    """Two independent code paths at L=64: the single-call fused step and the drop-in cost
+    (vol_forward + ProjectedCost autograd) on the same discretized plan."""
+    L, r, B = 64, 4, 16
+    g = torch.Generator(device=dev).manual_seed(1)
+    covar = pkg.Covar(L, r, upsampling_factor=2).to(dev)
+    covar.init_grid_correction("bilinear")
+    R = torch.linalg.qr(torch.randn((B, 3, 3), device=dev, generator=g))[0].contiguous()
+    imgs = torch.randn((B, L, L), device=dev, generator=g, dtype=torch.complex64) * 50
+    ctf = torch.rand((B, L, L), device=dev, generator=g) + 0.2
+    plan = pkg.NufftPlanDiscretized((L,) * 3, upsample_factor=2, mode="bilinear")
+    plan.setrot(R)
+    val = pkg.cost_maximum_liklihood_fourier_domain(covar.get_vectors_fourier_domain(), imgs, plan, ctf, 300.0)
+    val.backward()
+    step = pkg.FusedCovarStep(L, r, "bilinear", 2, device=dev)
+    step.set_rotations(R)
+    v2, gv, gl = step(covar.vectors.detach(), covar.log_sqrt_eigenvals.detach(), imgs.reshape(B, -1),
+                      ctf.reshape(B, -1), 300.0, sync_cost=True)
+    assert rel(v2, val.item()) < 1e-5
+    assert rel(gv, covar.vectors.grad) < 1e-4
+    assert rel(gl, covar.log_sqrt_eigenvals.grad) < 1e-4
+
+
+def test_latent_map_matches_reference(pkg, dev):
+    g = load_golden("latent_L10_r3.npz")
+    z, m, b = pkg.wiener_coords.compute_latentMAP_batch(torch.tensor(g["images"], device=dev),
+                                                        torch.tensor(g["eigen_forward"], device=dev),
+                                                        float(g["noise_var"]),
+                                                        torch.tensor(g["eigenvals_inv"], device=dev))
+    assert rel(z, g["z"]) < TOL_COST and rel(m, g["m"]) < TOL_COST and rel(b, g["b"]) < TOL_COST
+    z, m, b = pkg.wiener_coords.compute_latentMAP_batch(torch.tensor(g["images"].real, device=dev),
+                                                        torch.tensor(g["eigen_forward"].real, device=dev),
+                                                        float(g["noise_var"]),
+                                                        torch.tensor(g["eigenvals_inv"], device=dev))
+    assert rel(z, g["z_real"]) < TOL_COST and rel(m, g["m_real"]) < TOL_COST

@@ -233,7 +233,7 @@ def run_gb300(args):
                           grad_log_sqrt=covar.log_sqrt_eigenvals.grad)
         grads_allreduce()
         opt.step()
-        return c
+        return c.reshape(())
 
     def barrier():
         if world > 1:

@@ -68,6 +68,8 @@ _SIGNATURES = {
                            c_void_p, c_void_p]),
     "cov3d_cost_solve": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_double, c_void_p, c_double,
                                  c_double, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "cov3d_latent_map_noalloc": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_int64, c_int64, c_int64,
+                                         c_void_p, c_double, c_void_p, c_void_p, c_void_p, c_void_p]),
     "cov3d_wpass": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_int64, c_int64, c_int64, c_void_p, c_void_p,
                             c_void_p, c_void_p, c_int64, c_int64, c_int64]),
 }

@@ -221,6 +221,25 @@ int cov3d_wpass(void *stream, int n_images, int P, int r, const void *d_q, int64
                 int64_t chan_stride, const void *d_images, const void *d_C, const void *d_u, void *d_w,
                 int64_t w_img_stride, int64_t w_point_stride, int64_t w_chan_stride);
 
+/* ------------------------------------------------------------------ allocation-free variant
+ * No counterpart in the reference.  Same result as cov3d_gram followed by cov3d_cost_solve
+ * (objective 0, no adjoint coefficients, no costs) for callers that cannot let a library
+ * allocate device memory: their own pool owns the GPU, or cudaMalloc's device-wide
+ * synchronisation is not acceptable on their call path.  The intermediates live in a 4 MiB
+ * file-scope device array that each GPU loading the library keeps until exit; the call
+ * allocates nothing (no cudaMalloc / cudaFree / allocating library routine).
+ * Limit: n_images * (8 r^2 + 8 r + 4) bytes plus alignment must fit in 4 MiB (e.g. 4,700
+ * images at r = 10); larger requests return COV3D_EINVAL with the limit in the message.
+ * The first call on each device looks up the array's device address (cudaGetSymbolAddress)
+ * with that device current; make that first call before any stream capture.  All calls share
+ * the one array and it keeps the last call's contents: calls that overlap on the GPU (other
+ * streams, other host threads) race, so serialise them.  d_z (n_images, r) complex64 and/or
+ * d_m (n_images, r, r) complex64 receive the results; d_bad (optional, device int) receives 1
+ * when some m is not positive definite, else 0. */
+int cov3d_latent_map_noalloc(void *stream, int n_images, int P, int r, const void *d_q, int64_t img_stride,
+                             int64_t point_stride, int64_t chan_stride, const void *d_images, double noise_var,
+                             const double *d_linv, void *d_z, void *d_m, int *d_bad);
+
 #ifdef __cplusplus
 }
 #endif

@@ -80,6 +80,33 @@ __device__ __forceinline__ int first_cell(float t) {
   return (int)ceilf(t - 0.5f * (float)W);
 }
 
+// ES kernel value exp(beta * (sqrt(1 - (2x/W)^2) - 1)) for |x| < W/2, else 0, with the fast
+// hardware exponential and reciprocal square root (relative error ~1e-6, far below the ES
+// approximation error of the NUFFT).
+template <int W>
+__device__ __forceinline__ float es_weight(float x, float beta) {
+  const float y = x * (2.0f / (float)W);
+  const float u = 1.0f - y * y;
+  return u > 0.0f ? __expf(beta * (u * rsqrtf(u) - 1.0f)) : 0.0f;
+}
+
+// Sorted point record written by the sort: fractional grid indices along axes 0..2 and the
+// point id, with kNyquistBit set when the point lies on the Nyquist row / column of an
+// even-sized image (vol_forward zeroes those pixels, projection_funcs.py:355-358).
+struct SortedPoint {
+  float t0, t1, t2;
+  int idf;
+};
+constexpr int kNyquistBit = 1 << 30;
+__device__ __forceinline__ int sp_id(int idf) { return idf & (kNyquistBit - 1); }
+__device__ __forceinline__ bool sp_nyquist(int idf) { return (idf & kNyquistBit) != 0; }
+
+__device__ __forceinline__ bool on_nyquist(const PointGeom &g, int64_t id) {
+  if (g.Lp % 2 != 0) return false;
+  const int p = (int)(id % g.P);
+  return p < g.Lp || (p % g.Lp) == 0;
+}
+
 // Kernel taps along one axis: window cells c0 .. c0+W-1 and their weights.
 template <int KT, int W>
 __device__ __forceinline__ int taps(float t, float beta, float *wt) {
@@ -93,15 +120,22 @@ __device__ __forceinline__ int taps(float t, float beta, float *wt) {
     return (int)f0;
   } else {
     const int c0 = (int)ceilf(t - 0.5f * (float)W);
-    const float inv_half = 2.0f / (float)W;
 #pragma unroll
-    for (int j = 0; j < W; ++j) {
-      const float x = (t - (float)(c0 + j)) * inv_half;
-      const float u = 1.0f - x * x;
-      wt[j] = u > 0.0f ? expf(beta * (sqrtf(u) - 1.0f)) : 0.0f;
-    }
+    for (int j = 0; j < W; ++j) wt[j] = es_weight<W>(t - (float)(c0 + j), beta);
     return c0;
   }
+}
+
+// Weight of tap q (0 <= q < W) of the window of a point at fractional index t.
+template <int KT, int W>
+__device__ __forceinline__ float tap_weight(float t, int q, float beta) {
+  if (KT == COV3D_KERNEL_NEAREST) return 1.0f;
+  if (KT == COV3D_KERNEL_LINEAR) {
+    const float f0 = floorf(t);
+    return q == 0 ? (f0 + 1.0f) - t : t - f0;
+  }
+  const int c0 = (int)ceilf(t - 0.5f * (float)W);
+  return es_weight<W>(t - (float)(c0 + q), beta);
 }
 
 }  // namespace cov3d

@@ -413,7 +413,7 @@ int covar_cost_grad(cov3d_plan *p, const cov3d_cost_args *a, double *h_cost, dou
   }
   // 3. interpolate at the central slices with the fused projection epilogue -> Q (B*P, r)
   const int shift = p->n - p->n / 2;
-  GridArgs ga{p->fine.ptr, r, 1, shift};
+  GridArgs ga{p->fine.ptr, 1, n3, shift};
   EpilogueArgs ep{a->d_ctf, 1, 1.0f / (float)L};
   {
     PhaseScope ps(p, kPhaseInterp);
@@ -440,7 +440,7 @@ int covar_cost_grad(cov3d_plan *p, const cov3d_cost_args *a, double *h_cost, dou
   {
     PhaseScope ps(p, kPhaseSpread);
     COV3D_TRY(launch_zero(p, p->fine2.ptr, n3 * r * 8));
-    COV3D_TRY(launch_spread(p, p->q.ptr, r, 1, r, ep, p->fine2.ptr, r, 1, shift));
+    COV3D_TRY(launch_spread(p, p->q.ptr, r, 1, r, ep, p->fine2.ptr, 1, n3, shift));
   }
   // 8. regulariser on the fine grid
   if (a->d_fourier_reg && a->reg_scale != 0.0) {

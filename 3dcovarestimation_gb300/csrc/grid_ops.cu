@@ -4,7 +4,8 @@
 // projection_funcs.py:11-165, whose fftshift/ifftshift/pad copies are folded into index maps).
 //
 // Storage order of the fine grid is the raw FFT order: voxel offset k = j - L/2 sits at
-// storage index k mod n, so no shift pass is needed on either side of the FFT.
+// storage index k mod n, so no shift pass is needed on either side of the FFT.  Fine grids are
+// channels-first (nchan planes of n^3 cells) so cuFFT runs unit-stride batched transforms.
 #include "cov3d_device.cuh"
 
 namespace cov3d {
@@ -34,9 +35,9 @@ __global__ void pack_kernel(const float *__restrict__ vr, const float2 *__restri
   const int s1 = (int)((cell / n) % n);
   const int s0 = (int)(cell / ((int64_t)n * n));
   const int j0 = storage_to_voxel(s0, L, n), j1 = storage_to_voxel(s1, L, n), j2 = storage_to_voxel(s2, L, n);
-  float2 *out = fine + cell * nchan;
+  float2 *out = fine + cell;
   if (j0 < 0 || j1 < 0 || j2 < 0) {
-    for (int c = 0; c < nchan; ++c) out[c] = make_float2(0.f, 0.f);
+    for (int c = 0; c < nchan; ++c) out[c * n3] = make_float2(0.f, 0.f);
     return;
   }
   const int64_t L3 = (int64_t)L * L * L;
@@ -45,7 +46,7 @@ __global__ void pack_kernel(const float *__restrict__ vr, const float2 *__restri
   for (int c = 0; c < nchan; ++c) {
     const float sc = logs ? g * expf(__ldg(logs + c)) : g;
     float2 x = vr ? make_float2(__ldg(vr + c * L3 + v), 0.f) : vc[c * L3 + v];
-    out[c] = make_float2(x.x * sc, x.y * sc);
+    out[c * n3] = make_float2(x.x * sc, x.y * sc);
   }
 }
 
@@ -59,7 +60,7 @@ __global__ void unpack_complex_kernel(const float2 *__restrict__ fine, const flo
       ((int64_t)voxel_to_storage(j0, L, n) * n + voxel_to_storage(j1, L, n)) * n + voxel_to_storage(j2, L, n);
   const float g = gc ? 1.0f / (__ldg(gc + j0) * __ldg(gc + j1) * __ldg(gc + j2)) : 1.0f;
   for (int c = 0; c < nchan; ++c) {
-    const float2 x = fine[cell * nchan + c];
+    const float2 x = fine[(int64_t)c * n * n * n + cell];
     out[c * L3 + v] = make_float2(x.x * g, x.y * g);
   }
 }
@@ -84,7 +85,7 @@ __global__ void unpack_grad_kernel(const float2 *__restrict__ fine, const float 
     double part = 0.0;
     if (live) {
       const float e = expf(__ldg(logs + c));
-      const float dV = 2.0f * fine[cell * nchan + c].x * g;
+      const float dV = 2.0f * fine[(int64_t)c * n * n * n + cell].x * g;
       const float vec = __ldg(vectors + c * L3 + v);
       gvec[c * L3 + v] = dV * e;
       part = (double)dV * (double)(vec * e);
@@ -114,11 +115,11 @@ __global__ void ml_reg_kernel(const float2 *__restrict__ grid, float2 *__restric
     const float w = __ldg(fr + ((int64_t)s0 * n + s1) * n + s2);
     const float cf = (float)coef * w;
     for (int c = 0; c < nchan; ++c) {
-      const float2 x = grid[cell * nchan + c];
-      float2 y = gg[cell * nchan + c];
+      const float2 x = grid[c * n3 + cell];
+      float2 y = gg[c * n3 + cell];
       y.x = fmaf(cf, x.x, y.x);
       y.y = fmaf(cf, x.y, y.y);
-      gg[cell * nchan + c] = y;
+      gg[c * n3 + cell] = y;
       part += (double)w * ((double)x.x * x.x + (double)x.y * x.y);
     }
   }
@@ -198,8 +199,9 @@ int get_fft(cov3d_plan *p, int nchan, cufftHandle *out) {
   }
   cufftHandle h;
   int dims[3] = {p->n, p->n, p->n};
-  COV3D_TRY(check_cufft(cufftPlanMany(&h, 3, dims, dims, nchan, 1, dims, nchan, 1, CUFFT_C2C, nchan),
-                        "cufftPlanMany"));
+  const int n3 = p->n * p->n * p->n;
+  // channels-first: nchan contiguous n^3 transforms (unit stride, distance n^3)
+  COV3D_TRY(check_cufft(cufftPlanMany(&h, 3, dims, dims, 1, n3, dims, 1, n3, CUFFT_C2C, nchan), "cufftPlanMany"));
   (*p->ffts)[nchan] = h;
   *out = h;
   return check_cufft(cufftSetStream(h, p->stream), "cufftSetStream");

@@ -1,8 +1,7 @@
-// Interpolation ("type-2" half of the NUFFT, and the reference's grid_sample forward):
-// one thread per nonuniform point, visited in bin-sorted order so that the warps of a block
-// gather overlapping neighbourhoods of the fine grid through L1.  All channels of a pass are
-// accumulated in registers from channels-last cells (one 16-byte vector load per two complex
-// channels), and the projection epilogue (Nyquist zeroing, CTF multiply, 1/L) is fused.
+// Interpolation ("type-2" half of the NUFFT, and the reference's grid_sample forward) over
+// bin-sorted points: each subproblem's tile of the fine grid is read from HBM once into shared
+// memory and reused by all its points; the projection epilogue (Nyquist zeroing, CTF
+// multiply, 1/L) is fused.
 #include "cov3d_device.cuh"
 
 namespace cov3d {
@@ -12,12 +11,17 @@ namespace {
 struct InterpParams {
   PointGeom g;
   KernelSpec k;
-  int64_t M;
-  const int *perm;
+  Bins bins;
+  const SortedPoint *pts;
+  const int *sub_bin;
+  const int *sub_first;
+  const int *sub_count;
+  const int *nsub;
   const float2 *grid;
   int64_t cs, chs;
   int shift;
   int ch0;
+  int nch;  // channels in this pass (<= 2 * CP)
   float2 *out;
   int64_t ops, ocs;
   const float *ctf;
@@ -25,114 +29,200 @@ struct InterpParams {
   float scale;
 };
 
-template <int KT, int W, int CH, bool CONTIG>
-__global__ void __launch_bounds__(256) interp_kernel(const InterpParams a) {
-  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= a.M) return;
-  const int64_t id = a.perm ? (int64_t)__ldg(a.perm + k) : k;
+constexpr int kBin = 8;
+constexpr int kInterpWarps = 16;
+
+// Channel pairs per pass: lanes are (window cell, channel pair) pairs, so W * CP <= 32, and the
+// tile (bin + halo) of 2*CP complex channels must fit in shared memory.
+template <int W>
+struct InterpCP {
+  static constexpr int value = W <= 2 ? 16 : 32 / W;
+};
+
+// One block per subproblem.  The block stages the bin's tile (bin + (W-1)-cell halo) of 2*CP
+// channels in shared memory as [cell][channel] complex, then each warp takes one point at a
+// time: lane (j, q) reads the two channels 2q, 2q+1 of tile[row][corner2 + j] for the W*W
+// window rows -- W*CP contiguous 16-byte values per row, no bank conflicts -- and accumulates
+// weight * value; the W partial sums of each pair are combined through shared memory and the
+// epilogue (Nyquist zeroing, CTF, scale) is applied.
+template <int KT, int W, int CP>
+__global__ void __launch_bounds__(kInterpWarps * 32) interp_kernel(const InterpParams a) {
+  constexpr int T = kBin + W - 1;
+  constexpr int CH = 2 * CP;
+  constexpr int LANES = W * CP;
+  extern __shared__ float4 tile4[];  // T^3 * CP float4 (= 2 complex), then kInterpWarps * 32 float4
+  float2 *tile = reinterpret_cast<float2 *>(tile4);
+  float4 *red = tile4 + T * T * T * CP;
+  const int sub = blockIdx.x;
+  if (sub >= *a.nsub) return;
+  const int bin = a.sub_bin[sub];
+  const int first = a.sub_first[sub];
+  const int cnt = a.sub_count[sub];
+  const int nb12 = a.bins.nb[1] * a.bins.nb[2];
+  const int ts0 = (bin / nb12) * kBin;
+  const int ts1 = ((bin / a.bins.nb[2]) % a.bins.nb[1]) * kBin;
+  const int ts2 = (bin % a.bins.nb[2]) * kBin;
   const int n = a.g.n;
-  float t[3];
-  point_index(a.g, id, t);
-  float wt[3][W];
-  int s[3][W];
-#pragma unroll
-  for (int d = 0; d < 3; ++d) {
-    const int c0 = taps<KT, W>(t[d], a.k.beta, wt[d]);
-#pragma unroll
-    for (int j = 0; j < W; ++j) {
-      int m = c0 + j;
-      if (KT == COV3D_KERNEL_ES) {
-        m = pmod(m, n);
-      } else if (m < 0 || m >= n) {
-        wt[d][j] = 0.0f;
-        m = 0;
-      }
-      m += a.shift;
-      s[d][j] = m >= n ? m - n : m;
+  const int tid = threadIdx.x;
+
+  // stage the tile: (channel, row, cell) with cell fastest for coalesced global reads
+  for (int e = tid; e < CH * T * T * T; e += blockDim.x) {
+    const int c2 = e % T;
+    const int rowi = (e / T) % (T * T);
+    const int ch = e / (T * T * T);
+    const int c0 = rowi / T, c1 = rowi - (rowi / T) * T;
+    int m0 = ts0 + c0, m1 = ts1 + c1, m2 = ts2 + c2;
+    float2 v = make_float2(0.f, 0.f);
+    bool ok = ch < a.nch;
+    if (KT == COV3D_KERNEL_ES) {
+      m0 = m0 >= n ? m0 - n : m0;
+      m1 = m1 >= n ? m1 - n : m1;
+      m2 = m2 >= n ? m2 - n : m2;
+    } else {
+      ok = ok && m0 < n && m1 < n && m2 < n;
     }
+    if (ok) {
+      m0 += a.shift;
+      m1 += a.shift;
+      m2 += a.shift;
+      m0 = m0 >= n ? m0 - n : m0;
+      m1 = m1 >= n ? m1 - n : m1;
+      m2 = m2 >= n ? m2 - n : m2;
+      v = __ldg(a.grid + (((int64_t)m0 * n + m1) * n + m2) * a.cs + (int64_t)(a.ch0 + ch) * a.chs);
+    }
+    tile[(rowi * T + c2) * CH + ch] = v;
   }
-  float2 acc[CH];
+  __syncthreads();
+
+  const int warp = tid >> 5, lane = tid & 31;
+  const int j = lane / CP, q = lane - (lane / CP) * CP;  // window cell along axis 2, channel pair
+  float4 *wred = red + warp * 32;
+  for (int k = warp; k < cnt; k += kInterpWarps) {
+    const SortedPoint sp = a.pts[first + k];
+    int c0[3];
+    c0[0] = first_cell<KT, W>(sp.t0);
+    c0[1] = first_cell<KT, W>(sp.t1);
+    c0[2] = first_cell<KT, W>(sp.t2);
+    // one kernel weight per lane < 3W, then shared through the warp
+    float myw = 0.0f;
+    if (lane < 3 * W) {
+      const int d = lane / W, tq = lane - (lane / W) * W;
+      const float td = d == 0 ? sp.t0 : d == 1 ? sp.t1 : sp.t2;
+      myw = tap_weight<KT, W>(td, tq, a.k.beta);
+    }
+    float w0[W], w1[W];
 #pragma unroll
-  for (int c = 0; c < CH; ++c) acc[c] = make_float2(0.f, 0.f);
-  const float2 *gbase = a.grid + a.ch0 * a.chs;
-#pragma unroll 1
-  for (int i0 = 0; i0 < W; ++i0) {
+    for (int r = 0; r < W; ++r) {
+      w0[r] = __shfl_sync(0xffffffffu, myw, r);
+      w1[r] = __shfl_sync(0xffffffffu, myw, W + r);
+    }
+    const float wj = __shfl_sync(0xffffffffu, myw, 2 * W + (j < W ? j : 0));
+    int l0 = c0[0], l1 = c0[1], l2 = c0[2];
+    if (KT == COV3D_KERNEL_ES) {
+      l0 = pmod(l0, n);
+      l1 = pmod(l1, n);
+      l2 = pmod(l2, n);
+    }
+    l0 -= ts0;
+    l1 -= ts1;
+    l2 -= ts2;
+    const int cell2 = l2 + j;
+    const bool lane_ok = lane < LANES && cell2 >= 0;
+    const float4 *base = tile4 + cell2 * CP + q;
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-    for (int i1 = 0; i1 < W; ++i1) {
-      const float wab = wt[0][i0] * wt[1][i1];
-      if (KT != COV3D_KERNEL_ES && wab == 0.0f) continue;
-      const int64_t row = ((int64_t)s[0][i0] * n + s[1][i1]) * n;
+    for (int i0 = 0; i0 < W; ++i0) {
+      const int r0 = l0 + i0;
+      if (KT != COV3D_KERNEL_ES && r0 < 0) continue;
+      const float w0j = w0[i0] * wj;
 #pragma unroll
-      for (int i2 = 0; i2 < W; ++i2) {
-        const float w = wab * wt[2][i2];
-        if (KT != COV3D_KERNEL_ES && w == 0.0f) continue;
-        const float2 *cell = gbase + (row + s[2][i2]) * a.cs;
-        if (CONTIG) {
-          const float4 *c4 = reinterpret_cast<const float4 *>(cell);
-#pragma unroll
-          for (int c = 0; c < CH / 2; ++c) {
-            const float4 v = __ldg(c4 + c);
-            acc[2 * c].x = fmaf(w, v.x, acc[2 * c].x);
-            acc[2 * c].y = fmaf(w, v.y, acc[2 * c].y);
-            acc[2 * c + 1].x = fmaf(w, v.z, acc[2 * c + 1].x);
-            acc[2 * c + 1].y = fmaf(w, v.w, acc[2 * c + 1].y);
-          }
-        } else {
-#pragma unroll
-          for (int c = 0; c < CH; ++c) {
-            const float2 v = __ldg(cell + c * a.chs);
-            acc[c].x = fmaf(w, v.x, acc[c].x);
-            acc[c].y = fmaf(w, v.y, acc[c].y);
-          }
+      for (int i1 = 0; i1 < W; ++i1) {
+        const int r1 = l1 + i1;
+        if (KT != COV3D_KERNEL_ES && r1 < 0) continue;
+        if (lane_ok) {
+          const float w = w0j * w1[i1];
+          const float4 v = base[(r0 * T + r1) * T * CP];
+          acc.x = fmaf(w, v.x, acc.x);
+          acc.y = fmaf(w, v.y, acc.y);
+          acc.z = fmaf(w, v.z, acc.z);
+          acc.w = fmaf(w, v.w, acc.w);
         }
       }
     }
-  }
-  // epilogue: vol_forward's Nyquist zeroing, CTF multiply and 1/L (projection_funcs.py:355-370)
-  const int64_t b = id / a.g.P;
-  const int p = (int)(id - b * a.g.P);
-  float sc = a.scale;
-  if (a.nyquist && (a.g.Lp % 2 == 0)) {
-    const int row = p / a.g.Lp;
-    const int col = p - row * a.g.Lp;
-    if (row == 0 || col == 0) sc = 0.0f;
-  }
-  if (a.ctf) sc *= __ldg(a.ctf + id);
-  float2 *o = a.out + id * a.ops + (int64_t)a.ch0 * a.ocs;
+    wred[lane] = acc;
+    __syncwarp();
+    if (lane < CP) {
+      float4 s = wred[lane];
 #pragma unroll
-  for (int c = 0; c < CH; ++c) o[c * a.ocs] = make_float2(acc[c].x * sc, acc[c].y * sc);
+      for (int r = 1; r < W; ++r) {
+        const float4 x = wred[r * CP + lane];
+        s.x += x.x;
+        s.y += x.y;
+        s.z += x.z;
+        s.w += x.w;
+      }
+      // epilogue: vol_forward's Nyquist zeroing, CTF multiply and 1/L (projection_funcs.py:355-370)
+      const int64_t id = sp_id(sp.idf);
+      float sc = (a.nyquist && sp_nyquist(sp.idf)) ? 0.0f : a.scale;
+      if (a.ctf) sc *= __ldg(a.ctf + id);
+      float2 *o = a.out + id * a.ops + (int64_t)(a.ch0 + 2 * lane) * a.ocs;
+      if (2 * lane < a.nch) o[0] = make_float2(s.x * sc, s.y * sc);
+      if (2 * lane + 1 < a.nch) o[a.ocs] = make_float2(s.z * sc, s.w * sc);
+    }
+    __syncwarp();
+  }
 }
 
-template <int KT, int W, int CH>
-int launch_ch(const InterpParams &a, bool contig, cudaStream_t st) {
-  const int blocks = (int)((a.M + 255) / 256);
-  if (CH % 2 == 0 && contig) {
-    interp_kernel<KT, W, CH, (CH % 2 == 0)><<<blocks, 256, 0, st>>>(a);
-  } else {
-    interp_kernel<KT, W, CH, false><<<blocks, 256, 0, st>>>(a);
+// Points whose window lies entirely outside the grid (zero padding) get zero outputs.
+__global__ void interp_dead_kernel(const SortedPoint *__restrict__ pts, const int *__restrict__ off, int64_t nbins,
+                                   int nchan, float2 *__restrict__ out, int64_t ops, int64_t ocs) {
+  const int lo = off[nbins], hi = off[nbins + 1];
+  for (int k = lo + blockIdx.x * blockDim.x + threadIdx.x; k < hi; k += gridDim.x * blockDim.x) {
+    const int64_t id = sp_id(pts[k].idf);
+    for (int c = 0; c < nchan; ++c) out[id * ops + c * ocs] = make_float2(0.f, 0.f);
   }
+}
+
+template <int KT, int W, int CP>
+int launch_cp(const InterpParams &a, int64_t max_blocks, cudaStream_t st) {
+  constexpr int T = kBin + W - 1;
+  const size_t smem = ((size_t)T * T * T * CP + kInterpWarps * 32) * sizeof(float4);
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(interp_kernel<KT, W, CP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return check_cuda(e, "cudaFuncSetAttribute(interp_kernel)");
+  }
+  interp_kernel<KT, W, CP><<<(unsigned)max_blocks, kInterpWarps * 32, smem, st>>>(a);
   return launched("interp_kernel");
 }
 
+// Channel passes of at most 2*InterpCP<W> channels; a short last pass uses a smaller tile.
 template <int KT, int W>
-int launch_w(InterpParams a, int nchan, cudaStream_t st) {
+int launch_w(InterpParams a, int nchan, int64_t max_blocks, cudaStream_t st) {
+  constexpr int CPMAX = InterpCP<W>::value;
   int done = 0;
   while (done < nchan) {
     const int left = nchan - done;
-    const int ch = left >= 16 ? 16 : left >= 10 ? 10 : left >= 8 ? 8 : left >= 4 ? 4 : left >= 2 ? 2 : 1;
     a.ch0 = done;
-    const bool contig = a.chs == 1 && (a.cs % 2 == 0) && (done % 2 == 0) &&
-                        ((reinterpret_cast<uintptr_t>(a.grid) & 15) == 0);
-    int st_ = COV3D_OK;
-    switch (ch) {
-      case 16: st_ = launch_ch<KT, W, 16>(a, contig, st); break;
-      case 10: st_ = launch_ch<KT, W, 10>(a, contig, st); break;
-      case 8: st_ = launch_ch<KT, W, 8>(a, contig, st); break;
-      case 4: st_ = launch_ch<KT, W, 4>(a, contig, st); break;
-      case 2: st_ = launch_ch<KT, W, 2>(a, contig, st); break;
-      default: st_ = launch_ch<KT, W, 1>(a, contig, st); break;
+    int s = COV3D_OK, ch = 0;
+    if (left >= 2 * CPMAX) {
+      ch = 2 * CPMAX;
+      a.nch = ch;
+      s = launch_cp<KT, W, CPMAX>(a, max_blocks, st);
+    } else if (left > 4) {
+      ch = left;  // up to 2*CPMAX - 1 channels in the full-size tile
+      a.nch = ch;
+      s = launch_cp<KT, W, CPMAX>(a, max_blocks, st);
+    } else if (left > 2) {
+      ch = left;
+      a.nch = ch;
+      s = launch_cp<KT, W, (CPMAX > 2 ? 2 : CPMAX)>(a, max_blocks, st);
+    } else {
+      ch = left;
+      a.nch = ch;
+      s = launch_cp<KT, W, 1>(a, max_blocks, st);
     }
-    if (st_ != COV3D_OK) return st_;
+    if (s != COV3D_OK) return s;
     done += ch;
   }
   return COV3D_OK;
@@ -149,8 +239,12 @@ int launch_interp(cov3d_plan *p, const GridArgs &ga, int nchan, void *out, int64
   InterpParams a{};
   a.g = make_geom(p);
   a.k = make_kernel(p);
-  a.M = p->n_points;
-  a.perm = p->perm.as<int>();
+  a.bins = p->bins;
+  a.pts = p->sorted.as<SortedPoint>();
+  a.sub_bin = p->sub_bin.as<int>();
+  a.sub_first = p->sub_first.as<int>();
+  a.sub_count = p->sub_count.as<int>();
+  a.nsub = p->nsub.as<int>();
   a.grid = static_cast<const float2 *>(ga.grid);
   a.cs = ga.cell_stride;
   a.chs = ga.chan_stride;
@@ -161,16 +255,22 @@ int launch_interp(cov3d_plan *p, const GridArgs &ga, int nchan, void *out, int64
   a.ctf = e.ctf;
   a.nyquist = e.nyquist;
   a.scale = e.scale;
+  const int64_t mb = p->bins.nbins + p->n_points / p->max_sub + 1;
+  if (p->kernel != COV3D_KERNEL_ES) {
+    interp_dead_kernel<<<64, 256, 0, p->stream>>>(a.pts, p->bin_off.as<int>(), p->bins.nbins, nchan, a.out, out_ps,
+                                                  out_cs);
+    COV3D_LAUNCHED("interp_dead_kernel");
+  }
   switch (p->kernel) {
-    case COV3D_KERNEL_NEAREST: return launch_w<COV3D_KERNEL_NEAREST, 1>(a, nchan, p->stream);
-    case COV3D_KERNEL_LINEAR: return launch_w<COV3D_KERNEL_LINEAR, 2>(a, nchan, p->stream);
+    case COV3D_KERNEL_NEAREST: return launch_w<COV3D_KERNEL_NEAREST, 1>(a, nchan, mb, p->stream);
+    case COV3D_KERNEL_LINEAR: return launch_w<COV3D_KERNEL_LINEAR, 2>(a, nchan, mb, p->stream);
     default:
       switch (p->width) {
-        case 4: return launch_w<COV3D_KERNEL_ES, 4>(a, nchan, p->stream);
-        case 5: return launch_w<COV3D_KERNEL_ES, 5>(a, nchan, p->stream);
-        case 6: return launch_w<COV3D_KERNEL_ES, 6>(a, nchan, p->stream);
-        case 7: return launch_w<COV3D_KERNEL_ES, 7>(a, nchan, p->stream);
-        case 8: return launch_w<COV3D_KERNEL_ES, 8>(a, nchan, p->stream);
+        case 4: return launch_w<COV3D_KERNEL_ES, 4>(a, nchan, mb, p->stream);
+        case 5: return launch_w<COV3D_KERNEL_ES, 5>(a, nchan, mb, p->stream);
+        case 6: return launch_w<COV3D_KERNEL_ES, 6>(a, nchan, mb, p->stream);
+        case 7: return launch_w<COV3D_KERNEL_ES, 7>(a, nchan, mb, p->stream);
+        case 8: return launch_w<COV3D_KERNEL_ES, 8>(a, nchan, mb, p->stream);
         default: set_error("unsupported ES width %d (supported: 4..8)", p->width); return COV3D_EINVAL;
       }
   }

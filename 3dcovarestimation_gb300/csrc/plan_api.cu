@@ -284,7 +284,12 @@ int cov3d_plan_create(int L, int n_trans, double eps, const cov3d_opts *opts, co
     p->width = o.kernel == COV3D_KERNEL_LINEAR ? 2 : 1;
     p->beta = 0.0;
   }
-  const int bs = o.bin_size > 0 ? o.bin_size : 8;
+  const int bs = 8;
+  if (o.bin_size != 0 && o.bin_size != 8) {
+    set_error("bin_size must be 0 or 8");
+    delete p;
+    return COV3D_EINVAL;
+  }
   for (int d = 0; d < 3; ++d) {
     p->bins.bs[d] = bs;
     p->bins.nb[d] = (n + bs - 1) / bs;
@@ -300,6 +305,7 @@ int cov3d_plan_create(int L, int n_trans, double eps, const cov3d_opts *opts, co
   if (st == COV3D_OK) st = grow(p->gc1d, L * 4);
   if (st == COV3D_OK) st = check_cuda(cudaMemcpy(p->gc1d.ptr, gf.data(), L * 4, cudaMemcpyHostToDevice), "cudaMemcpy");
   if (st == COV3D_OK) st = grow(p->acc, 64 * sizeof(double));
+  if (st == COV3D_OK) st = build_row_order(p);
   if (st == COV3D_OK) st = check_cuda(cudaMallocHost(&p->h_acc, 64 * sizeof(double)), "cudaMallocHost");
   if (st != COV3D_OK || !p->ffts || !p->ev_pool || !p->ev_phase) {
     cov3d_plan_destroy(p);
@@ -318,7 +324,7 @@ int cov3d_plan_destroy(cov3d_plan *p) {
     delete p->ffts;
   }
   DevBuf *bufs[] = {&p->gc1d, &p->pts, &p->rot, &p->bin_count, &p->bin_off, &p->sub_off, &p->pt_bin, &p->pt_rank,
-                    &p->perm, &p->sub_bin, &p->sub_first, &p->sub_count, &p->nsub, &p->fine, &p->fine2, &p->q,
+                    &p->perm, &p->sorted, &p->row_order, &p->sub_bin, &p->sub_first, &p->sub_count, &p->nsub, &p->fine, &p->fine2, &p->q,
                     &p->small, &p->acc};
   for (DevBuf *b : bufs) release(*b);
   if (p->h_acc) cudaFreeHost(p->h_acc);
@@ -460,7 +466,7 @@ int cov3d_execute_type2(cov3d_plan *p, const float *d_vol_real, const void *d_vo
   COV3D_TRY(get_fft(p, nchan, &fft));
   COV3D_TRY(check_cufft(cufftExecC2C(fft, p->fine.as<cufftComplex>(), p->fine.as<cufftComplex>(), CUFFT_FORWARD),
                         "cufftExecC2C(forward)"));
-  GridArgs g{p->fine.ptr, nchan, 1, p->n - p->n / 2};
+  GridArgs g{p->fine.ptr, 1, n3, p->n - p->n / 2};
   EpilogueArgs e{nullptr, 0, 1.0f};
   return launch_interp(p, g, nchan, d_out, 1, p->n_points, e);
 }
@@ -474,7 +480,7 @@ int cov3d_execute_type1(cov3d_plan *p, const void *d_values, int nchan, void *d_
   COV3D_TRY(grow(p->fine, n3 * nchan * 8));
   COV3D_TRY(launch_zero(p, p->fine.ptr, n3 * nchan * 8));
   EpilogueArgs e{nullptr, 0, 1.0f};
-  COV3D_TRY(launch_spread(p, d_values, 1, p->n_points, nchan, e, p->fine.ptr, nchan, 1, p->n - p->n / 2));
+  COV3D_TRY(launch_spread(p, d_values, 1, p->n_points, nchan, e, p->fine.ptr, 1, n3, p->n - p->n / 2));
   cufftHandle fft;
   COV3D_TRY(get_fft(p, nchan, &fft));
   COV3D_TRY(check_cufft(cufftExecC2C(fft, p->fine.as<cufftComplex>(), p->fine.as<cufftComplex>(), CUFFT_INVERSE),

@@ -83,11 +83,20 @@ __global__ void bin_scan_kernel(const int *__restrict__ count, int64_t nbins, in
   }
 }
 
-__global__ void scatter_kernel(int64_t M, const int *__restrict__ pt_bin, const int *__restrict__ pt_rank,
-                               const int *__restrict__ off, int *__restrict__ perm) {
+__global__ void scatter_kernel(PointGeom g, int64_t M, const int *__restrict__ pt_bin, const int *__restrict__ pt_rank,
+                               const int *__restrict__ off, int *__restrict__ perm, SortedPoint *__restrict__ sorted) {
   const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (id >= M) return;
-  perm[off[pt_bin[id]] + pt_rank[id]] = (int)id;
+  const int pos = off[pt_bin[id]] + pt_rank[id];
+  perm[pos] = (int)id;
+  float t[3];
+  point_index(g, id, t);
+  SortedPoint sp;
+  sp.t0 = t[0];
+  sp.t1 = t[1];
+  sp.t2 = t[2];
+  sp.idf = (int)id | (on_nyquist(g, id) ? kNyquistBit : 0);
+  sorted[pos] = sp;
 }
 
 __global__ void subproblem_kernel(int64_t nbins, int max_sub, const int *__restrict__ count,
@@ -115,8 +124,8 @@ void launch_count(cov3d_plan *p, const PointGeom &g, const KernelSpec &k, int bl
 int sort_points(cov3d_plan *p) {
   const int64_t M = p->n_points;
   if (M <= 0) return COV3D_OK;
-  if (M >= (int64_t)INT32_MAX) {
-    set_error("too many points (%lld); the limit is 2^31-1", (long long)M);
+  if (M >= (int64_t)(1 << 30)) {
+    set_error("too many points (%lld); the limit is 2^30-1 per plan", (long long)M);
     return COV3D_EINVAL;
   }
   const int64_t nb = p->bins.nbins;
@@ -127,6 +136,7 @@ int sort_points(cov3d_plan *p) {
   COV3D_TRY(grow(p->pt_bin, M * 4));
   COV3D_TRY(grow(p->pt_rank, M * 4));
   COV3D_TRY(grow(p->perm, M * 4));
+  COV3D_TRY(grow(p->sorted, M * (int64_t)sizeof(SortedPoint)));
   COV3D_TRY(grow(p->sub_bin, max_subs * 4));
   COV3D_TRY(grow(p->sub_first, max_subs * 4));
   COV3D_TRY(grow(p->sub_count, max_subs * 4));
@@ -154,7 +164,8 @@ int sort_points(cov3d_plan *p) {
   COV3D_LAUNCHED("bin_count_kernel");
   bin_scan_kernel<<<1, 1024, 0, p->stream>>>(p->bin_count.as<int>(), nb, p->max_sub, p->bin_off.as<int>(), p->sub_off.as<int>(), p->nsub.as<int>());
   COV3D_LAUNCHED("bin_scan_kernel");
-  scatter_kernel<<<blocks, 256, 0, p->stream>>>(M, p->pt_bin.as<int>(), p->pt_rank.as<int>(), p->bin_off.as<int>(), p->perm.as<int>());
+  scatter_kernel<<<blocks, 256, 0, p->stream>>>(g, M, p->pt_bin.as<int>(), p->pt_rank.as<int>(), p->bin_off.as<int>(),
+                                                p->perm.as<int>(), p->sorted.as<SortedPoint>());
   COV3D_LAUNCHED("scatter_kernel");
   subproblem_kernel<<<(int)((nb + 255) / 256), 256, 0, p->stream>>>(nb, p->max_sub, p->bin_count.as<int>(), p->bin_off.as<int>(),
                                                                     p->sub_off.as<int>(), p->sub_bin.as<int>(), p->sub_first.as<int>(),

@@ -1,22 +1,34 @@
 // Spreading ("type-1" half of the NUFFT; exact adjoint of interp.cu, replacing the
 // reference's grid_sample backward with FP32 global atomics, nufft_plan.py:171-242).
 //
-// One thread block per subproblem (<= max_sub points of one spatial bin).  The block
-// accumulates its points' kernel footprints into a shared-memory tile covering the bin plus
-// a (W-1)-cell halo, then adds the tile to the global grid once.  With `COMP` every shared
-// accumulation is compensated: atomicAdd returns the previous value, so the rounding error of
-// that exact addition is recovered with Knuth's TwoSum and accumulated in a second tile.
+// One thread block per subproblem (<= max_sub points of one 8^3-cell spatial bin), no
+// shared-memory atomics on the data path:
+//  1. the block counting-sorts its points by their (axis-0, axis-1) window corner inside the
+//     bin (64 columns) and stores, per point, its axis-0/1 kernel weights, its axis-2 weights
+//     expanded over the tile row, and its CH channel values (times the im_backward prologue:
+//     CTF, Nyquist zeroing, scale);
+//  2. every thread owns one axis-2 row of the tile (bin + (W-1)-cell halo) and accumulates, in
+//     registers, every point whose window covers that row -- the points of the W x W columns
+//     around it, walked as one flattened list -- over the whole row; with COMP each register
+//     accumulator is Kahan-compensated;
+//  3. the tile is added to the global grid once, one complex atomic per cell and channel.
+#include <algorithm>
+#include <vector>
+
 #include "cov3d_device.cuh"
 
 namespace cov3d {
 
 namespace {
 
+constexpr int kBin = 8;           // bin edge (cells); plans use 8^3 bins
+constexpr int kSpreadThreads = 256;
+
 struct SpreadParams {
   PointGeom g;
   KernelSpec k;
   Bins bins;
-  const int *perm;
+  const SortedPoint *pts;
   const int *sub_bin;
   const int *sub_first;
   const int *sub_count;
@@ -30,180 +42,283 @@ struct SpreadParams {
   float2 *grid;
   int64_t cs, chs;
   int shift;
-  int T0, T1, T2;
+  int max_sub;
+  const int *row_order;  // tile rows (a << 8 | b) in decreasing order of work
 };
-
-template <bool COMP>
-__device__ __forceinline__ void tile_add(float *hi, float *lo, int idx, float v) {
-  if (!COMP) {
-    atomicAdd(hi + idx, v);
-  } else {
-    const float old = atomicAdd(hi + idx, v);
-    const float s = old + v;
-    const float bb = s - old;
-    const float err = (old - (s - bb)) + (v - bb);
-    if (err != 0.0f) atomicAdd(lo + idx, err);
-  }
-}
 
 // Prologue factor of im_backward: CTF multiply, Nyquist zeroing, scale (projection_funcs.py:385-399).
 __device__ __forceinline__ float prologue(const PointGeom &g, int64_t id, const float *ctf, int nyquist, float scale) {
   float sc = scale;
-  if (nyquist && (g.Lp % 2 == 0)) {
-    const int64_t b = id / g.P;
-    const int p = (int)(id - b * g.P);
-    const int row = p / g.Lp;
-    const int col = p - row * g.Lp;
-    if (row == 0 || col == 0) sc = 0.0f;
-  }
+  if (nyquist && on_nyquist(g, id)) sc = 0.0f;
   if (ctf) sc *= __ldg(ctf + id);
   return sc;
 }
 
+template <int W, int CH>
+struct RowLayout {
+  static constexpr int T = kBin + W - 1;             // tile edge
+  static constexpr int T4 = (T + 3) / 4 * 4;         // axis-2 weights padded to float4
+  static constexpr int V = 2 * CH;                   // channel values (re, im)
+  static constexpr int V4 = (V + 3) / 4 * 4;
+  static constexpr int W0 = T4 + V4;                 // axis-0 weights
+  static constexpr int W1 = W0 + W;                  // axis-1 weights
+  static constexpr int S4 = (W1 + W + 3) / 4;        // float4 groups per record, made odd so that
+  static constexpr int STRIDE = 4 * (S4 % 2 ? S4 : S4 + 1);  // records of different points start on
+                                                              // different bank groups
+};
+
+// Number of bin columns along one axis whose window reaches tile row coordinate x.
+template <int W>
+__device__ constexpr int reach(int x) {
+  const int lo = x - W + 1 > 0 ? x - W + 1 : 0;
+  const int hi = x < kBin - 1 ? x : kBin - 1;
+  return hi >= lo ? hi - lo + 1 : 0;
+}
+
+template <int KT, int W, int CH>
+__device__ __forceinline__ void local_corner(const SpreadParams &a, float t, int ts, int &l, float *wt) {
+  int c0 = taps<KT, W>(t, a.k.beta, wt);
+  if (KT == COV3D_KERNEL_ES) c0 = pmod(c0, a.g.n);
+  l = c0 - ts;
+}
+
+template <int KT, int W>
+__device__ __forceinline__ int local_first(const SpreadParams &a, float t, int ts) {
+  int c0 = first_cell<KT, W>(t);
+  if (KT == COV3D_KERNEL_ES) c0 = pmod(c0, a.g.n);
+  return c0 - ts;
+}
+
 template <int KT, int W, int CH, bool COMP>
-__global__ void __launch_bounds__(256) spread_kernel(const SpreadParams a) {
-  extern __shared__ float smem[];
+__global__ void __launch_bounds__(kSpreadThreads, 2) spread_kernel(const SpreadParams a) {
+  using Lay = RowLayout<W, CH>;
+  constexpr int T = Lay::T;
+  extern __shared__ float4 smem4[];
+  int *s_cnt = reinterpret_cast<int *>(smem4);     // kBin*kBin
+  int *s_off = s_cnt + kBin * kBin;                 // kBin*kBin + 1 (+3 pad)
+  int *s_col = s_off + kBin * kBin + 4;             // max_sub
+  int *s_rank = s_col + a.max_sub;                  // max_sub
+  float *s_rec = reinterpret_cast<float *>(s_rank + a.max_sub);  // max_sub * STRIDE
+
   const int sub = blockIdx.x;
   if (sub >= *a.nsub) return;
-  const int TT = a.T0 * a.T1 * a.T2;
-  float *hi = smem;
-  float *lo = smem + 2 * CH * TT;
   const int bin = a.sub_bin[sub];
   const int first = a.sub_first[sub];
   const int cnt = a.sub_count[sub];
   const int nb12 = a.bins.nb[1] * a.bins.nb[2];
-  const int ts0 = (bin / nb12) * a.bins.bs[0];
-  const int ts1 = ((bin / a.bins.nb[2]) % a.bins.nb[1]) * a.bins.bs[1];
-  const int ts2 = (bin % a.bins.nb[2]) * a.bins.bs[2];
+  const int ts0 = (bin / nb12) * kBin;
+  const int ts1 = ((bin / a.bins.nb[2]) % a.bins.nb[1]) * kBin;
+  const int ts2 = (bin % a.bins.nb[2]) * kBin;
   const int n = a.g.n;
+  const int tid = threadIdx.x;
 
-  for (int q = threadIdx.x; q < (COMP ? 4 : 2) * CH * TT; q += blockDim.x) smem[q] = 0.0f;
+  for (int i = tid; i < kBin * kBin; i += blockDim.x) s_cnt[i] = 0;
   __syncthreads();
-
-  for (int kk = threadIdx.x; kk < cnt; kk += blockDim.x) {
-    const int64_t id = __ldg(a.perm + first + kk);
-    const float sc = prologue(a.g, id, a.ctf, a.nyquist, a.scale);
-    if (sc == 0.0f) continue;
-    float t[3];
-    point_index(a.g, id, t);
-    float wt[3][W];
-    int l[3];
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      int c0 = taps<KT, W>(t[d], a.k.beta, wt[d]);
-      if (KT == COV3D_KERNEL_ES) c0 = pmod(c0, n);
-      l[d] = c0 - (d == 0 ? ts0 : d == 1 ? ts1 : ts2);
+  // 1a. column of every point (window corner on axes 0, 1 inside the bin) and its rank
+  for (int k = tid; k < cnt; k += blockDim.x) {
+    const SortedPoint sp = a.pts[first + k];
+    const int l0 = local_first<KT, W>(a, sp.t0, ts0);
+    const int l1 = local_first<KT, W>(a, sp.t1, ts1);
+    const int col = max(l0, 0) * kBin + max(l1, 0);
+    s_col[k] = col;
+    s_rank[k] = atomicAdd(s_cnt + col, 1);
+  }
+  __syncthreads();
+  if (tid == 0) {
+    int acc = 0;
+    for (int i = 0; i < kBin * kBin; ++i) {
+      s_off[i] = acc;
+      acc += s_cnt[i];
     }
-    float2 v[CH];
+    s_off[kBin * kBin] = acc;
+  }
+  __syncthreads();
+  // 1b. point records in column order
+  for (int k = tid; k < cnt; k += blockDim.x) {
+    const SortedPoint sp = a.pts[first + k];
+    const int64_t id = sp_id(sp.idf);
+    float w0[W], w1[W], w2[W];
+    int l0, l1, l2;
+    local_corner<KT, W, CH>(a, sp.t0, ts0, l0, w0);
+    local_corner<KT, W, CH>(a, sp.t1, ts1, l1, w1);
+    local_corner<KT, W, CH>(a, sp.t2, ts2, l2, w2);
+    float *rec = s_rec + (s_off[s_col[k]] + s_rank[k]) * Lay::STRIDE;
+    float sc = (a.nyquist && sp_nyquist(sp.idf)) ? 0.0f : a.scale;
+    if (a.ctf) sc *= __ldg(a.ctf + id);
+#pragma unroll
+    for (int c = 0; c < Lay::T4; ++c) rec[c] = 0.0f;
+#pragma unroll
+    for (int j = 0; j < W; ++j) {
+      const int c = l2 + j;
+      if (c >= 0 && c < T) rec[c] = w2[j];
+    }
     const float2 *src = a.vals + id * a.ips + (int64_t)a.ch0 * a.ics;
 #pragma unroll
     for (int c = 0; c < CH; ++c) {
-      const float2 x = __ldg(src + c * a.ics);
-      v[c] = make_float2(x.x * sc, x.y * sc);
+      const float2 x = sc != 0.0f ? __ldg(src + c * a.ics) : make_float2(0.f, 0.f);
+      rec[Lay::T4 + 2 * c] = x.x * sc;
+      rec[Lay::T4 + 2 * c + 1] = x.y * sc;
     }
-#pragma unroll 1
-    for (int i0 = 0; i0 < W; ++i0) {
-      const int la = l[0] + i0;
-      if (KT != COV3D_KERNEL_ES && (la < 0 || wt[0][i0] == 0.0f)) continue;
+    // zero padding (grid_sample kernels): window cells below the grid were clamped into bin 0;
+    // shift their weights so that index (row - corner) still addresses the right tap
+    const int s0 = max(-l0, 0), s1 = max(-l1, 0);
 #pragma unroll
-      for (int i1 = 0; i1 < W; ++i1) {
-        const int lb = l[1] + i1;
-        if (KT != COV3D_KERNEL_ES && (lb < 0 || wt[1][i1] == 0.0f)) continue;
-        const float wab = wt[0][i0] * wt[1][i1];
-        const int rowi = (la * a.T1 + lb) * a.T2;
+    for (int j = 0; j < W; ++j) {
+      rec[Lay::W0 + j] = 0.0f;
+      rec[Lay::W1 + j] = 0.0f;
+    }
 #pragma unroll
-        for (int i2 = 0; i2 < W; ++i2) {
-          const int lc = l[2] + i2;
-          if (KT != COV3D_KERNEL_ES && (lc < 0 || wt[2][i2] == 0.0f)) continue;
-          const float w = wab * wt[2][i2];
-          const int idx = rowi + lc;
-#pragma unroll
-          for (int c = 0; c < CH; ++c) {
-            tile_add<COMP>(hi, lo, (2 * c) * TT + idx, w * v[c].x);
-            tile_add<COMP>(hi, lo, (2 * c + 1) * TT + idx, w * v[c].y);
-          }
-        }
-      }
+    for (int j = 0; j < W; ++j) {
+      if (j >= s0) rec[Lay::W0 + j - s0] = w0[j];
+      if (j >= s1) rec[Lay::W1 + j - s1] = w1[j];
     }
   }
   __syncthreads();
 
-  const int T12 = a.T1 * a.T2;
-  for (int q = threadIdx.x; q < TT; q += blockDim.x) {
-    const int la = q / T12;
-    const int lb = (q / a.T2) % a.T1;
-    const int lc = q % a.T2;
-    int m0 = ts0 + la, m1 = ts1 + lb, m2 = ts2 + lc;
-    if (KT == COV3D_KERNEL_ES) {
-      m0 = m0 >= n ? m0 - n : m0;
-      m1 = m1 >= n ? m1 - n : m1;
-      m2 = m2 >= n ? m2 - n : m2;
-    } else if (m0 >= n || m1 >= n || m2 >= n) {
-      continue;
+  // 2. one axis-2 row of the tile per thread.  The thread walks the points of the W x W
+  //    columns around its row as one flattened list, so the lanes of a warp stay converged
+  //    (their totals differ far less than their per-column counts).  Rows are handed out in
+  //    decreasing order of the number of columns that reach them (halo rows see fewer), so
+  //    the rows of one warp carry similar work.
+  if (tid >= T * T) return;
+  const int packed = __ldg(a.row_order + tid);
+  const int ra = packed >> 8, rb = packed & 255;
+  float2 acc[T][CH];
+  float2 cmp[COMP ? T : 1][COMP ? CH : 1];
+#pragma unroll
+  for (int c = 0; c < T; ++c)
+#pragma unroll
+    for (int h = 0; h < CH; ++h) {
+      acc[c][h] = make_float2(0.f, 0.f);
+      if (COMP) cmp[COMP ? c : 0][COMP ? h : 0] = make_float2(0.f, 0.f);
     }
-    m0 += a.shift;
-    m1 += a.shift;
-    m2 += a.shift;
+  int next = 0, p = 0, pend = 0, o0 = 0, o1 = 0;
+  while (true) {
+    while (p >= pend && next < W * W) {
+      const int d0 = next / W, d1 = next - (next / W) * W;
+      ++next;
+      const int l0 = ra - d0, l1 = rb - d1;
+      if (l0 < 0 || l0 >= kBin || l1 < 0 || l1 >= kBin) continue;
+      p = s_off[l0 * kBin + l1];
+      pend = s_off[l0 * kBin + l1 + 1];
+      o0 = d0;
+      o1 = d1;
+    }
+    if (p >= pend) break;
+    const float *rec = s_rec + p * Lay::STRIDE;
+    ++p;
+    const float wab = rec[Lay::W0 + o0] * rec[Lay::W1 + o1];
+    float w2[Lay::T4];
+#pragma unroll
+    for (int q = 0; q < Lay::T4 / 4; ++q) {
+      const float4 x = reinterpret_cast<const float4 *>(rec)[q];
+      w2[4 * q] = x.x;
+      w2[4 * q + 1] = x.y;
+      w2[4 * q + 2] = x.z;
+      w2[4 * q + 3] = x.w;
+    }
+    float v[Lay::V4];
+#pragma unroll
+    for (int q = 0; q < Lay::V4 / 4; ++q) {
+      const float4 x = reinterpret_cast<const float4 *>(rec + Lay::T4)[q];
+      v[4 * q] = x.x;
+      v[4 * q + 1] = x.y;
+      v[4 * q + 2] = x.z;
+      v[4 * q + 3] = x.w;
+    }
+#pragma unroll
+    for (int c = 0; c < T; ++c) {
+      const float w = wab * w2[c];
+#pragma unroll
+      for (int h = 0; h < CH; ++h) {
+        if (!COMP) {
+          acc[c][h].x = fmaf(w, v[2 * h], acc[c][h].x);
+          acc[c][h].y = fmaf(w, v[2 * h + 1], acc[c][h].y);
+        } else {
+          float y = w * v[2 * h] - cmp[COMP ? c : 0][COMP ? h : 0].x;
+          float t2 = acc[c][h].x + y;
+          cmp[COMP ? c : 0][COMP ? h : 0].x = (t2 - acc[c][h].x) - y;
+          acc[c][h].x = t2;
+          y = w * v[2 * h + 1] - cmp[COMP ? c : 0][COMP ? h : 0].y;
+          t2 = acc[c][h].y + y;
+          cmp[COMP ? c : 0][COMP ? h : 0].y = (t2 - acc[c][h].y) - y;
+          acc[c][h].y = t2;
+        }
+      }
+    }
+  }
+
+  // 3. add the row to the global grid
+  int m0 = ts0 + ra, m1 = ts1 + rb;
+  if (KT == COV3D_KERNEL_ES) {
     m0 = m0 >= n ? m0 - n : m0;
     m1 = m1 >= n ? m1 - n : m1;
-    m2 = m2 >= n ? m2 - n : m2;
-    float2 *dst = a.grid + (((int64_t)m0 * n + m1) * n + m2) * a.cs + (int64_t)a.ch0 * a.chs;
+  } else if (m0 >= n || m1 >= n) {
+    return;
+  }
+  m0 += a.shift;
+  m1 += a.shift;
+  m0 = m0 >= n ? m0 - n : m0;
+  m1 = m1 >= n ? m1 - n : m1;
+  const int64_t row = ((int64_t)m0 * n + m1) * n;
 #pragma unroll
-    for (int c = 0; c < CH; ++c) {
-      float re = hi[(2 * c) * TT + q];
-      float im = hi[(2 * c + 1) * TT + q];
+  for (int c = 0; c < T; ++c) {
+    int m2 = ts2 + c;
+    if (KT == COV3D_KERNEL_ES) {
+      m2 = m2 >= n ? m2 - n : m2;
+    } else if (m2 >= n) {
+      continue;
+    }
+    m2 += a.shift;
+    m2 = m2 >= n ? m2 - n : m2;
+    float2 *dst = a.grid + (row + m2) * a.cs + (int64_t)a.ch0 * a.chs;
+#pragma unroll
+    for (int h = 0; h < CH; ++h) {
+      float2 val = acc[c][h];
       if (COMP) {
-        re += lo[(2 * c) * TT + q];
-        im += lo[(2 * c + 1) * TT + q];
+        val.x -= cmp[COMP ? c : 0][COMP ? h : 0].x;
+        val.y -= cmp[COMP ? c : 0][COMP ? h : 0].y;
       }
-      if (re != 0.0f) atomicAdd(&dst[c * a.chs].x, re);
-      if (im != 0.0f) atomicAdd(&dst[c * a.chs].y, im);
+      if (val.x != 0.0f || val.y != 0.0f) atomicAdd(dst + h * a.chs, val);
     }
   }
 }
 
 template <int KT, int W, int CH, bool COMP>
+size_t smem_bytes(int max_sub) {
+  return (size_t)(2 * kBin * kBin + 8 + 2 * max_sub) * sizeof(int) +
+         (size_t)max_sub * RowLayout<W, CH>::STRIDE * sizeof(float);
+}
+
+template <int KT, int W, int CH, bool COMP>
 int launch_one(const SpreadParams &a, int64_t max_blocks, cudaStream_t st) {
-  const int64_t TT = (int64_t)a.T0 * a.T1 * a.T2;
-  const size_t smem = (size_t)(COMP ? 4 : 2) * CH * TT * sizeof(float);
-  static size_t configured = 0;
-  if (smem > 48 * 1024 && smem > configured) {
+  const size_t smem = smem_bytes<KT, W, CH, COMP>(a.max_sub);
+  if (smem > 200 * 1024) {
+    set_error("spread tile records of %zu bytes exceed shared memory", smem);
+    return COV3D_EINVAL;
+  }
+  if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(spread_kernel<KT, W, CH, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return check_cuda(e, "cudaFuncSetAttribute(spread_kernel)");
-    configured = smem;
   }
-  spread_kernel<KT, W, CH, COMP><<<(unsigned)max_blocks, 256, smem, st>>>(a);
+  spread_kernel<KT, W, CH, COMP><<<(unsigned)max_blocks, kSpreadThreads, smem, st>>>(a);
   return launched("spread_kernel");
 }
 
-constexpr size_t kSpreadSmemBudget = 112 * 1024;  // two blocks per SM
-
 template <int KT, int W>
 int launch_w(SpreadParams a, int nchan, bool comp, int64_t max_blocks, cudaStream_t st) {
-  const int64_t TT = (int64_t)a.T0 * a.T1 * a.T2;
-  const size_t per_ch = (size_t)(comp ? 4 : 2) * TT * sizeof(float);
   int done = 0;
   while (done < nchan) {
     const int left = nchan - done;
-    int ch = 1;
-    if (left >= 4 && 4 * per_ch <= kSpreadSmemBudget) ch = 4;
-    else if (left >= 2 && 2 * per_ch <= kSpreadSmemBudget) ch = 2;
-    if (per_ch > 200 * 1024) {
-      set_error("spreading tile of %lld cells does not fit in shared memory; use a smaller bin_size",
-                (long long)TT);
-      return COV3D_EINVAL;
-    }
     a.ch0 = done;
-    int s = COV3D_OK;
+    int s = COV3D_OK, ch = 1;
     if (comp) {
-      s = ch == 4 ? launch_one<KT, W, 4, true>(a, max_blocks, st)
-        : ch == 2 ? launch_one<KT, W, 2, true>(a, max_blocks, st)
-                  : launch_one<KT, W, 1, true>(a, max_blocks, st);
+      ch = 1;
+      s = launch_one<KT, W, 1, true>(a, max_blocks, st);
     } else {
-      s = ch == 4 ? launch_one<KT, W, 4, false>(a, max_blocks, st)
-        : ch == 2 ? launch_one<KT, W, 2, false>(a, max_blocks, st)
-                  : launch_one<KT, W, 1, false>(a, max_blocks, st);
+      ch = left >= 2 ? 2 : 1;
+      s = ch == 2 ? launch_one<KT, W, 2, false>(a, max_blocks, st) : launch_one<KT, W, 1, false>(a, max_blocks, st);
     }
     if (s != COV3D_OK) return s;
     done += ch;
@@ -252,6 +367,26 @@ __global__ void spread_unagg_kernel(PointGeom g, KernelSpec k, int64_t M, const 
 
 }  // namespace
 
+int build_row_order(cov3d_plan *p) {
+  const int W = p->kernel == COV3D_KERNEL_NEAREST ? 1 : p->kernel == COV3D_KERNEL_LINEAR ? 2 : p->width;
+  const int T = kBin + W - 1;
+  auto reach_h = [&](int x) {
+    const int lo = x - W + 1 > 0 ? x - W + 1 : 0;
+    const int hi = x < kBin - 1 ? x : kBin - 1;
+    return hi >= lo ? hi - lo + 1 : 0;
+  };
+  std::vector<int> rows(T * T);
+  for (int q = 0; q < T * T; ++q) rows[q] = q;
+  std::stable_sort(rows.begin(), rows.end(), [&](int x, int y) {
+    return reach_h(x / T) * reach_h(x % T) > reach_h(y / T) * reach_h(y % T);
+  });
+  std::vector<int> packed(T * T);
+  for (int i = 0; i < T * T; ++i) packed[i] = ((rows[i] / T) << 8) | (rows[i] % T);
+  COV3D_TRY(grow(p->row_order, (int64_t)packed.size() * 4));
+  return check_cuda(cudaMemcpy(p->row_order.ptr, packed.data(), packed.size() * 4, cudaMemcpyHostToDevice),
+                    "cudaMemcpy(row_order)");
+}
+
 int launch_spread(cov3d_plan *p, const void *values, int64_t in_ps, int64_t in_cs, int nchan, const EpilogueArgs &e,
                   void *grid, int64_t cell_stride, int64_t chan_stride, int shift) {
   if (p->point_kind == kPointsNone || p->n_points == 0) {
@@ -262,7 +397,7 @@ int launch_spread(cov3d_plan *p, const void *values, int64_t in_ps, int64_t in_c
   a.g = make_geom(p);
   a.k = make_kernel(p);
   a.bins = p->bins;
-  a.perm = p->perm.as<int>();
+  a.pts = p->sorted.as<SortedPoint>();
   a.sub_bin = p->sub_bin.as<int>();
   a.sub_first = p->sub_first.as<int>();
   a.sub_count = p->sub_count.as<int>();
@@ -277,10 +412,12 @@ int launch_spread(cov3d_plan *p, const void *values, int64_t in_ps, int64_t in_c
   a.cs = cell_stride;
   a.chs = chan_stride;
   a.shift = shift;
-  const int W = p->kernel == COV3D_KERNEL_NEAREST ? 1 : p->kernel == COV3D_KERNEL_LINEAR ? 2 : p->width;
-  a.T0 = p->bins.bs[0] + W - 1;
-  a.T1 = p->bins.bs[1] + W - 1;
-  a.T2 = p->bins.bs[2] + W - 1;
+  a.max_sub = p->max_sub;
+  a.row_order = p->row_order.as<int>();
+  if (p->bins.bs[0] != kBin || p->bins.bs[1] != kBin || p->bins.bs[2] != kBin) {
+    set_error("spreading requires %d^3-cell bins", kBin);
+    return COV3D_EINVAL;
+  }
   const int64_t max_blocks = p->bins.nbins + p->n_points / p->max_sub + 1;
   const bool comp = p->compensated != 0;
   switch (p->kernel) {

@@ -46,6 +46,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--seed", type=int, default=2000)
+    ap.add_argument("--uncompensated", action="store_true", help="plain FP32 spreading (no Kahan terms)")
     return ap.parse_args()
 
 
@@ -202,7 +203,8 @@ def run_gb300(args):
     rot = rot.reshape(nb, B, 3, 3).contiguous()
     ctf = ctf.reshape(nb, B, -1)
     covar = pkg.Covar(L, r, upsampling_factor=2).to(dev)
-    step_fn = pkg.FusedCovarStep(L, r, "nufft", 2, width=args.width, device=dev)
+    step_fn = pkg.FusedCovarStep(L, r, "nufft", 2, width=args.width, device=dev,
+                                 compensated=not args.uncompensated)
     covar.vectors.grad = torch.zeros_like(covar.vectors)
     covar.log_sqrt_eigenvals.grad = torch.zeros_like(covar.log_sqrt_eigenvals)
     groups = covar.grad_lr_factor()
@@ -329,6 +331,7 @@ def run_gb300(args):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOAD, "global_batch": B * world, "L": L, "rank": r, "upsample": 2,
                    "es_width": args.width, "resident_images": nb * B,
+                   "spreading": "fp32" if args.uncompensated else "fp32 + Kahan compensation",
                    "l2": "inputs larger than L2: each step reads a distinct resident 1024-image batch "
                          "(134 MB images + 67 MB CTF) and 1.34 GB fine grids",
                    "parallelism": f"dp{world}", "seed": args.seed},

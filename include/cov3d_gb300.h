@@ -61,7 +61,7 @@ typedef struct {
   int width;         /* ES width w in [2, 16]; 0 = from eps: ceil(-log10(eps/10)) */
   double beta;       /* ES shape; 0 = 0.97*pi*(1 - 1/(2 sigma))*w */
   int compensated;   /* 1 = TwoSum-compensated FP32 spreading in shared memory */
-  int bin_size;      /* spatial bin edge in fine-grid cells for point sorting; 0 = 8 */
+  int bin_size;      /* spatial bin edge in fine-grid cells (0 or 8; spreading tiles are 8^3 bins) */
   void *stream;      /* cudaStream_t for all work of this plan (NULL = legacy default) */
 } cov3d_opts;
 

@@ -10,6 +10,9 @@ __device__ __forceinline__ int pmod(int a, int n) {
   return r < 0 ? r + n : r;
 }
 
+// a mod n for a in [-n, 2n): the window corners of wrapped points.
+__device__ __forceinline__ int wrap1(int a, int n) { return a < 0 ? a + n : (a >= n ? a - n : a); }
+
 // torch.remainder(x + pi, 2 pi) - pi in float32 (poses.py:259-261, nufft_plan.py:327).
 __device__ __forceinline__ float wrap_pi(float x) {
   const float two_pi = 6.28318530717958647692f;

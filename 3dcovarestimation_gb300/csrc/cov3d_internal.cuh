@@ -110,13 +110,13 @@ struct cov3d_plan {
 
   // sort / subproblems
   cov3d::Bins bins{};
-  int max_sub = 512;
+  int max_sub = 288;
   cov3d::DevBuf bin_count;     // int (nbins + 1), last = dead points
   cov3d::DevBuf bin_off;       // int (nbins + 2)
   cov3d::DevBuf sub_off;       // int (nbins + 1)
   cov3d::DevBuf pt_bin, pt_rank, perm;        // int (M)
   cov3d::DevBuf sorted;        // SortedPoint (M), bin-sorted order
-  cov3d::DevBuf row_order;     // spreading tile rows, decreasing work
+  cov3d::DevBuf row_order;     // spreading plane schedule per warp
   cov3d::DevBuf sub_bin, sub_first, sub_count;  // int (max subproblems)
   cov3d::DevBuf nsub;          // int scalar
 
@@ -179,7 +179,7 @@ int launch_interp(cov3d_plan *p, const GridArgs &g, int nchan, void *out, int64_
 // spread.cu
 int launch_spread(cov3d_plan *p, const void *values, int64_t in_ps, int64_t in_cs, int nchan, const EpilogueArgs &e,
                   void *grid, int64_t cell_stride, int64_t chan_stride, int shift);
-int build_row_order(cov3d_plan *p);
+int build_plane_schedule(cov3d_plan *p);
 int launch_spread_unaggregated(cov3d_plan *p, const void *values, int64_t in_ps, const EpilogueArgs &e,
                                void *grids);
 

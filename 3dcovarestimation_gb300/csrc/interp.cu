@@ -22,6 +22,7 @@ struct InterpParams {
   int shift;
   int ch0;
   int nch;  // channels in this pass (<= 2 * CP)
+  int max_sub;
   float2 *out;
   int64_t ops, ocs;
   const float *ctf;
@@ -53,6 +54,8 @@ __global__ void __launch_bounds__(kInterpWarps * 32) interp_kernel(const InterpP
   extern __shared__ float4 tile4[];  // T^3 * CP float4 (= 2 complex), then kInterpWarps * 32 float4
   float2 *tile = reinterpret_cast<float2 *>(tile4);
   float4 *red = tile4 + T * T * T * CP;
+  SortedPoint *s_sp = reinterpret_cast<SortedPoint *>(red + kInterpWarps * 32);  // max_sub
+  float *s_sc = reinterpret_cast<float *>(s_sp + a.max_sub);                     // epilogue factor
   const int sub = blockIdx.x;
   if (sub >= *a.nsub) return;
   const int bin = a.sub_bin[sub];
@@ -65,40 +68,70 @@ __global__ void __launch_bounds__(kInterpWarps * 32) interp_kernel(const InterpP
   const int n = a.g.n;
   const int tid = threadIdx.x;
 
-  // stage the tile: (channel, row, cell) with cell fastest for coalesced global reads
+  // stage the tile: per-row global offsets and per-cell axis-2 offsets are tabulated first, then
+  // (channel, row, cell) elements are copied with cell fastest for coalesced global reads
+  __shared__ long long s_rowoff[T * T];
+  __shared__ int s_coloff[T];
+  for (int e = tid; e < T * T; e += blockDim.x) {
+    const int c0 = e / T, c1 = e - (e / T) * T;
+    int m0 = ts0 + c0, m1 = ts1 + c1;
+    bool ok = true;
+    if (KT == COV3D_KERNEL_ES) {
+      m0 = m0 >= n ? m0 - n : m0;
+      m1 = m1 >= n ? m1 - n : m1;
+    } else {
+      ok = m0 < n && m1 < n;
+    }
+    m0 += a.shift;
+    m1 += a.shift;
+    m0 = m0 >= n ? m0 - n : m0;
+    m1 = m1 >= n ? m1 - n : m1;
+    s_rowoff[e] = ok ? ((int64_t)m0 * n + m1) * n * a.cs : -1;
+  }
+  for (int e = tid; e < T; e += blockDim.x) {
+    int m2 = ts2 + e;
+    bool ok = true;
+    if (KT == COV3D_KERNEL_ES) {
+      m2 = m2 >= n ? m2 - n : m2;
+    } else {
+      ok = m2 < n;
+    }
+    m2 += a.shift;
+    m2 = m2 >= n ? m2 - n : m2;
+    s_coloff[e] = ok ? m2 : -1;
+  }
+  __syncthreads();
+  // the subproblem's point records and epilogue factors (Nyquist zeroing, CTF, scale)
+  for (int k = tid; k < cnt; k += blockDim.x) {
+    const SortedPoint sp = a.pts[first + k];
+    s_sp[k] = sp;
+    float sc = (a.nyquist && sp_nyquist(sp.idf)) ? 0.0f : a.scale;
+    if (a.ctf) sc *= __ldg(a.ctf + sp_id(sp.idf));
+    s_sc[k] = sc;
+  }
+  const float2 *gbase = a.grid + (int64_t)a.ch0 * a.chs;
+  // asynchronous copies global -> shared (8 bytes each, zero-filled outside the grid / past the
+  // pass's channels), all in flight before one wait
   for (int e = tid; e < CH * T * T * T; e += blockDim.x) {
     const int c2 = e % T;
     const int rowi = (e / T) % (T * T);
     const int ch = e / (T * T * T);
-    const int c0 = rowi / T, c1 = rowi - (rowi / T) * T;
-    int m0 = ts0 + c0, m1 = ts1 + c1, m2 = ts2 + c2;
-    float2 v = make_float2(0.f, 0.f);
-    bool ok = ch < a.nch;
-    if (KT == COV3D_KERNEL_ES) {
-      m0 = m0 >= n ? m0 - n : m0;
-      m1 = m1 >= n ? m1 - n : m1;
-      m2 = m2 >= n ? m2 - n : m2;
-    } else {
-      ok = ok && m0 < n && m1 < n && m2 < n;
-    }
-    if (ok) {
-      m0 += a.shift;
-      m1 += a.shift;
-      m2 += a.shift;
-      m0 = m0 >= n ? m0 - n : m0;
-      m1 = m1 >= n ? m1 - n : m1;
-      m2 = m2 >= n ? m2 - n : m2;
-      v = __ldg(a.grid + (((int64_t)m0 * n + m1) * n + m2) * a.cs + (int64_t)(a.ch0 + ch) * a.chs);
-    }
-    tile[(rowi * T + c2) * CH + ch] = v;
+    const long long ro = s_rowoff[rowi];
+    const int co = s_coloff[c2];
+    const bool ok = ch < a.nch && ro >= 0 && co >= 0;
+    const float2 *src = ok ? gbase + ro + (int64_t)co * a.cs + (int64_t)ch * a.chs : gbase;
+    const unsigned dst = (unsigned)__cvta_generic_to_shared(tile + (rowi * T + c2) * CH + ch);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(dst), "l"(src), "r"(ok ? 8 : 0) : "memory");
   }
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
   __syncthreads();
 
   const int warp = tid >> 5, lane = tid & 31;
   const int j = lane / CP, q = lane - (lane / CP) * CP;  // window cell along axis 2, channel pair
   float4 *wred = red + warp * 32;
   for (int k = warp; k < cnt; k += kInterpWarps) {
-    const SortedPoint sp = a.pts[first + k];
+    const SortedPoint sp = s_sp[k];
     int c0[3];
     c0[0] = first_cell<KT, W>(sp.t0);
     c0[1] = first_cell<KT, W>(sp.t1);
@@ -119,9 +152,9 @@ __global__ void __launch_bounds__(kInterpWarps * 32) interp_kernel(const InterpP
     const float wj = __shfl_sync(0xffffffffu, myw, 2 * W + (j < W ? j : 0));
     int l0 = c0[0], l1 = c0[1], l2 = c0[2];
     if (KT == COV3D_KERNEL_ES) {
-      l0 = pmod(l0, n);
-      l1 = pmod(l1, n);
-      l2 = pmod(l2, n);
+      l0 = wrap1(l0, n);
+      l1 = wrap1(l1, n);
+      l2 = wrap1(l2, n);
     }
     l0 -= ts0;
     l1 -= ts1;
@@ -163,8 +196,7 @@ __global__ void __launch_bounds__(kInterpWarps * 32) interp_kernel(const InterpP
       }
       // epilogue: vol_forward's Nyquist zeroing, CTF multiply and 1/L (projection_funcs.py:355-370)
       const int64_t id = sp_id(sp.idf);
-      float sc = (a.nyquist && sp_nyquist(sp.idf)) ? 0.0f : a.scale;
-      if (a.ctf) sc *= __ldg(a.ctf + id);
+      const float sc = s_sc[k];
       float2 *o = a.out + id * a.ops + (int64_t)(a.ch0 + 2 * lane) * a.ocs;
       if (2 * lane < a.nch) o[0] = make_float2(s.x * sc, s.y * sc);
       if (2 * lane + 1 < a.nch) o[a.ocs] = make_float2(s.z * sc, s.w * sc);
@@ -186,8 +218,9 @@ __global__ void interp_dead_kernel(const SortedPoint *__restrict__ pts, const in
 template <int KT, int W, int CP>
 int launch_cp(const InterpParams &a, int64_t max_blocks, cudaStream_t st) {
   constexpr int T = kBin + W - 1;
-  const size_t smem = ((size_t)T * T * T * CP + kInterpWarps * 32) * sizeof(float4);
-  if (smem > 48 * 1024) {
+  const size_t smem =
+      ((size_t)T * T * T * CP + kInterpWarps * 32) * sizeof(float4) + (size_t)a.max_sub * (sizeof(SortedPoint) + 4);
+  if (smem > 32 * 1024) {  // static shared arrays come on top of the dynamic size
     cudaError_t e = cudaFuncSetAttribute(interp_kernel<KT, W, CP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return check_cuda(e, "cudaFuncSetAttribute(interp_kernel)");
@@ -241,6 +274,7 @@ int launch_interp(cov3d_plan *p, const GridArgs &ga, int nchan, void *out, int64
   a.k = make_kernel(p);
   a.bins = p->bins;
   a.pts = p->sorted.as<SortedPoint>();
+  a.max_sub = p->max_sub;
   a.sub_bin = p->sub_bin.as<int>();
   a.sub_first = p->sub_first.as<int>();
   a.sub_count = p->sub_count.as<int>();

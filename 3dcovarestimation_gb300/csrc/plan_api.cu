@@ -305,7 +305,7 @@ int cov3d_plan_create(int L, int n_trans, double eps, const cov3d_opts *opts, co
   if (st == COV3D_OK) st = grow(p->gc1d, L * 4);
   if (st == COV3D_OK) st = check_cuda(cudaMemcpy(p->gc1d.ptr, gf.data(), L * 4, cudaMemcpyHostToDevice), "cudaMemcpy");
   if (st == COV3D_OK) st = grow(p->acc, 64 * sizeof(double));
-  if (st == COV3D_OK) st = build_row_order(p);
+  if (st == COV3D_OK) st = build_plane_schedule(p);
   if (st == COV3D_OK) st = check_cuda(cudaMallocHost(&p->h_acc, 64 * sizeof(double)), "cudaMallocHost");
   if (st != COV3D_OK || !p->ffts || !p->ev_pool || !p->ev_phase) {
     cov3d_plan_destroy(p);

@@ -1,17 +1,6 @@
 // Spreading ("type-1" half of the NUFFT; exact adjoint of interp.cu, replacing the
-// reference's grid_sample backward with FP32 global atomics, nufft_plan.py:171-242).
-//
-// One thread block per subproblem (<= max_sub points of one 8^3-cell spatial bin), no
-// shared-memory atomics on the data path:
-//  1. the block counting-sorts its points by their (axis-0, axis-1) window corner inside the
-//     bin (64 columns) and stores, per point, its axis-0/1 kernel weights, its axis-2 weights
-//     expanded over the tile row, and its CH channel values (times the im_backward prologue:
-//     CTF, Nyquist zeroing, scale);
-//  2. every thread owns one axis-2 row of the tile (bin + (W-1)-cell halo) and accumulates, in
-//     registers, every point whose window covers that row -- the points of the W x W columns
-//     around it, walked as one flattened list -- over the whole row; with COMP each register
-//     accumulator is Kahan-compensated;
-//  3. the tile is added to the global grid once, one complex atomic per cell and channel.
+// reference's grid_sample backward with FP32 global atomics, nufft_plan.py:171-242), over the
+// bin-sorted point records of points_sort.cu.  See spread_kernel for the decomposition.
 #include <algorithm>
 #include <vector>
 
@@ -21,8 +10,9 @@ namespace cov3d {
 
 namespace {
 
-constexpr int kBin = 8;           // bin edge (cells); plans use 8^3 bins
-constexpr int kSpreadThreads = 256;
+constexpr int kBin = 8;
+constexpr int kSpreadWarps = 8;
+constexpr int kPlanesPerWarp = 4;
 
 struct SpreadParams {
   PointGeom g;
@@ -36,6 +26,7 @@ struct SpreadParams {
   const float2 *vals;
   int64_t ips, ics;
   int ch0;
+  int nch;  // channels in this pass (<= 2 * CP)
   const float *ctf;
   int nyquist;
   float scale;
@@ -43,7 +34,7 @@ struct SpreadParams {
   int64_t cs, chs;
   int shift;
   int max_sub;
-  const int *row_order;  // tile rows (a << 8 | b) in decreasing order of work
+  const int *plane_sched;  // kSpreadWarps x kPlanesPerWarp tile planes per warp (-1 = none)
 };
 
 // Prologue factor of im_backward: CTF multiply, Nyquist zeroing, scale (projection_funcs.py:385-399).
@@ -54,51 +45,46 @@ __device__ __forceinline__ float prologue(const PointGeom &g, int64_t id, const 
   return sc;
 }
 
-template <int W, int CH>
-struct RowLayout {
-  static constexpr int T = kBin + W - 1;             // tile edge
-  static constexpr int T4 = (T + 3) / 4 * 4;         // axis-2 weights padded to float4
-  static constexpr int V = 2 * CH;                   // channel values (re, im)
-  static constexpr int V4 = (V + 3) / 4 * 4;
-  static constexpr int W0 = T4 + V4;                 // axis-0 weights
-  static constexpr int W1 = W0 + W;                  // axis-1 weights
-  static constexpr int S4 = (W1 + W + 3) / 4;        // float4 groups per record, made odd so that
-  static constexpr int STRIDE = 4 * (S4 % 2 ? S4 : S4 + 1);  // records of different points start on
-                                                              // different bank groups
+// Channel pairs per pass (lanes are (window cell, channel pair)); COMP keeps a second
+// (compensation) tile, so it uses half as many pairs.
+template <int W, bool COMP>
+struct SpreadCP {
+  // largest W*CP <= 32 whose tile plus staged point values fit in shared memory
+  static constexpr int full = W <= 2 ? 8 : W == 4 ? 7 : W == 8 ? 3 : 32 / W;
+  static constexpr int value = COMP ? (full / 2 > 0 ? full / 2 : 1) : full;
 };
 
-// Number of bin columns along one axis whose window reaches tile row coordinate x.
+// Per-point record staged once per block: packed window corner (tile-local, biased by 32 so
+// zero-padding corners below the tile stay non-negative) and the 3W kernel weights.
 template <int W>
-__device__ constexpr int reach(int x) {
-  const int lo = x - W + 1 > 0 ? x - W + 1 : 0;
-  const int hi = x < kBin - 1 ? x : kBin - 1;
-  return hi >= lo ? hi - lo + 1 : 0;
-}
+struct PointRec {
+  static constexpr int FLOATS = (1 + 3 * W + 3) / 4 * 4;
+};
 
-template <int KT, int W, int CH>
-__device__ __forceinline__ void local_corner(const SpreadParams &a, float t, int ts, int &l, float *wt) {
-  int c0 = taps<KT, W>(t, a.k.beta, wt);
-  if (KT == COV3D_KERNEL_ES) c0 = pmod(c0, a.g.n);
-  l = c0 - ts;
-}
-
-template <int KT, int W>
-__device__ __forceinline__ int local_first(const SpreadParams &a, float t, int ts) {
-  int c0 = first_cell<KT, W>(t);
-  if (KT == COV3D_KERNEL_ES) c0 = pmod(c0, a.g.n);
-  return c0 - ts;
-}
-
-template <int KT, int W, int CH, bool COMP>
-__global__ void __launch_bounds__(kSpreadThreads, 2) spread_kernel(const SpreadParams a) {
-  using Lay = RowLayout<W, CH>;
-  constexpr int T = Lay::T;
+// One block per subproblem, tile = bin + (W-1)-cell halo of 2*CP channels in shared memory.
+//  1. the block buckets its points by the axis-0 corner of their window (8 buckets);
+//  2. warp w owns whole axis-0 planes of the tile (plane_sched balances the work: plane a is
+//     reached by the points of min(W, ...) buckets); for every point reaching one of its planes
+//     the warp's lanes (j, q) add weight * value to channels 2q, 2q+1 of tile[a][b][corner2 + j]
+//     for the W rows b of the window -- contiguous 16-byte read-modify-writes, no bank
+//     conflicts, and no two warps ever touch the same cell, so no atomics;
+//     with COMP every addition is a TwoSum whose rounding error goes to the second tile;
+//  3. the tile is added to the global grid, one complex atomic per cell and channel.
+template <int KT, int W, int CP, bool COMP>
+__global__ void __launch_bounds__(kSpreadWarps * 32) spread_kernel(const SpreadParams a) {
+  constexpr int T = kBin + W - 1;
+  constexpr int RG = 32 / (W * CP);  // window rows handled side by side by spare lanes
+  constexpr int LANES = W * CP * RG;
+  constexpr int TILE4 = T * T * T * CP;
   extern __shared__ float4 smem4[];
-  int *s_cnt = reinterpret_cast<int *>(smem4);     // kBin*kBin
-  int *s_off = s_cnt + kBin * kBin;                 // kBin*kBin + 1 (+3 pad)
-  int *s_col = s_off + kBin * kBin + 4;             // max_sub
-  int *s_rank = s_col + a.max_sub;                  // max_sub
-  float *s_rec = reinterpret_cast<float *>(s_rank + a.max_sub);  // max_sub * STRIDE
+  float4 *hi = smem4;
+  float4 *lo = smem4 + (COMP ? TILE4 : 0);
+  float4 *s_val = smem4 + (COMP ? 2 : 1) * TILE4;  // max_sub * CP: scaled channel pairs per point
+  float *s_rec = reinterpret_cast<float *>(s_val + a.max_sub * CP);  // max_sub * PointRec<W>::FLOATS
+  int *s_idx = reinterpret_cast<int *>(s_rec + a.max_sub * PointRec<W>::FLOATS);
+  int *s_bucket = s_idx + a.max_sub;
+  int *s_cnt = s_bucket + a.max_sub;  // kBin
+  int *s_off = s_cnt + kBin;          // kBin + 1
 
   const int sub = blockIdx.x;
   if (sub >= *a.nsub) return;
@@ -112,218 +98,220 @@ __global__ void __launch_bounds__(kSpreadThreads, 2) spread_kernel(const SpreadP
   const int n = a.g.n;
   const int tid = threadIdx.x;
 
-  for (int i = tid; i < kBin * kBin; i += blockDim.x) s_cnt[i] = 0;
+  for (int e = tid; e < (COMP ? 2 : 1) * TILE4; e += blockDim.x) smem4[e] = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (tid < kBin) s_cnt[tid] = 0;
   __syncthreads();
-  // 1a. column of every point (window corner on axes 0, 1 inside the bin) and its rank
+  // 1. stage the points' scaled values (im_backward prologue folded in) and bucket the points
+  //    by axis-0 window corner
+  for (int e = tid; e < cnt * CP; e += blockDim.x) {
+    const int k = e / CP, qq = e - (e / CP) * CP;
+    const SortedPoint sp = a.pts[first + k];
+    const int64_t id = sp_id(sp.idf);
+    float sc = (a.nyquist && sp_nyquist(sp.idf)) ? 0.0f : a.scale;
+    if (a.ctf) sc *= __ldg(a.ctf + id);
+    const float2 *src = a.vals + id * a.ips + (int64_t)(a.ch0 + 2 * qq) * a.ics;
+    const float2 v0 = 2 * qq < a.nch ? __ldg(src) : make_float2(0.f, 0.f);
+    const float2 v1 = 2 * qq + 1 < a.nch ? __ldg(src + a.ics) : make_float2(0.f, 0.f);
+    s_val[e] = make_float4(v0.x * sc, v0.y * sc, v1.x * sc, v1.y * sc);
+  }
   for (int k = tid; k < cnt; k += blockDim.x) {
     const SortedPoint sp = a.pts[first + k];
-    const int l0 = local_first<KT, W>(a, sp.t0, ts0);
-    const int l1 = local_first<KT, W>(a, sp.t1, ts1);
-    const int col = max(l0, 0) * kBin + max(l1, 0);
-    s_col[k] = col;
-    s_rank[k] = atomicAdd(s_cnt + col, 1);
+    float w0[W], w1[W], w2[W];
+    int c0 = taps<KT, W>(sp.t0, a.k.beta, w0);
+    int c1 = taps<KT, W>(sp.t1, a.k.beta, w1);
+    int c2 = taps<KT, W>(sp.t2, a.k.beta, w2);
+    if (KT == COV3D_KERNEL_ES) {
+      c0 = wrap1(c0, n);
+      c1 = wrap1(c1, n);
+      c2 = wrap1(c2, n);
+    }
+    float *rec = s_rec + k * PointRec<W>::FLOATS;
+    rec[0] = __int_as_float((c0 - ts0 + 32) | ((c1 - ts1 + 32) << 8) | ((c2 - ts2 + 32) << 16));
+#pragma unroll
+    for (int r = 0; r < W; ++r) {
+      rec[1 + r] = w0[r];
+      rec[1 + W + r] = w1[r];
+      rec[1 + 2 * W + r] = w2[r];
+    }
+    const int b0 = max(c0 - ts0, 0);
+    s_bucket[k] = b0 | (atomicAdd(s_cnt + b0, 1) << 4);
   }
   __syncthreads();
   if (tid == 0) {
     int acc = 0;
-    for (int i = 0; i < kBin * kBin; ++i) {
+    for (int i = 0; i < kBin; ++i) {
       s_off[i] = acc;
       acc += s_cnt[i];
     }
-    s_off[kBin * kBin] = acc;
+    s_off[kBin] = acc;
   }
   __syncthreads();
-  // 1b. point records in column order
   for (int k = tid; k < cnt; k += blockDim.x) {
-    const SortedPoint sp = a.pts[first + k];
-    const int64_t id = sp_id(sp.idf);
-    float w0[W], w1[W], w2[W];
-    int l0, l1, l2;
-    local_corner<KT, W, CH>(a, sp.t0, ts0, l0, w0);
-    local_corner<KT, W, CH>(a, sp.t1, ts1, l1, w1);
-    local_corner<KT, W, CH>(a, sp.t2, ts2, l2, w2);
-    float *rec = s_rec + (s_off[s_col[k]] + s_rank[k]) * Lay::STRIDE;
-    float sc = (a.nyquist && sp_nyquist(sp.idf)) ? 0.0f : a.scale;
-    if (a.ctf) sc *= __ldg(a.ctf + id);
-#pragma unroll
-    for (int c = 0; c < Lay::T4; ++c) rec[c] = 0.0f;
-#pragma unroll
-    for (int j = 0; j < W; ++j) {
-      const int c = l2 + j;
-      if (c >= 0 && c < T) rec[c] = w2[j];
-    }
-    const float2 *src = a.vals + id * a.ips + (int64_t)a.ch0 * a.ics;
-#pragma unroll
-    for (int c = 0; c < CH; ++c) {
-      const float2 x = sc != 0.0f ? __ldg(src + c * a.ics) : make_float2(0.f, 0.f);
-      rec[Lay::T4 + 2 * c] = x.x * sc;
-      rec[Lay::T4 + 2 * c + 1] = x.y * sc;
-    }
-    // zero padding (grid_sample kernels): window cells below the grid were clamped into bin 0;
-    // shift their weights so that index (row - corner) still addresses the right tap
-    const int s0 = max(-l0, 0), s1 = max(-l1, 0);
-#pragma unroll
-    for (int j = 0; j < W; ++j) {
-      rec[Lay::W0 + j] = 0.0f;
-      rec[Lay::W1 + j] = 0.0f;
-    }
-#pragma unroll
-    for (int j = 0; j < W; ++j) {
-      if (j >= s0) rec[Lay::W0 + j - s0] = w0[j];
-      if (j >= s1) rec[Lay::W1 + j - s1] = w1[j];
-    }
+    const int bk = s_bucket[k];
+    s_idx[s_off[bk & 15] + (bk >> 4)] = k;
   }
   __syncthreads();
 
-  // 2. one axis-2 row of the tile per thread.  The thread walks the points of the W x W
-  //    columns around its row as one flattened list, so the lanes of a warp stay converged
-  //    (their totals differ far less than their per-column counts).  Rows are handed out in
-  //    decreasing order of the number of columns that reach them (halo rows see fewer), so
-  //    the rows of one warp carry similar work.
-  if (tid >= T * T) return;
-  const int packed = __ldg(a.row_order + tid);
-  const int ra = packed >> 8, rb = packed & 255;
-  float2 acc[T][CH];
-  float2 cmp[COMP ? T : 1][COMP ? CH : 1];
+  // 2. planes of this warp
+  const int warp = tid >> 5, lane = tid & 31;
+  const int g = lane / (W * CP), lr = lane - g * (W * CP);
+  const int j = lr / CP, q = lr - (lr / CP) * CP;
+  const bool lane_live = lane < LANES;
+  for (int s = 0; s < kPlanesPerWarp; ++s) {
+    const int pa = __ldg(a.plane_sched + warp * kPlanesPerWarp + s);
+    if (pa < 0) break;
+    const int blo = max(0, pa - W + 1), bhi = min(kBin - 1, pa);
+    const int i1end = s_off[bhi + 1];
+    for (int i = s_off[blo]; i < i1end; ++i) {
+      const int kp = s_idx[i];
+      const float *rec = s_rec + kp * PointRec<W>::FLOATS;
+      const int packed = __float_as_int(rec[0]);
+      const int l0 = (packed & 255) - 32, l1 = ((packed >> 8) & 255) - 32, l2 = ((packed >> 16) & 255) - 32;
+      const int o0 = pa - l0;  // tap along axis 0 that lands on this plane
+      if (o0 >= W) continue;   // zero padding: window clamped into bucket 0 but below this plane
+      const int cell2 = l2 + j;
+      if (!lane_live || cell2 < 0) continue;
+      const float4 vv = s_val[kp * CP + q];
+      const float waj = rec[1 + o0] * rec[1 + 2 * W + j];
+      float4 *rowp = hi + ((pa * T) * T + cell2) * CP + q;
+      float4 *rowl = lo + ((pa * T) * T + cell2) * CP + q;
 #pragma unroll
-  for (int c = 0; c < T; ++c)
-#pragma unroll
-    for (int h = 0; h < CH; ++h) {
-      acc[c][h] = make_float2(0.f, 0.f);
-      if (COMP) cmp[COMP ? c : 0][COMP ? h : 0] = make_float2(0.f, 0.f);
-    }
-  int next = 0, p = 0, pend = 0, o0 = 0, o1 = 0;
-  while (true) {
-    while (p >= pend && next < W * W) {
-      const int d0 = next / W, d1 = next - (next / W) * W;
-      ++next;
-      const int l0 = ra - d0, l1 = rb - d1;
-      if (l0 < 0 || l0 >= kBin || l1 < 0 || l1 >= kBin) continue;
-      p = s_off[l0 * kBin + l1];
-      pend = s_off[l0 * kBin + l1 + 1];
-      o0 = d0;
-      o1 = d1;
-    }
-    if (p >= pend) break;
-    const float *rec = s_rec + p * Lay::STRIDE;
-    ++p;
-    const float wab = rec[Lay::W0 + o0] * rec[Lay::W1 + o1];
-    float w2[Lay::T4];
-#pragma unroll
-    for (int q = 0; q < Lay::T4 / 4; ++q) {
-      const float4 x = reinterpret_cast<const float4 *>(rec)[q];
-      w2[4 * q] = x.x;
-      w2[4 * q + 1] = x.y;
-      w2[4 * q + 2] = x.z;
-      w2[4 * q + 3] = x.w;
-    }
-    float v[Lay::V4];
-#pragma unroll
-    for (int q = 0; q < Lay::V4 / 4; ++q) {
-      const float4 x = reinterpret_cast<const float4 *>(rec + Lay::T4)[q];
-      v[4 * q] = x.x;
-      v[4 * q + 1] = x.y;
-      v[4 * q + 2] = x.z;
-      v[4 * q + 3] = x.w;
-    }
-#pragma unroll
-    for (int c = 0; c < T; ++c) {
-      const float w = wab * w2[c];
-#pragma unroll
-      for (int h = 0; h < CH; ++h) {
+      for (int ii = 0; ii < (W + RG - 1) / RG; ++ii) {
+        const int i1 = ii * RG + g;
+        if (i1 >= W) break;
+        const int r1 = l1 + i1;
+        if (KT != COV3D_KERNEL_ES && r1 < 0) continue;
+        const float w = waj * rec[1 + W + i1];
+        float4 &h = rowp[r1 * T * CP];
         if (!COMP) {
-          acc[c][h].x = fmaf(w, v[2 * h], acc[c][h].x);
-          acc[c][h].y = fmaf(w, v[2 * h + 1], acc[c][h].y);
+          float4 x = h;
+          x.x = fmaf(w, vv.x, x.x);
+          x.y = fmaf(w, vv.y, x.y);
+          x.z = fmaf(w, vv.z, x.z);
+          x.w = fmaf(w, vv.w, x.w);
+          h = x;
         } else {
-          float y = w * v[2 * h] - cmp[COMP ? c : 0][COMP ? h : 0].x;
-          float t2 = acc[c][h].x + y;
-          cmp[COMP ? c : 0][COMP ? h : 0].x = (t2 - acc[c][h].x) - y;
-          acc[c][h].x = t2;
-          y = w * v[2 * h + 1] - cmp[COMP ? c : 0][COMP ? h : 0].y;
-          t2 = acc[c][h].y + y;
-          cmp[COMP ? c : 0][COMP ? h : 0].y = (t2 - acc[c][h].y) - y;
-          acc[c][h].y = t2;
+          float4 x = h, e = rowl[r1 * T * CP];
+          const float d[4] = {w * vv.x, w * vv.y, w * vv.z, w * vv.w};
+          float *xs = &x.x, *es = &e.x;
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const float s2 = xs[u] + d[u];
+            const float bb = s2 - xs[u];
+            es[u] += (xs[u] - (s2 - bb)) + (d[u] - bb);
+            xs[u] = s2;
+          }
+          h = x;
+          rowl[r1 * T * CP] = e;
         }
       }
     }
   }
+  __syncthreads();
 
-  // 3. add the row to the global grid
-  int m0 = ts0 + ra, m1 = ts1 + rb;
-  if (KT == COV3D_KERNEL_ES) {
+  // 3. add the tile to the global grid: per-row global offsets and per-cell axis-2 offsets first
+  long long *s_rowoff = reinterpret_cast<long long *>(s_val);  // reuses the staged values
+  int *s_coloff = reinterpret_cast<int *>(s_rowoff + T * T);
+  for (int e = tid; e < T * T; e += blockDim.x) {
+    const int ra = e / T, rb = e - (e / T) * T;
+    int m0 = ts0 + ra, m1 = ts1 + rb;
+    bool ok = true;
+    if (KT == COV3D_KERNEL_ES) {
+      m0 = m0 >= n ? m0 - n : m0;
+      m1 = m1 >= n ? m1 - n : m1;
+    } else {
+      ok = m0 < n && m1 < n;
+    }
+    m0 += a.shift;
+    m1 += a.shift;
     m0 = m0 >= n ? m0 - n : m0;
     m1 = m1 >= n ? m1 - n : m1;
-  } else if (m0 >= n || m1 >= n) {
-    return;
+    s_rowoff[e] = ok ? ((int64_t)m0 * n + m1) * n : -1;
   }
-  m0 += a.shift;
-  m1 += a.shift;
-  m0 = m0 >= n ? m0 - n : m0;
-  m1 = m1 >= n ? m1 - n : m1;
-  const int64_t row = ((int64_t)m0 * n + m1) * n;
-#pragma unroll
-  for (int c = 0; c < T; ++c) {
-    int m2 = ts2 + c;
+  for (int e = tid; e < T; e += blockDim.x) {
+    int m2 = ts2 + e;
+    bool ok = true;
     if (KT == COV3D_KERNEL_ES) {
       m2 = m2 >= n ? m2 - n : m2;
-    } else if (m2 >= n) {
-      continue;
+    } else {
+      ok = m2 < n;
     }
     m2 += a.shift;
     m2 = m2 >= n ? m2 - n : m2;
-    float2 *dst = a.grid + (row + m2) * a.cs + (int64_t)a.ch0 * a.chs;
-#pragma unroll
-    for (int h = 0; h < CH; ++h) {
-      float2 val = acc[c][h];
-      if (COMP) {
-        val.x -= cmp[COMP ? c : 0][COMP ? h : 0].x;
-        val.y -= cmp[COMP ? c : 0][COMP ? h : 0].y;
-      }
-      if (val.x != 0.0f || val.y != 0.0f) atomicAdd(dst + h * a.chs, val);
+    s_coloff[e] = ok ? m2 : -1;
+  }
+  __syncthreads();
+  for (int e = tid; e < TILE4; e += blockDim.x) {
+    const int qq = e % CP;
+    const int cell = e / CP;
+    const int cc = cell % T, rowi = cell / T;
+    const long long ro = s_rowoff[rowi];
+    const int co = s_coloff[cc];
+    if (ro < 0 || co < 0) continue;
+    float4 x = hi[e];
+    if (COMP) {
+      const float4 c = lo[e];
+      x.x += c.x;
+      x.y += c.y;
+      x.z += c.z;
+      x.w += c.w;
     }
+    float2 *dst = a.grid + (ro + co) * a.cs + (int64_t)(a.ch0 + 2 * qq) * a.chs;
+    if (2 * qq < a.nch && (x.x != 0.0f || x.y != 0.0f)) atomicAdd(dst, make_float2(x.x, x.y));
+    if (2 * qq + 1 < a.nch && (x.z != 0.0f || x.w != 0.0f)) atomicAdd(dst + a.chs, make_float2(x.z, x.w));
   }
 }
 
-template <int KT, int W, int CH, bool COMP>
-size_t smem_bytes(int max_sub) {
-  return (size_t)(2 * kBin * kBin + 8 + 2 * max_sub) * sizeof(int) +
-         (size_t)max_sub * RowLayout<W, CH>::STRIDE * sizeof(float);
-}
-
-template <int KT, int W, int CH, bool COMP>
+template <int KT, int W, int CP, bool COMP>
 int launch_one(const SpreadParams &a, int64_t max_blocks, cudaStream_t st) {
-  const size_t smem = smem_bytes<KT, W, CH, COMP>(a.max_sub);
-  if (smem > 200 * 1024) {
-    set_error("spread tile records of %zu bytes exceed shared memory", smem);
+  constexpr int T = kBin + W - 1;
+  const size_t smem = (size_t)(COMP ? 2 : 1) * T * T * T * CP * sizeof(float4) +
+                      (size_t)a.max_sub * (CP * sizeof(float4) + PointRec<W>::FLOATS * 4 + 2 * sizeof(int)) +
+                      (2 * kBin + 1) * sizeof(int);
+  if (smem > 227 * 1024) {
+    set_error("spreading tile of %zu bytes exceeds shared memory", smem);
     return COV3D_EINVAL;
   }
-  if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(spread_kernel<KT, W, CH, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  if (smem > 32 * 1024) {  // static shared arrays come on top of the dynamic size
+    cudaError_t e = cudaFuncSetAttribute(spread_kernel<KT, W, CP, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return check_cuda(e, "cudaFuncSetAttribute(spread_kernel)");
   }
-  spread_kernel<KT, W, CH, COMP><<<(unsigned)max_blocks, kSpreadThreads, smem, st>>>(a);
+  spread_kernel<KT, W, CP, COMP><<<(unsigned)max_blocks, kSpreadWarps * 32, smem, st>>>(a);
   return launched("spread_kernel");
 }
 
-template <int KT, int W>
-int launch_w(SpreadParams a, int nchan, bool comp, int64_t max_blocks, cudaStream_t st) {
+template <int KT, int W, bool COMP>
+int launch_wc(SpreadParams a, int nchan, int64_t max_blocks, cudaStream_t st) {
+  constexpr int CPMAX = SpreadCP<W, COMP>::value;
   int done = 0;
   while (done < nchan) {
     const int left = nchan - done;
     a.ch0 = done;
-    int s = COV3D_OK, ch = 1;
-    if (comp) {
-      ch = 1;
-      s = launch_one<KT, W, 1, true>(a, max_blocks, st);
+    int s = COV3D_OK, ch = 0;
+    if (left >= 2 * CPMAX || left > 4) {
+      ch = left < 2 * CPMAX ? left : 2 * CPMAX;
+      a.nch = ch;
+      s = launch_one<KT, W, CPMAX, COMP>(a, max_blocks, st);
+    } else if (left > 2) {
+      ch = left;
+      a.nch = ch;
+      s = launch_one<KT, W, (CPMAX > 2 ? 2 : CPMAX), COMP>(a, max_blocks, st);
+      if (CPMAX < 2) ch = 2 * CPMAX;
     } else {
-      ch = left >= 2 ? 2 : 1;
-      s = ch == 2 ? launch_one<KT, W, 2, false>(a, max_blocks, st) : launch_one<KT, W, 1, false>(a, max_blocks, st);
+      ch = left;
+      a.nch = ch;
+      s = launch_one<KT, W, 1, COMP>(a, max_blocks, st);
     }
     if (s != COV3D_OK) return s;
     done += ch;
   }
   return COV3D_OK;
+}
+
+template <int KT, int W>
+int launch_w(SpreadParams a, int nchan, bool comp, int64_t max_blocks, cudaStream_t st) {
+  return comp ? launch_wc<KT, W, true>(a, nchan, max_blocks, st) : launch_wc<KT, W, false>(a, nchan, max_blocks, st);
 }
 
 // Per-image adjoint (no sum over images): direct global atomics, one thread per point.
@@ -367,24 +355,35 @@ __global__ void spread_unagg_kernel(PointGeom g, KernelSpec k, int64_t M, const 
 
 }  // namespace
 
-int build_row_order(cov3d_plan *p) {
+// Tile planes (axis-0 index a of the bin + halo tile) per warp.  Plane a is reached by the
+// points whose axis-0 window corner lies in [a - W + 1, a] (clipped to the bin): planes are
+// assigned greedily, heaviest first, to the least loaded warp, so all warps get equal work.
+int build_plane_schedule(cov3d_plan *p) {
   const int W = p->kernel == COV3D_KERNEL_NEAREST ? 1 : p->kernel == COV3D_KERNEL_LINEAR ? 2 : p->width;
   const int T = kBin + W - 1;
-  auto reach_h = [&](int x) {
+  std::vector<int> order(T), load(kSpreadWarps, 0), count(kSpreadWarps, 0);
+  std::vector<int> sched(kSpreadWarps * kPlanesPerWarp, -1);
+  auto reach = [&](int x) {
     const int lo = x - W + 1 > 0 ? x - W + 1 : 0;
     const int hi = x < kBin - 1 ? x : kBin - 1;
     return hi >= lo ? hi - lo + 1 : 0;
   };
-  std::vector<int> rows(T * T);
-  for (int q = 0; q < T * T; ++q) rows[q] = q;
-  std::stable_sort(rows.begin(), rows.end(), [&](int x, int y) {
-    return reach_h(x / T) * reach_h(x % T) > reach_h(y / T) * reach_h(y % T);
-  });
-  std::vector<int> packed(T * T);
-  for (int i = 0; i < T * T; ++i) packed[i] = ((rows[i] / T) << 8) | (rows[i] % T);
-  COV3D_TRY(grow(p->row_order, (int64_t)packed.size() * 4));
-  return check_cuda(cudaMemcpy(p->row_order.ptr, packed.data(), packed.size() * 4, cudaMemcpyHostToDevice),
-                    "cudaMemcpy(row_order)");
+  for (int i = 0; i < T; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return reach(x) > reach(y); });
+  for (int pa : order) {
+    int best = -1;
+    for (int w = 0; w < kSpreadWarps; ++w)
+      if (count[w] < kPlanesPerWarp && (best < 0 || load[w] < load[best])) best = w;
+    if (best < 0) {
+      set_error("cannot schedule %d tile planes", T);
+      return COV3D_EINVAL;
+    }
+    sched[best * kPlanesPerWarp + count[best]++] = pa;
+    load[best] += reach(pa);
+  }
+  COV3D_TRY(grow(p->row_order, (int64_t)sched.size() * 4));
+  return check_cuda(cudaMemcpy(p->row_order.ptr, sched.data(), sched.size() * 4, cudaMemcpyHostToDevice),
+                    "cudaMemcpy(plane schedule)");
 }
 
 int launch_spread(cov3d_plan *p, const void *values, int64_t in_ps, int64_t in_cs, int nchan, const EpilogueArgs &e,
@@ -413,7 +412,7 @@ int launch_spread(cov3d_plan *p, const void *values, int64_t in_ps, int64_t in_c
   a.chs = chan_stride;
   a.shift = shift;
   a.max_sub = p->max_sub;
-  a.row_order = p->row_order.as<int>();
+  a.plane_sched = p->row_order.as<int>();
   if (p->bins.bs[0] != kBin || p->bins.bs[1] != kBin || p->bins.bs[2] != kBin) {
     set_error("spreading requires %d^3-cell bins", kBin);
     return COV3D_EINVAL;

@@ -6,8 +6,10 @@ The directory name starts with a digit, so import it with
 ``importlib.import_module("3dcovarestimation_gb300")``.
 """
 
-from . import _lib, wiener_coords
+from . import _lib, mean, wiener_coords
 from .covar import Covar, Mean
+from .mean import (MeanBackprojector, cg_solve, circulant_symbol, complex_conjugate_gradient,
+                   correct_upsampling_padding, get_grid_correction, reconstruct_mean, regularize_lhs, solve_mean)
 from .covar_sgd import (CovarTrainer, FusedCovarStep, ProjectedCost, cost, cost_fourier_domain,
                         cost_maximum_liklihood, cost_maximum_liklihood_fourier_domain, raw_cost_fourier_domain,
                         raw_cost_maximum_liklihood_fourier_domain)

@@ -72,6 +72,12 @@ _SIGNATURES = {
                                          c_void_p, c_double, c_void_p, c_void_p, c_void_p, c_void_p]),
     "cov3d_wpass": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_int64, c_int64, c_int64, c_void_p, c_void_p,
                             c_void_p, c_void_p, c_int64, c_int64, c_int64]),
+    "cov3d_mean_accumulate": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int]),
+    "cov3d_regularize_lhs": (c_int, [c_void_p, c_void_p, c_void_p]),
+    "cov3d_mean_init": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "cov3d_circulant_symbol": (c_int, [c_void_p, c_void_p, c_void_p]),
+    "cov3d_cg_solve": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_double, c_int, c_int, c_void_p,
+                               ctypes.POINTER(c_int), ctypes.POINTER(c_double), c_void_p]),
 }
 
 _lib = None

@@ -125,6 +125,7 @@ struct cov3d_plan {
   cov3d::DevBuf q;             // per-point values (points * r) complex
   cov3d::DevBuf small;         // per-image small matrices
   cov3d::DevBuf acc;           // double accumulators
+  cov3d::DevBuf cgw;           // mean / CG workspace (state, vectors, shell sums)
   double *h_acc = nullptr;     // pinned host mirror of acc (64 doubles)
   std::map<int, cufftHandle> *ffts = nullptr;  // cuFFT plans by channel count
 

@@ -62,3 +62,30 @@ def ctf_images(defocus_um, L, pixel_size, voltage_kv=300.0, cs_mm=2.7, amplitude
     chi = math.pi * lam * df * k2 - 0.5 * math.pi * cs * lam**3 * k2 * k2
     A = amplitude_contrast
     return (-(math.sqrt(1 - A * A) * torch.sin(chi) + A * torch.cos(chi))).to(torch.float32)
+
+
+def vmf_cluster_rotations(n, clusters=8, kappa=5.0, generator=None, device="cuda"):
+    """(n, 3, 3) rotations whose viewing directions (third column, the normal of the projected
+    Fourier plane) follow an equal-weight mixture of ``clusters`` von Mises-Fisher
+    distributions on the sphere with concentration ``kappa`` (centres uniform), with a uniform
+    in-plane angle.  Gives an anisotropic sampling of Fourier space."""
+    g = generator
+    dev = torch.device(device)
+    cen = torch.randn((clusters, 3), generator=g, device=dev, dtype=torch.float64)
+    cen = cen / cen.norm(dim=1, keepdim=True)
+    mu = cen[torch.randint(0, clusters, (n,), generator=g, device=dev)]
+    # Wood's method on S^2: w = 1 + log(u + (1 - u) e^{-2 kappa}) / kappa
+    u = torch.rand((n,), generator=g, device=dev, dtype=torch.float64)
+    w = 1.0 + torch.log(u + (1.0 - u) * math.exp(-2.0 * kappa)) / kappa
+    v = torch.randn((n, 3), generator=g, device=dev, dtype=torch.float64)
+    v = v - (v * mu).sum(1, keepdim=True) * mu
+    v = v / v.norm(dim=1, keepdim=True)
+    d = w[:, None] * mu + torch.sqrt(torch.clamp(1.0 - w * w, min=0.0))[:, None] * v
+    a = torch.randn((n, 3), generator=g, device=dev, dtype=torch.float64)
+    a = a - (a * d).sum(1, keepdim=True) * d
+    a = a / a.norm(dim=1, keepdim=True)
+    b = torch.cross(d, a, dim=1)
+    th = torch.rand((n, 1), generator=g, device=dev, dtype=torch.float64) * (2 * math.pi)
+    e1 = torch.cos(th) * a + torch.sin(th) * b
+    e2 = torch.cross(d, e1, dim=1)
+    return torch.stack([e1, e2, d], dim=2).to(torch.float32)

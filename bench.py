@@ -47,6 +47,11 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--seed", type=int, default=2000)
     ap.add_argument("--uncompensated", action="store_true", help="plain FP32 spreading (no Kahan terms)")
+    ap.add_argument("--mean-images", type=int, default=300000, help="images backprojected for the mean-CG solve")
+    ap.add_argument("--mean-L", type=int, default=128)
+    ap.add_argument("--mean-rtol", type=float, default=1e-5)
+    ap.add_argument("--mean-maxiter", type=int, default=6000)
+    ap.add_argument("--no-mean", action="store_true", help="skip the mean-CG measurement")
     return ap.parse_args()
 
 
@@ -181,6 +186,65 @@ def make_dataset(pkg, args, dev, n_images):
     noise_var = signal_var / 0.05
     images += torch.randn(images.shape, generator=g, device=dev, dtype=torch.complex64) * (noise_var ** 0.5)
     return images, rot, ctf.reshape(n_images, -1), noise_var
+
+
+def run_mean_cg(pkg, args, dev):
+    """Mean reconstruction at L = args.mean_L from args.mean_images images whose viewing
+    directions follow a mixture of 8 von Mises-Fisher clusters (kappa 5): backprojection
+    throughput, then wall time and iterations of the padding CG to relative residual
+    args.mean_rtol with each preconditioner."""
+    import torch
+
+    from importlib import import_module
+
+    syn = import_module("3dcovarestimation_gb300.synthetic")
+    mean = import_module("3dcovarestimation_gb300.mean")
+    L, B, N = args.mean_L, args.batch, args.mean_images
+    g = torch.Generator(device=dev).manual_seed(args.seed + 4000)
+    vol = syn.gaussian_blob_volumes(1, L, generator=g, device=dev)
+    rot = syn.vmf_cluster_rotations(N, 8, 5.0, generator=g, device=dev)
+    fwd = pkg.NufftPlan((L,) * 3, batch_size=1, device=dev, width=args.width)
+    acc = mean.MeanBackprojector(L, 2, dev)
+    stream = torch.cuda.current_stream()
+    bp_ms = 0.0
+    noise_sd = None
+    for i in range(0, N, B):
+        rb = rot[i:i + B]
+        defocus = torch.rand((rb.shape[0],), generator=g, device=dev) * 2.0 + 1.0
+        ctf = syn.ctf_images(defocus, L, 1.5, device=dev)
+        fwd.setrot(rb)
+        img = pkg.vol_forward(vol, fwd, ctf, fourier_domain=True)[:, 0]
+        if noise_sd is None:
+            noise_sd = (float((img.abs() ** 2).mean()) / 0.05) ** 0.5
+        img = img + torch.randn(img.shape, generator=g, device=dev, dtype=torch.complex64) * noise_sd
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        acc.add(img, ctf, rotations=rb)
+        e1.record(stream)
+        e1.synchronize()
+        bp_ms += e0.elapsed_time(e1)
+    reg = mean.regularize_lhs(acc.lhs)
+    plan = mean._MeanSolver.get(L, 2, dev)
+    b = torch.empty((L,) * 3, dtype=torch.complex64, device=dev)
+    x0 = torch.empty_like(b)
+    pkg._lib.call("cov3d_mean_init", plan.bind(), pkg._lib.ptr(acc.rhs.contiguous()), pkg._lib.ptr(reg),
+                  pkg._lib.ptr(b), pkg._lib.ptr(x0))
+    out = {"workload": f"mean at L={L}, {N} images, viewing directions from 8 vMF clusters (kappa 5), "
+                       f"nearest plan at upsampling 2, CG to relative residual {args.mean_rtol}",
+           "backprojection_images_per_s": N / (bp_ms / 1e3), "rtol": args.mean_rtol,
+           "maxiter": args.mean_maxiter}
+    # warm the cuFFT plans and the symbol path once
+    mean.cg_solve(reg, b, x0, L, rtol=1e-1, maxiter=2, precond="circulant")
+    mean.cg_solve(reg, b, x0, L, rtol=1e-1, maxiter=2, precond="diagonal")
+    for name, pc in (("plain", None), ("diagonal_pc", "diagonal"), ("circulant_pc", "circulant")):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        x, info = mean.cg_solve(reg, b, x0, L, rtol=args.mean_rtol, maxiter=args.mean_maxiter, precond=pc)
+        torch.cuda.synchronize()
+        sec = time.perf_counter() - t0
+        out[name] = {"seconds": sec, "iters": info.iters, "relres": info.relres, "converged": info.converged,
+                     "ms_per_iter": 1e3 * sec / max(1, info.iters + 1)}
+    return out
 
 
 def run_gb300(args):
@@ -346,6 +410,8 @@ def run_gb300(args):
         "phases_ms_per_step": {k: v[0] / args.steps for k, v in phases.items() if v[1]},
         "final_cost": float(cost_acc) / (args.warmup + args.steps),
     }
+    if not args.no_mean:
+        line["mean_cg"] = run_mean_cg(pkg, args, dev)
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args)
     print(json.dumps(line), flush=True)

@@ -221,6 +221,46 @@ int cov3d_wpass(void *stream, int n_images, int P, int r, const void *d_q, int64
                 int64_t chan_stride, const void *d_images, const void *d_C, const void *d_u, void *d_w,
                 int64_t w_img_stride, int64_t w_point_stride, int64_t w_chan_stride);
 
+/* ------------------------------------------------------------------ mean volume and its CG solve */
+
+/* Backproject one batch for the mean (reconstruct_mean's loop body, cov3d/mean.py:196-215):
+ * d_grids (2, n, n, n) centered complex64 receives channel 0 = sum im_backward(y * phase(-offset),
+ * c * ctf) (the rhs) and channel 1 = sum im_backward(c * ctf, c * ctf) / L (the kernel, lhs),
+ * with Nyquist zeroing and the 1/L of im_backward.  d_images (n_images, L^2) complex64 Fourier
+ * images; d_ctf (n_images, L^2), d_offsets (n_images, 2) in pixels and d_contrasts (n_images)
+ * may be NULL.  The plan's points (setpts / setrot with points_L = L) give the poses; the
+ * reference uses the nearest-neighbour plan at upsampling 2 (mean.py:185).  The grids are
+ * zeroed first unless accumulate != 0. */
+int cov3d_mean_accumulate(cov3d_plan *plan, const void *d_images, const float *d_ctf, const float *d_offsets,
+                          const float *d_contrasts, void *d_grids, int accumulate);
+
+/* regularize_lhs (cov3d/mean.py:135-142): d_reg_lhs = max(|lhs|, 1e-3 * Fourier-shell mean of
+ * Re lhs), clamped at 1e-8.  d_lhs (n, n, n) centered complex64, d_reg_lhs (n, n, n) float. */
+int cov3d_regularize_lhs(cov3d_plan *plan, const void *d_lhs, float *d_reg_lhs);
+
+/* Right-hand side and starting point of correct_upsampling_padding (cov3d/mean.py:124-128,
+ * 238-239): d_b = crop_L(centered_ifft3(rhs)) and d_x0 = Re crop_L(centered_ifft3(rhs / reg_lhs))
+ * as complex, both (L, L, L) complex64; either output may be NULL (d_reg_lhs only needed for
+ * d_x0). */
+int cov3d_mean_init(cov3d_plan *plan, const void *d_rhs, const float *d_reg_lhs, void *d_b, void *d_x0);
+
+/* No counterpart in the reference: the optimal circulant approximation (T. Chan) of the CG
+ * operator A(x) = crop(ifft3(reg_lhs * fft3(pad x))) on the L^3 grid, as its Fourier symbol
+ * d_symbol (L, L, L) float, centered order; the preconditioner of cov3d_cg_solve(precond=2). */
+int cov3d_circulant_symbol(cov3d_plan *plan, const float *d_reg_lhs, float *d_symbol);
+
+/* complex_conjugate_gradient on the operator of correct_upsampling_padding (cov3d/mean.py:43-132):
+ * solves A x = b with A(x) = crop_L(centered_ifft3(reg_lhs * centered_fft3(pad_n(x)))), d_x
+ * (L^3 complex64) holding the starting point on entry; stops when ||r|| < rtol ||b|| (FP64
+ * inner products) or after maxiter iterations.  precond: 0 none (the reference), 1 the
+ * Fourier-diagonal 1 / reg_lhs on the fine grid, 2 division by d_symbol (L^3 float, centered)
+ * in the L^3 Fourier domain.  *iters receives the loop index at which it stopped (the
+ * reference's num_iter), *relres ||r|| / ||b||; d_history (maxiter + 1 doubles, may be NULL)
+ * the relative residual before the loop and after each iteration.  Returns COV3D_EMAXITER
+ * (with d_x holding the last iterate) when the tolerance was not reached. */
+int cov3d_cg_solve(cov3d_plan *plan, const float *d_reg_lhs, const void *d_b, void *d_x, double rtol, int maxiter,
+                   int precond, const float *d_symbol, int *iters, double *relres, double *d_history);
+
 /* ------------------------------------------------------------------ allocation-free variant
  * No counterpart in the reference.  Same result as cov3d_gram followed by cov3d_cost_solve
  * (objective 0, no adjoint coefficients, no costs) for callers that cannot let a library

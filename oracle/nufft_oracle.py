@@ -588,3 +588,86 @@ def sphere_mask(L):
     g = grid_1d(L)
     z, y, x = np.meshgrid(g, g, g, indexing="ij")
     return np.sqrt(x * x + y * y + z * z) <= 1
+
+
+def phase_shift_grid(L):
+    """``get_phase_shift_grid`` (``poses.py:70-89``): (gx, gy) with gx[i, j] = g[j], gy[i, j] = g[i],
+    g = ceil(k - L/2) 2 pi / L."""
+    g = np.ceil(np.arange(-L / 2, L / 2)) * 2 * np.pi / L
+    gx, gy = np.meshgrid(g, g, indexing="xy")
+    return gx, gy
+
+
+def mean_backprojection(images, pts, filters, offsets, contrasts, L, upsample=2):
+    """Loop body of ``reconstruct_mean`` (``mean.py:196-215``) over all images at once with the
+    nearest plan: rhs = sum im_backward(y * phase(-offset), c ctf), lhs = sum im_backward(c ctf,
+    c ctf) / L.  Returns (rhs, lhs), centered (n, n, n) complex."""
+    n = L * upsample
+    N = images.shape[0]
+    images = np.asarray(images, np.complex128).reshape(N, L, L)
+    gx, gy = phase_shift_grid(L)
+    off = -np.asarray(offsets, np.float64)
+    ph = np.exp(1j * (gx[None] * off[:, 0, None, None] + gy[None] * off[:, 1, None, None]))
+    f = np.asarray(filters, np.float64).reshape(N, L, L) * np.asarray(contrasts, np.float64)[:, None, None]
+    y = im_backward_fourier_prologue(images * ph, f, L).reshape(N, L * L)
+    k = im_backward_fourier_prologue(f.astype(np.complex128), f, L).reshape(N, L * L)
+    rhs = spread_discretized(y, pts, n, mode="nearest")[0] / L
+    lhs = spread_discretized(k, pts, n, mode="nearest")[0] / L / L
+    return rhs, lhs
+
+
+def reconstruct_mean(images, pts, filters, offsets, contrasts, L, upsample=2, rtol=1e-6, grid_correction=True,
+                     precond=None):
+    """``reconstruct_mean`` (``mean.py:145-259``) without init_vol / mask: backprojection,
+    ``regularize_lhs``, the Fourier-diagonal solve, ``correct_upsampling_padding``, the
+    sphere mask and the nearest grid correction.  Returns (volume, rhs, lhs, iterations)."""
+    rhs, lhs = mean_backprojection(images, pts, filters, offsets, contrasts, L, upsample)
+    reg = regularize_lhs(lhs)
+    vol = np.real(centered_ifft3(rhs / reg, crop_to=L))
+    it = -1
+    if upsample > 1:
+        b = centered_ifft3(rhs, crop_to=L).reshape(-1)
+        x, it, _ = conjugate_gradient(padding_operator(reg, L), b, x0=vol.reshape(-1).astype(np.complex128),
+                                      rtol=rtol, precond=precond)
+        vol = x.reshape((L,) * 3).real
+    vol = np.real(centered_ifft3(centered_fft3(vol) * sphere_mask(L)))
+    if grid_correction:
+        vol = vol / grid_correction_discretized(L, upsample, "nearest")
+    return vol, rhs, lhs, it
+
+
+def circulant_symbol(reg_lhs, L):
+    """Fourier symbol (centered, L^3) of T. Chan's optimal circulant approximation of
+    ``padding_operator(reg_lhs, L)``: its convolution kernel t = ifft_n(reg_lhs) folded per axis
+    as c[tau] = ((L - tau) t[tau] + tau t[tau - L]) / L, then fft_L."""
+    n = reg_lhs.shape[-1]
+    t = np.fft.ifftn(np.fft.ifftshift(reg_lhs))
+    tau = np.arange(L)
+    opts = [(tau, (L - tau) / L), ((tau - L) % n, tau / L)]
+    c = np.zeros((L, L, L), np.complex128)
+    for i0, w0 in opts:
+        for i1, w1 in opts:
+            for i2, w2 in opts:
+                c += t[np.ix_(i0, i1, i2)] * w0[:, None, None] * w1[None, :, None] * w2[None, None, :]
+    return np.fft.fftshift(np.real(np.fft.fftn(c)))
+
+
+def circulant_preconditioner(symbol):
+    """M r = ifft_L(fft_L(r) / symbol) with a centered symbol (L^3)."""
+    L = symbol.shape[-1]
+    native = np.fft.ifftshift(symbol)
+
+    def M(r):
+        return np.fft.ifftn(np.fft.fftn(r.reshape(L, L, L)) / native).reshape(-1)
+
+    return M
+
+
+def fine_diagonal_preconditioner(reg_lhs, L):
+    """M r = crop(ifft3(fft3(pad r) / reg_lhs)): the Fourier-diagonal solve on the fine grid."""
+    n = reg_lhs.shape[-1]
+
+    def M(r):
+        return centered_ifft3(centered_fft3(r.reshape(L, L, L), pad_to=n) / reg_lhs, crop_to=L).reshape(-1)
+
+    return M

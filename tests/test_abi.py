@@ -38,6 +38,14 @@ def test_host_side_validation(pkg):
     assert lib.cov3d_plan_create(16, 1, 1e-6, ctypes.byref(opts), ctypes.byref(h)) == pkg._lib.EINVAL
     assert lib.cov3d_plan_destroy(None) == 0
     assert lib.cov3d_setpts(None, None, 1, 4, 48, 16, 0) == pkg._lib.EINVAL
+    assert lib.cov3d_mean_accumulate(None, None, None, None, None, None, 0) == pkg._lib.EINVAL
+    assert lib.cov3d_regularize_lhs(None, None, None) == pkg._lib.EINVAL
+    assert lib.cov3d_mean_init(None, None, None, None, None) == pkg._lib.EINVAL
+    assert lib.cov3d_circulant_symbol(None, None, None) == pkg._lib.EINVAL
+    it, rr = ctypes.c_int(), ctypes.c_double()
+    assert lib.cov3d_cg_solve(None, None, None, None, 1e-6, 10, 0, None, ctypes.byref(it), ctypes.byref(rr),
+                              None) == pkg._lib.EINVAL
+    assert "cg_solve" in pkg._lib.last_error()
     assert lib.cov3d_status_string(pkg._lib.ENOMEM) == b"out of device memory"
     try:
         pkg._lib.check(pkg._lib.EINVAL)

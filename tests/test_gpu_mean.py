@@ -1,0 +1,147 @@
+"""GPU parity of the mean reconstruction (backprojection, regularize_lhs, the padding CG and its
+preconditioners) through the C ABI, against the reference's float64 outputs (golden fixtures)
+and the float64 oracle."""
+import numpy as np
+import pytest
+import torch
+
+from conftest import load_golden
+from oracle import nufft_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+TOL_FP32 = 1e-5  # float32 kernels against float64 truths, same arithmetic
+# A CG stopped at ||r|| < rtol ||b|| leaves an error up to cond(A) * rtol in x; the float32
+# and float64 runs stop at slightly different iterates.
+TOL_CG = 1e-4
+
+
+def rel(a, b):
+    a = a.detach().cpu().numpy() if torch.is_tensor(a) else np.asarray(a)
+    b = b.detach().cpu().numpy() if torch.is_tensor(b) else np.asarray(b)
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def T(x, dev, dtype=None):
+    t = torch.as_tensor(np.asarray(x))
+    return t.to(device=dev, dtype=dtype) if dtype is not None else t.to(dev)
+
+
+def test_backprojection_matches_reference(pkg, dev):
+    g = load_golden("mean_L10.npz")
+    L, us = int(g["L"]), int(g["us"])
+    acc = pkg.MeanBackprojector(L, us, dev)
+    for lo in range(0, len(g["images"]), 32):  # the reference's batches of 32
+        sl = slice(lo, lo + 32)
+        acc.add(T(g["images"][sl], dev), T(g["filters"][sl], dev), T(g["offsets"][sl], dev),
+                T(g["contrasts"][sl], dev), pts_rot=T(g["pts"][sl], dev, torch.float32))
+    assert rel(acc.rhs, g["rhs"]) < TOL_FP32
+    assert rel(acc.lhs, g["lhs"]) < TOL_FP32
+
+
+def test_regularize_lhs_matches_reference(pkg, dev):
+    g = load_golden("cg_L8.npz")
+    reg = pkg.regularize_lhs(T(g["lhs"], dev).to(torch.complex64))
+    assert rel(reg, g["reg_lhs"]) < 1e-6
+
+
+def test_mean_init_matches_oracle(pkg, dev):
+    g = load_golden("cg_L8.npz")
+    L, us = int(g["L"]), int(g["us"])
+    plan = pkg.mean._MeanSolver.get(L, us, dev)
+    rhs = T(g["rhs"], dev)
+    reg = T(g["reg_lhs"], dev, torch.float32)
+    b = torch.empty((L,) * 3, dtype=torch.complex64, device=dev)
+    x0 = torch.empty_like(b)
+    pkg._lib.call("cov3d_mean_init", plan.bind(), pkg._lib.ptr(rhs), pkg._lib.ptr(reg), pkg._lib.ptr(b),
+                  pkg._lib.ptr(x0))
+    assert rel(b, g["b"]) < TOL_FP32
+    assert rel(x0.real, g["init"]) < TOL_FP32
+    assert x0.imag.abs().max().item() == 0.0
+
+
+def test_cg_matches_reference(pkg, dev):
+    g = load_golden("cg_L8.npz")
+    L = int(g["L"])
+    x, info = pkg.cg_solve(T(g["reg_lhs"], dev), T(g["b"], dev), T(g["init"], dev).to(torch.complex64), L, rtol=1e-6,
+                           history=True)
+    assert info.converged
+    assert rel(x.real.reshape((L,) * 3), g["x"]) < TOL_CG
+    # same iteration as the reference: the count can move by one or two at float32
+    assert abs(info.iters - int(g["iters"][0])) <= 2
+    assert info.history[0] > info.history[-1] and info.history[-1] < 1e-6
+    # the wrapper with the reference signature
+    xr = pkg.correct_upsampling_padding(T(g["reg_lhs"], dev), T(g["rhs"], dev), T(g["init"], dev), L, int(g["us"]))
+    assert rel(xr, g["x"]) < TOL_CG
+
+
+def test_generic_cg_on_a_callable(pkg, dev):
+    g = load_golden("cg_L8.npz")
+    L, n = int(g["L"]), int(g["L"]) * int(g["us"])
+    reg = T(g["reg_lhs"], dev).to(torch.complex128)
+
+    def A(x):
+        X = pkg.centered_fft3(x.reshape((L,) * 3), padding_size=(n,) * 3)
+        return pkg.centered_ifft3(reg * X, cropping_size=(L,) * 3).reshape(-1)
+
+    x = pkg.complex_conjugate_gradient(A, T(g["b"], dev).reshape(-1), x0=T(g["init"], dev).reshape(-1).to(
+        torch.complex128))
+    assert rel(x.real.reshape((L,) * 3), g["x"]) < 1e-10
+
+
+def test_circulant_symbol_matches_oracle(pkg, dev):
+    g = load_golden("cg_L8.npz")
+    L = int(g["L"])
+    sym = pkg.circulant_symbol(T(g["reg_lhs"], dev), L)
+    assert rel(sym, O.circulant_symbol(g["reg_lhs"], L)) < TOL_FP32
+
+
+def _clustered_case(L=12, N=160, seed=5):
+    """Poses in a few tight clusters: an anisotropic kernel whose CG needs many iterations."""
+    rng = np.random.default_rng(seed)
+    centres = O.rotvec_to_rotmat(rng.standard_normal((4, 3)))
+    R = []
+    for i in range(N):
+        jitter = O.rotvec_to_rotmat(0.15 * rng.standard_normal((1, 3)))[0]
+        R.append(jitter @ centres[i % 4])
+    R = np.array(R)
+    pts = O.rotated_points(R, L).astype(np.float32)
+    images = (rng.standard_normal((N, L, L)) + 1j * rng.standard_normal((N, L, L))).astype(np.complex64)
+    filters = rng.uniform(0.3, 1.2, (N, L, L)).astype(np.float32)
+    offsets = rng.uniform(-1.5, 1.5, (N, 2)).astype(np.float32)
+    contrasts = rng.uniform(0.8, 1.2, N).astype(np.float32)
+    return L, pts, images, filters, offsets, contrasts
+
+
+@pytest.mark.parametrize("precond", [None, "diagonal", "circulant"])
+def test_mean_pipeline_matches_oracle(pkg, dev, precond):
+    L, pts, images, filters, offsets, contrasts = _clustered_case()
+    acc = pkg.MeanBackprojector(L, 2, dev)
+    acc.add(T(images, dev), T(filters, dev), T(offsets, dev), T(contrasts, dev), pts_rot=T(pts, dev))
+    vol, info = pkg.solve_mean(acc.rhs, acc.lhs, L, 2, rtol=1e-6, precond=precond, return_info=True)
+    ref, rhs, lhs, it = O.reconstruct_mean(images, pts.astype(np.float64), filters, offsets, contrasts, L, 2,
+                                           rtol=1e-6)
+    assert rel(acc.rhs, rhs) < TOL_FP32 and rel(acc.lhs, lhs) < TOL_FP32
+    assert info.converged
+    assert rel(vol, ref) < TOL_CG
+
+
+def test_preconditioners_cut_iterations(pkg, dev):
+    L, pts, images, filters, offsets, contrasts = _clustered_case()
+    acc = pkg.MeanBackprojector(L, 2, dev)
+    acc.add(T(images, dev), T(filters, dev), T(offsets, dev), T(contrasts, dev), pts_rot=T(pts, dev))
+    its = {}
+    for pc in (None, "diagonal", "circulant"):
+        _, info = pkg.solve_mean(acc.rhs, acc.lhs, L, 2, rtol=1e-5, precond=pc, return_info=True)
+        assert info.converged
+        its[pc] = info.iters
+    assert its["circulant"] < its[None]
+    assert its["diagonal"] < its[None]
+
+
+def test_cg_reports_maxiter(pkg, dev):
+    g = load_golden("cg_L8.npz")
+    L = int(g["L"])
+    x, info = pkg.cg_solve(T(g["reg_lhs"], dev), T(g["b"], dev), T(g["init"], dev), L, rtol=1e-12, maxiter=3)
+    assert not info.converged and info.iters == 2
+    assert np.isfinite(info.relres) and info.relres > 1e-12

@@ -132,3 +132,49 @@ def test_gradient_matches_finite_differences():
         d[1] = eps
         fd = (f(vec, ls + d) - f(vec, ls - d)) / (2 * eps)
         assert abs(fd - gl[1]) <= 1e-6 * max(1.0, abs(fd))
+
+
+def test_reconstruct_mean_pipeline():
+    """Backprojection, regularize_lhs, Fourier-diagonal start, padding CG, sphere mask and
+    grid correction against reconstruct_mean run by the reference in float64.  rhs / lhs are
+    exact; the volume agrees to the accuracy an rtol=1e-6 CG of ~5,500 iterations allows (the
+    two FFT libraries round differently, so the iterates drift apart slowly)."""
+    g = load_golden("mean_L10.npz")
+    L = int(g["L"])
+    vol, rhs, lhs, it = O.reconstruct_mean(g["images"], g["pts"], g["filters"], g["offsets"], g["contrasts"], L,
+                                           int(g["us"]))
+    assert rel(rhs, g["rhs"]) < 1e-12
+    assert rel(lhs, g["lhs"]) < 1e-12
+    assert rel(vol, g["volume"]) < 1e-4
+    assert abs(it - int(g["iters"][0])) < 0.02 * int(g["iters"][0])
+
+
+def test_circulant_symbol_is_the_operator_diagonal_in_fourier():
+    """T. Chan's optimal circulant has eigenvalues diag(F A F^-1): check a few Fourier modes."""
+    g = load_golden("cg_L8.npz")
+    L = int(g["L"])
+    reg = g["reg_lhs"]
+    sym = O.circulant_symbol(reg, L)
+    A = O.padding_operator(reg, L)
+    rng = np.random.default_rng(0)
+    native = np.fft.ifftshift(sym)
+    for _ in range(6):
+        k = tuple(rng.integers(0, L, 3))
+        e = np.zeros((L, L, L), np.complex128)
+        e[k] = 1.0
+        f = np.fft.ifftn(e).reshape(-1) * np.sqrt(L**3)
+        assert abs(np.vdot(f, A(f)) - native[k]) < 1e-12 * np.abs(sym).max()
+
+
+def test_preconditioned_cg_reaches_the_same_solution():
+    g = load_golden("cg_L8.npz")
+    L = int(g["L"])
+    reg = g["reg_lhs"]
+    A = O.padding_operator(reg, L)
+    b = g["b"].reshape(-1)
+    x0 = g["init"].reshape(-1).astype(np.complex128)
+    ref, it0, _ = O.conjugate_gradient(A, b, x0=x0, rtol=1e-10)
+    for M in (O.fine_diagonal_preconditioner(reg, L), O.circulant_preconditioner(O.circulant_symbol(reg, L))):
+        x, it, h = O.conjugate_gradient(A, b, x0=x0, rtol=1e-10, precond=M)
+        assert rel(x, ref) < 1e-8
+        assert h[-1] < 1e-10

@@ -78,6 +78,16 @@ _SIGNATURES = {
     "cov3d_circulant_symbol": (c_int, [c_void_p, c_void_p, c_void_p]),
     "cov3d_cg_solve": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_double, c_int, c_int, c_void_p,
                                ctypes.POINTER(c_int), ctypes.POINTER(c_double), c_void_p]),
+    "cov3d_conv3d_forward": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_int,
+                                     c_int, c_int, c_void_p]),
+    "cov3d_conv3d_backward_data": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_int, c_void_p, c_int,
+                                           c_int, c_void_p, c_void_p]),
+    "cov3d_conv3d_backward_weight": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_int, c_int,
+                                             c_int, c_void_p, c_void_p]),
+    "cov3d_relu_backward": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p]),
+    "cov3d_avgpool2": (c_int, [c_void_p, c_void_p, c_int64, c_int, c_int, c_int, c_int, c_void_p]),
+    "cov3d_upsample2": (c_int, [c_void_p, c_void_p, c_int64, c_int, c_int, c_int, c_int, c_void_p]),
+    "cov3d_resample3d": (c_int, [c_void_p, c_void_p, c_int64, c_int, c_int, c_int, c_void_p]),
 }
 
 _lib = None

@@ -89,3 +89,14 @@ def vmf_cluster_rotations(n, clusters=8, kappa=5.0, generator=None, device="cuda
     e1 = torch.cos(th) * a + torch.sin(th) * b
     e2 = torch.cross(d, e1, dim=1)
     return torch.stack([e1, e2, d], dim=2).to(torch.float32)
+
+
+def orthonormalize(v):
+    """Rows of v (k, m) orthonormalised by modified Gram-Schmidt in float64 (returns float32)."""
+    out = []
+    for i in range(v.shape[0]):
+        w = v[i].to(torch.float64)
+        for u in out:
+            w = w - torch.dot(u, w) * u
+        out.append(w / torch.linalg.vector_norm(w))
+    return torch.stack(out).to(torch.float32)

@@ -50,7 +50,7 @@ def parse():
     ap.add_argument("--mean-images", type=int, default=300000, help="images backprojected for the mean-CG solve")
     ap.add_argument("--mean-L", type=int, default=128)
     ap.add_argument("--mean-rtol", type=float, default=1e-5)
-    ap.add_argument("--mean-maxiter", type=int, default=6000)
+    ap.add_argument("--mean-maxiter", type=int, default=20000)
     ap.add_argument("--no-mean", action="store_true", help="skip the mean-CG measurement")
     return ap.parse_args()
 
@@ -169,7 +169,7 @@ def make_dataset(pkg, args, dev, n_images):
     g = torch.Generator(device=dev).manual_seed(args.seed)
     L, r = args.L, args.rank
     eig = syn.gaussian_blob_volumes(r, L, generator=g, device=dev)
-    eig = torch.linalg.qr(eig.reshape(r, -1).T)[0].T.reshape(r, L, L, L).contiguous()
+    eig = syn.orthonormalize(eig.reshape(r, -1)).reshape(r, L, L, L).contiguous()
     sqrt_lam = torch.linspace(1.0, 0.3, r, device=dev) * L**1.5
     rot = syn.uniform_rotations(n_images, generator=g, device=dev)
     defocus = torch.rand((n_images,), generator=g, device=dev) * 2.0 + 1.0
@@ -244,6 +244,21 @@ def run_mean_cg(pkg, args, dev):
         sec = time.perf_counter() - t0
         out[name] = {"seconds": sec, "iters": info.iters, "relres": info.relres, "converged": info.converged,
                      "ms_per_iter": 1e3 * sec / max(1, info.iters + 1)}
+    lp = import_module("3dcovarestimation_gb300.learned_pc")
+    if os.path.exists(lp.WEIGHTS_PATH):
+        pcn = lp.LearnedPreconditioner(device=dev)
+        pcn.symbol(reg, L)  # warm
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sym = pcn.symbol(reg, L)  # features + network + upsampling, inside the timed solve
+        x, info = mean.cg_solve(reg, b, x0, L, rtol=args.mean_rtol, maxiter=args.mean_maxiter, precond=sym)
+        torch.cuda.synchronize()
+        sec = time.perf_counter() - t0
+        out["learned_pc"] = {"seconds": sec, "iters": info.iters, "relres": info.relres, "converged": info.converged,
+                             "ms_per_iter": 1e3 * sec / max(1, info.iters + 1)}
+        out["learned_vs_diagonal_pc_time"] = sec / out["diagonal_pc"]["seconds"]
+    else:
+        out["learned_pc"] = "no trained weights (3dcovarestimation_gb300/learned_pc_weights.npz)"
     return out
 
 
@@ -282,13 +297,10 @@ def run_gb300(args):
     reg_scale = 1.0 / 100000  # reg / N with N = 100,000 images
     cost_acc = torch.zeros((), dtype=torch.float64, device=dev)
 
-    def grads_allreduce():
-        if world > 1:
-            import torch.distributed as dist
+    dp = import_module("3dcovarestimation_gb300.distributed")
 
-            for t in (covar.vectors.grad, covar.log_sqrt_eigenvals.grad):
-                dist.all_reduce(t)
-                t /= world
+    def grads_allreduce():
+        dp.allreduce_mean_([covar.vectors.grad, covar.log_sqrt_eigenvals.grad])
 
     def step(k, imgs=None, ctfs=None, rots=None):
         b = (k * world + rank) % nb

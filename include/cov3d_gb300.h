@@ -261,6 +261,42 @@ int cov3d_circulant_symbol(cov3d_plan *plan, const float *d_reg_lhs, float *d_sy
 int cov3d_cg_solve(cov3d_plan *plan, const float *d_reg_lhs, const void *d_b, void *d_x, double rtol, int maxiter,
                    int precond, const float *d_symbol, int *iters, double *relres, double *d_history);
 
+/* ------------------------------------------------------------------ learned CG preconditioner
+ * No counterpart in the reference.  Layers of the small 3D U-Net that predicts a correction of
+ * the circulant CG preconditioner from the kernel density, forward and backward, so that the
+ * network is trained and run by this library.  Tensors are (N, C, D, H, W) float32, contiguous;
+ * weights (Cout, Cin, k, k, k) with k = ksize in {1, 3}; stride 1, zero padding k / 2.  All
+ * calls are asynchronous on `stream`. */
+
+/* y = conv(x, w) + bias (bias may be NULL), ReLU applied when relu != 0. */
+int cov3d_conv3d_forward(void *stream, const float *d_x, int N, int Cin, int D, int H, int W, const float *d_w,
+                         const float *d_bias, int Cout, int ksize, int relu, float *d_y);
+
+/* gx = gradient of sum(gy * conv(x, w)) with respect to x; d_wt_scratch holds Cout * Cin * k^3
+ * floats (the flipped, channel-transposed kernel). */
+int cov3d_conv3d_backward_data(void *stream, const float *d_gy, int N, int Cout, int D, int H, int W,
+                               const float *d_w, int Cin, int ksize, float *d_wt_scratch, float *d_gx);
+
+/* gw (Cout, Cin, k^3) and gb (Cout, may be NULL) = gradients of sum(gy * (conv(x, w) + b)),
+ * overwritten. */
+int cov3d_conv3d_backward_weight(void *stream, const float *d_x, const float *d_gy, int N, int Cin, int Cout, int D,
+                                 int H, int W, int ksize, float *d_gw, float *d_gb);
+
+/* gx = gy where y > 0, else 0 (may run in place on gy). */
+int cov3d_relu_backward(void *stream, const float *d_y, const float *d_gy, int64_t count, float *d_gx);
+
+/* 2x average pooling: direction 0 forward (NC, D, H, W) -> (NC, D/2, H/2, W/2), 1 its adjoint
+ * (d_in the gradient of the pooled volume, d_out (NC, D, H, W)). */
+int cov3d_avgpool2(void *stream, const float *d_in, int64_t NC, int D, int H, int W, int direction, float *d_out);
+
+/* 2x nearest upsampling: direction 0 forward (NC, d, h, w) -> (NC, 2d, 2h, 2w), 1 its adjoint
+ * (sum over the 8 children; d_in (NC, 2d, 2h, 2w), d_out (NC, d, h, w)). */
+int cov3d_upsample2(void *stream, const float *d_in, int64_t NC, int d, int h, int w, int direction, float *d_out);
+
+/* Cubic resampling: direction 0 trilinear (align_corners = False) (NC, d^3) -> (NC, D^3);
+ * 1 its adjoint (NC, D^3) -> (NC, d^3); 2 block mean (NC, D^3) -> (NC, d^3), D a multiple of d. */
+int cov3d_resample3d(void *stream, const float *d_in, int64_t NC, int d, int D, int direction, float *d_out);
+
 /* ------------------------------------------------------------------ allocation-free variant
  * No counterpart in the reference.  Same result as cov3d_gram followed by cov3d_cost_solve
  * (objective 0, no adjoint coefficients, no costs) for callers that cannot let a library

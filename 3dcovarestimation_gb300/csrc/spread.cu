@@ -11,7 +11,7 @@ namespace cov3d {
 namespace {
 
 constexpr int kBin = 8;
-constexpr int kSpreadWarps = 8;
+constexpr int kSpreadWarps = 16;
 constexpr int kPlanesPerWarp = 4;
 
 struct SpreadParams {
@@ -34,7 +34,7 @@ struct SpreadParams {
   int64_t cs, chs;
   int shift;
   int max_sub;
-  const int *plane_sched;  // kSpreadWarps x kPlanesPerWarp tile planes per warp (-1 = none)
+  const int *plane_sched;  // kSpreadWarps x kPlanesPerWarp tasks 2 * plane + row parity (-1 = none)
 };
 
 // Prologue factor of im_backward: CTF multiply, Nyquist zeroing, scale (projection_funcs.py:385-399).
@@ -45,14 +45,17 @@ __device__ __forceinline__ float prologue(const PointGeom &g, int64_t id, const 
   return sc;
 }
 
-// Channel pairs per pass (lanes are (window cell, channel pair)); COMP keeps a second
-// (compensation) tile, so it uses half as many pairs.
+// Channel pairs per pass: lanes are (tile column, channel pair), so T * CP <= 32 with
+// T = 8 + W - 1 tile columns; COMP keeps a second (compensation) tile, which leaves room for
+// only one pair at W = 8.
 template <int W, bool COMP>
 struct SpreadCP {
-  // largest W*CP <= 32 whose tile plus staged point values fit in shared memory
-  static constexpr int full = W <= 2 ? 8 : W == 4 ? 7 : W == 8 ? 3 : 32 / W;
-  static constexpr int value = COMP ? (full / 2 > 0 ? full / 2 : 1) : full;
+  static constexpr int T = 8 + W - 1;
+  static constexpr int value = (COMP && W == 8) ? 1 : 32 / T;
 };
+
+constexpr int kLMin = -8;     // window corners relative to the bin lie in [kLMin, kLMin + 16)
+constexpr int kKeys = 256;    // sort key (l1 - kLMin) * 16 + (l0 - kLMin)
 
 // Per-point record staged once per block: packed window corner (tile-local, biased by 32 so
 // zero-padding corners below the tile stay non-negative) and the 3W kernel weights.
@@ -62,29 +65,33 @@ struct PointRec {
 };
 
 // One block per subproblem, tile = bin + (W-1)-cell halo of 2*CP channels in shared memory.
-//  1. the block buckets its points by the axis-0 corner of their window (8 buckets);
-//  2. warp w owns whole axis-0 planes of the tile (plane_sched balances the work: plane a is
-//     reached by the points of min(W, ...) buckets); for every point reaching one of its planes
-//     the warp's lanes (j, q) add weight * value to channels 2q, 2q+1 of tile[a][b][corner2 + j]
-//     for the W rows b of the window -- contiguous 16-byte read-modify-writes, no bank
-//     conflicts, and no two warps ever touch the same cell, so no atomics;
-//     with COMP every addition is a TwoSum whose rounding error goes to the second tile;
+//  1. the block counting-sorts its points by the (axis-1, axis-0) corner (l1, l0) of their
+//     window and stages, in that order, each point's record (packed corner, 3W weights) and
+//     CTF-scaled values;
+//  2. each warp owns (plane, row parity) tasks: a whole axis-0 plane of the tile, and within it
+//     the tile rows of one parity (plane_sched balances the work over the 16 warps).  Lane
+//     (q, c) owns tile column c and channel pair q.  For a plane the points with a given l1 and
+//     an l0 that reaches the plane are one contiguous range; all of them hit rows l1 .. l1+W-1,
+//     so the lane accumulates weight * value for its column and its rows in registers and adds
+//     the sums to the tile once per range -- conflict-free 16-byte read-modify-writes, and no
+//     two warps ever touch the same cell, so there are no atomics.  With COMP that addition is
+//     a TwoSum whose rounding error goes to the second tile (the register sums of a range carry
+//     only the rounding of their own terms);
 //  3. the tile is added to the global grid, one complex atomic per cell and channel.
 template <int KT, int W, int CP, bool COMP>
 __global__ void __launch_bounds__(kSpreadWarps * 32) spread_kernel(const SpreadParams a) {
   constexpr int T = kBin + W - 1;
-  constexpr int RG = 32 / (W * CP);  // window rows handled side by side by spare lanes
-  constexpr int LANES = W * CP * RG;
+  static_assert(T * CP <= 32, "one lane per tile column and channel pair");
   constexpr int TILE4 = T * T * T * CP;
+  constexpr int NR = (W + 1) / 2;  // window rows of one parity, at most
   extern __shared__ float4 smem4[];
   float4 *hi = smem4;
   float4 *lo = smem4 + (COMP ? TILE4 : 0);
-  float4 *s_val = smem4 + (COMP ? 2 : 1) * TILE4;  // max_sub * CP: scaled channel pairs per point
+  float4 *s_val = smem4 + (COMP ? 2 : 1) * TILE4;  // max_sub * CP, sorted order
   float *s_rec = reinterpret_cast<float *>(s_val + a.max_sub * CP);  // max_sub * PointRec<W>::FLOATS
-  int *s_idx = reinterpret_cast<int *>(s_rec + a.max_sub * PointRec<W>::FLOATS);
-  int *s_bucket = s_idx + a.max_sub;
-  int *s_cnt = s_bucket + a.max_sub;  // kBin
-  int *s_off = s_cnt + kBin;          // kBin + 1
+  int *s_key = reinterpret_cast<int *>(s_rec + a.max_sub * PointRec<W>::FLOATS);  // max_sub
+  int *s_cnt = s_key + a.max_sub;  // kKeys
+  int *s_off = s_cnt + kKeys;      // kKeys + 1
 
   const int sub = blockIdx.x;
   if (sub >= *a.nsub) return;
@@ -99,23 +106,47 @@ __global__ void __launch_bounds__(kSpreadWarps * 32) spread_kernel(const SpreadP
   const int tid = threadIdx.x;
 
   for (int e = tid; e < (COMP ? 2 : 1) * TILE4; e += blockDim.x) smem4[e] = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (tid < kBin) s_cnt[tid] = 0;
+  for (int e = tid; e < kKeys; e += blockDim.x) s_cnt[e] = 0;
   __syncthreads();
-  // 1. stage the points' scaled values (im_backward prologue folded in) and bucket the points
-  //    by axis-0 window corner
-  for (int e = tid; e < cnt * CP; e += blockDim.x) {
-    const int k = e / CP, qq = e - (e / CP) * CP;
-    const SortedPoint sp = a.pts[first + k];
-    const int64_t id = sp_id(sp.idf);
-    float sc = (a.nyquist && sp_nyquist(sp.idf)) ? 0.0f : a.scale;
-    if (a.ctf) sc *= __ldg(a.ctf + id);
-    const float2 *src = a.vals + id * a.ips + (int64_t)(a.ch0 + 2 * qq) * a.ics;
-    const float2 v0 = 2 * qq < a.nch ? __ldg(src) : make_float2(0.f, 0.f);
-    const float2 v1 = 2 * qq + 1 < a.nch ? __ldg(src + a.ics) : make_float2(0.f, 0.f);
-    s_val[e] = make_float4(v0.x * sc, v0.y * sc, v1.x * sc, v1.y * sc);
-  }
+  // 1a. sort keys and ranks
   for (int k = tid; k < cnt; k += blockDim.x) {
     const SortedPoint sp = a.pts[first + k];
+    int c0 = first_cell<KT, W>(sp.t0), c1 = first_cell<KT, W>(sp.t1);
+    if (KT == COV3D_KERNEL_ES) {
+      c0 = wrap1(c0, n);
+      c1 = wrap1(c1, n);
+    }
+    const int key = (min(max(c1 - ts1 - kLMin, 0), 15) << 4) | min(max(c0 - ts0 - kLMin, 0), 15);
+    s_key[k] = key | (atomicAdd(s_cnt + key, 1) << 8);
+  }
+  __syncthreads();
+  if (tid < 32) {  // exclusive scan of the 256 counters by one warp, 8 per lane
+    int v[kKeys / 32], sum = 0;
+#pragma unroll
+    for (int u = 0; u < kKeys / 32; ++u) {
+      v[u] = s_cnt[tid * (kKeys / 32) + u];
+      sum += v[u];
+    }
+    int incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, incl, o);
+      if (tid >= o) incl += t;
+    }
+    int base = incl - sum;
+#pragma unroll
+    for (int u = 0; u < kKeys / 32; ++u) {
+      s_off[tid * (kKeys / 32) + u] = base;
+      base += v[u];
+    }
+    if (tid == 31) s_off[kKeys] = incl;
+  }
+  __syncthreads();
+  // 1b. records and scaled values (im_backward prologue folded in) in sorted order
+  for (int k = tid; k < cnt; k += blockDim.x) {
+    const SortedPoint sp = a.pts[first + k];
+    const int kr = s_key[k];
+    const int slot = s_off[kr & 255] + (kr >> 8);
     float w0[W], w1[W], w2[W];
     int c0 = taps<KT, W>(sp.t0, a.k.beta, w0);
     int c1 = taps<KT, W>(sp.t1, a.k.beta, w1);
@@ -125,7 +156,7 @@ __global__ void __launch_bounds__(kSpreadWarps * 32) spread_kernel(const SpreadP
       c1 = wrap1(c1, n);
       c2 = wrap1(c2, n);
     }
-    float *rec = s_rec + k * PointRec<W>::FLOATS;
+    float *rec = s_rec + slot * PointRec<W>::FLOATS;
     rec[0] = __int_as_float((c0 - ts0 + 32) | ((c1 - ts1 + 32) << 8) | ((c2 - ts2 + 32) << 16));
 #pragma unroll
     for (int r = 0; r < W; ++r) {
@@ -133,76 +164,88 @@ __global__ void __launch_bounds__(kSpreadWarps * 32) spread_kernel(const SpreadP
       rec[1 + W + r] = w1[r];
       rec[1 + 2 * W + r] = w2[r];
     }
-    const int b0 = max(c0 - ts0, 0);
-    s_bucket[k] = b0 | (atomicAdd(s_cnt + b0, 1) << 4);
-  }
-  __syncthreads();
-  if (tid == 0) {
-    int acc = 0;
-    for (int i = 0; i < kBin; ++i) {
-      s_off[i] = acc;
-      acc += s_cnt[i];
+    const int64_t id = sp_id(sp.idf);
+    float sc = (a.nyquist && sp_nyquist(sp.idf)) ? 0.0f : a.scale;
+    if (a.ctf) sc *= __ldg(a.ctf + id);
+#pragma unroll
+    for (int qq = 0; qq < CP; ++qq) {
+      const float2 *src = a.vals + id * a.ips + (int64_t)(a.ch0 + 2 * qq) * a.ics;
+      const float2 v0 = 2 * qq < a.nch ? __ldg(src) : make_float2(0.f, 0.f);
+      const float2 v1 = 2 * qq + 1 < a.nch ? __ldg(src + a.ics) : make_float2(0.f, 0.f);
+      s_val[slot * CP + qq] = make_float4(v0.x * sc, v0.y * sc, v1.x * sc, v1.y * sc);
     }
-    s_off[kBin] = acc;
-  }
-  __syncthreads();
-  for (int k = tid; k < cnt; k += blockDim.x) {
-    const int bk = s_bucket[k];
-    s_idx[s_off[bk & 15] + (bk >> 4)] = k;
   }
   __syncthreads();
 
-  // 2. planes of this warp
+  // 2. tasks of this warp; lane (q, c): channel pair q, tile column c
   const int warp = tid >> 5, lane = tid & 31;
-  const int g = lane / (W * CP), lr = lane - g * (W * CP);
-  const int j = lr / CP, q = lr - (lr / CP) * CP;
-  const bool lane_live = lane < LANES;
+  const int q = lane / T, c = lane - (lane / T) * T;
+  const bool lane_live = q < CP;
+  const int qv = lane_live ? q : 0;
   for (int s = 0; s < kPlanesPerWarp; ++s) {
-    const int pa = __ldg(a.plane_sched + warp * kPlanesPerWarp + s);
-    if (pa < 0) break;
-    const int blo = max(0, pa - W + 1), bhi = min(kBin - 1, pa);
-    const int i1end = s_off[bhi + 1];
-    for (int i = s_off[blo]; i < i1end; ++i) {
-      const int kp = s_idx[i];
-      const float *rec = s_rec + kp * PointRec<W>::FLOATS;
-      const int packed = __float_as_int(rec[0]);
-      const int l0 = (packed & 255) - 32, l1 = ((packed >> 8) & 255) - 32, l2 = ((packed >> 16) & 255) - 32;
-      const int o0 = pa - l0;  // tap along axis 0 that lands on this plane
-      if (o0 >= W) continue;   // zero padding: window clamped into bucket 0 but below this plane
-      const int cell2 = l2 + j;
-      if (!lane_live || cell2 < 0) continue;
-      const float4 vv = s_val[kp * CP + q];
-      const float waj = rec[1 + o0] * rec[1 + 2 * W + j];
-      float4 *rowp = hi + ((pa * T) * T + cell2) * CP + q;
-      float4 *rowl = lo + ((pa * T) * T + cell2) * CP + q;
+    const int task = __ldg(a.plane_sched + warp * kPlanesPerWarp + s);
+    if (task < 0) break;
+    const int pa = task >> 1, par = task & 1;
+    // corners l0 reaching plane pa: [pa - W + 1, pa]
+    const int b0lo = max(pa - W + 1 - kLMin, 0), b0hi = min(pa - kLMin, 15);
+    if (b0lo > b0hi) continue;
+    for (int b1 = 0; b1 < 16; ++b1) {
+      const int ibeg = s_off[(b1 << 4) | b0lo], iend = s_off[((b1 << 4) | b0hi) + 1];
+      if (ibeg >= iend) continue;
+      const int l1 = b1 + kLMin;
+      const int r0 = (par - l1) & 1;  // first window row whose tile row has parity par
+      float4 acc[NR];
 #pragma unroll
-      for (int ii = 0; ii < (W + RG - 1) / RG; ++ii) {
-        const int i1 = ii * RG + g;
-        if (i1 >= W) break;
-        const int r1 = l1 + i1;
-        if (KT != COV3D_KERNEL_ES && r1 < 0) continue;
-        const float w = waj * rec[1 + W + i1];
-        float4 &h = rowp[r1 * T * CP];
-        if (!COMP) {
-          float4 x = h;
-          x.x = fmaf(w, vv.x, x.x);
-          x.y = fmaf(w, vv.y, x.y);
-          x.z = fmaf(w, vv.z, x.z);
-          x.w = fmaf(w, vv.w, x.w);
-          h = x;
-        } else {
-          float4 x = h, e = rowl[r1 * T * CP];
-          const float d[4] = {w * vv.x, w * vv.y, w * vv.z, w * vv.w};
-          float *xs = &x.x, *es = &e.x;
+      for (int u = 0; u < NR; ++u) acc[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+      bool touched = false;
+      for (int i = ibeg; i < iend; ++i) {
+        const float *rec = s_rec + i * PointRec<W>::FLOATS;
+        const int packed = __float_as_int(rec[0]);
+        const int o0 = pa - ((packed & 255) - 32);  // in [0, W) by the range above
+        const int jj = c - (((packed >> 16) & 255) - 32);
+        if (!lane_live || jj < 0 || jj >= W) continue;
+        touched = true;
+        const float w02 = rec[1 + o0] * rec[1 + 2 * W + jj];
+        const float4 vv = s_val[i * CP + qv];
 #pragma unroll
-          for (int u = 0; u < 4; ++u) {
-            const float s2 = xs[u] + d[u];
-            const float bb = s2 - xs[u];
-            es[u] += (xs[u] - (s2 - bb)) + (d[u] - bb);
-            xs[u] = s2;
+        for (int u = 0; u < NR; ++u) {
+          const int r = r0 + 2 * u;
+          if (r < W) {
+            const float w = w02 * rec[1 + W + r];
+            acc[u].x = fmaf(w, vv.x, acc[u].x);
+            acc[u].y = fmaf(w, vv.y, acc[u].y);
+            acc[u].z = fmaf(w, vv.z, acc[u].z);
+            acc[u].w = fmaf(w, vv.w, acc[u].w);
           }
-          h = x;
-          rowl[r1 * T * CP] = e;
+        }
+      }
+      if (!touched) continue;
+#pragma unroll
+      for (int u = 0; u < NR; ++u) {
+        const int r = r0 + 2 * u;
+        const int r1 = l1 + r;
+        if (r >= W || (KT != COV3D_KERNEL_ES && r1 < 0)) continue;
+        const int e = ((pa * T + r1) * T + c) * CP + q;
+        if (!COMP) {
+          float4 x = hi[e];
+          x.x += acc[u].x;
+          x.y += acc[u].y;
+          x.z += acc[u].z;
+          x.w += acc[u].w;
+          hi[e] = x;
+        } else {
+          float4 x = hi[e], err = lo[e];
+          const float d[4] = {acc[u].x, acc[u].y, acc[u].z, acc[u].w};
+          float *xs = &x.x, *es = &err.x;
+#pragma unroll
+          for (int v = 0; v < 4; ++v) {  // TwoSum (Knuth): xs + d = s2 + rounding error, exactly
+            const float s2 = xs[v] + d[v];
+            const float bb = s2 - xs[v];
+            es[v] += (xs[v] - (s2 - bb)) + (d[v] - bb);
+            xs[v] = s2;
+          }
+          hi[e] = x;
+          lo[e] = err;
         }
       }
     }
@@ -266,8 +309,8 @@ template <int KT, int W, int CP, bool COMP>
 int launch_one(const SpreadParams &a, int64_t max_blocks, cudaStream_t st) {
   constexpr int T = kBin + W - 1;
   const size_t smem = (size_t)(COMP ? 2 : 1) * T * T * T * CP * sizeof(float4) +
-                      (size_t)a.max_sub * (CP * sizeof(float4) + PointRec<W>::FLOATS * 4 + 2 * sizeof(int)) +
-                      (2 * kBin + 1) * sizeof(int);
+                      (size_t)a.max_sub * (CP * sizeof(float4) + PointRec<W>::FLOATS * 4 + sizeof(int)) +
+                      (2 * kKeys + 1) * sizeof(int);
   if (smem > 227 * 1024) {
     set_error("spreading tile of %zu bytes exceeds shared memory", smem);
     return COV3D_EINVAL;
@@ -355,22 +398,25 @@ __global__ void spread_unagg_kernel(PointGeom g, KernelSpec k, int64_t M, const 
 
 }  // namespace
 
-// Tile planes (axis-0 index a of the bin + halo tile) per warp.  Plane a is reached by the
-// points whose axis-0 window corner lies in [a - W + 1, a] (clipped to the bin): planes are
-// assigned greedily, heaviest first, to the least loaded warp, so all warps get equal work.
+// Warp tasks: (tile plane a, row parity) pairs, encoded 2 * a + parity.  Plane a is reached by
+// the points whose axis-0 window corner lies in [a - W + 1, a] (clipped to the bin), and a
+// parity holds about half of each window's rows: tasks are assigned greedily, heaviest first,
+// to the least loaded warp, so all warps get equal work.
 int build_plane_schedule(cov3d_plan *p) {
   const int W = p->kernel == COV3D_KERNEL_NEAREST ? 1 : p->kernel == COV3D_KERNEL_LINEAR ? 2 : p->width;
   const int T = kBin + W - 1;
-  std::vector<int> order(T), load(kSpreadWarps, 0), count(kSpreadWarps, 0);
+  std::vector<int> order(2 * T), load(kSpreadWarps, 0), count(kSpreadWarps, 0);
   std::vector<int> sched(kSpreadWarps * kPlanesPerWarp, -1);
-  auto reach = [&](int x) {
+  auto work = [&](int task) {
+    const int x = task >> 1;
     const int lo = x - W + 1 > 0 ? x - W + 1 : 0;
     const int hi = x < kBin - 1 ? x : kBin - 1;
-    return hi >= lo ? hi - lo + 1 : 0;
+    const int rows = (task & 1) ? W / 2 : (W + 1) / 2;
+    return hi >= lo ? (hi - lo + 1) * rows : 0;
   };
-  for (int i = 0; i < T; ++i) order[i] = i;
-  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return reach(x) > reach(y); });
-  for (int pa : order) {
+  for (int i = 0; i < 2 * T; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return work(x) > work(y); });
+  for (int task : order) {
     int best = -1;
     for (int w = 0; w < kSpreadWarps; ++w)
       if (count[w] < kPlanesPerWarp && (best < 0 || load[w] < load[best])) best = w;
@@ -378,8 +424,8 @@ int build_plane_schedule(cov3d_plan *p) {
       set_error("cannot schedule %d tile planes", T);
       return COV3D_EINVAL;
     }
-    sched[best * kPlanesPerWarp + count[best]++] = pa;
-    load[best] += reach(pa);
+    sched[best * kPlanesPerWarp + count[best]++] = task;
+    load[best] += work(task);
   }
   COV3D_TRY(grow(p->row_order, (int64_t)sched.size() * 4));
   return check_cuda(cudaMemcpy(p->row_order.ptr, sched.data(), sched.size() * 4, cudaMemcpyHostToDevice),

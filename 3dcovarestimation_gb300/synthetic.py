@@ -21,6 +21,7 @@ def gaussian_blob_volumes(count, L, blobs=50, radius=0.35, width=(1.0, 3.0), amp
     ax = torch.arange(L, device=dev, dtype=torch.float32) - L // 2
     z, y, x = torch.meshgrid(ax, ax, ax, indexing="ij")
     out = torch.zeros((count, L, L, L), device=dev)
+    grid = torch.stack([z, y, x]).reshape(3, -1)
     for c in range(count):
         d = torch.randn((blobs, 3), generator=g, device=dev)
         d = d / d.norm(dim=1, keepdim=True)
@@ -28,9 +29,11 @@ def gaussian_blob_volumes(count, L, blobs=50, radius=0.35, width=(1.0, 3.0), amp
         centres = d * rr
         sig = torch.rand((blobs,), generator=g, device=dev) * (width[1] - width[0]) + width[0]
         a = torch.rand((blobs,), generator=g, device=dev) * (amp[1] - amp[0]) + amp[0]
-        for i in range(blobs):
-            r2 = (z - centres[i, 0]) ** 2 + (y - centres[i, 1]) ** 2 + (x - centres[i, 2]) ** 2
-            out[c] += a[i] * torch.exp(-r2 / (2 * sig[i] ** 2))
+        # all blobs at once, in slabs of voxels to bound the (blobs, voxels) temporary
+        for lo in range(0, grid.shape[1], 1 << 20):
+            pts = grid[:, lo:lo + (1 << 20)]
+            r2 = ((pts[None] - centres[:, :, None]) ** 2).sum(1)
+            out[c].view(-1)[lo:lo + pts.shape[1]] = (a[:, None] * torch.exp(-r2 / (2 * sig[:, None] ** 2))).sum(0)
     return out
 
 

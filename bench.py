@@ -238,10 +238,12 @@ def run_mean_cg(pkg, args, dev):
     mean.cg_solve(reg, b, x0, L, rtol=1e-1, maxiter=2, precond="diagonal")
     for name, pc in (("plain", None), ("diagonal_pc", "diagonal"), ("circulant_pc", "circulant")):
         torch.cuda.synchronize()
+        torch.cuda.nvtx.range_push("mean_cg_" + name)
         t0 = time.perf_counter()
         x, info = mean.cg_solve(reg, b, x0, L, rtol=args.mean_rtol, maxiter=args.mean_maxiter, precond=pc)
         torch.cuda.synchronize()
         sec = time.perf_counter() - t0
+        torch.cuda.nvtx.range_pop()
         out[name] = {"seconds": sec, "iters": info.iters, "relres": info.relres, "converged": info.converged,
                      "ms_per_iter": 1e3 * sec / max(1, info.iters + 1)}
     lp = import_module("3dcovarestimation_gb300.learned_pc")
@@ -330,11 +332,13 @@ def run_gb300(args):
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(torch.cuda.current_device()) as clk:
         barrier()
+        torch.cuda.nvtx.range_push("cov_sgd_steps")
         e0.record(stream)
         for k in range(args.steps):
             cost_acc += step(args.warmup + k)
         e1.record(stream)
         barrier()
+        torch.cuda.nvtx.range_pop()
     ms_total = e0.elapsed_time(e1)
     launches = lib.launch_count() - launches0
     phases = step_fn.plan.timing_read()

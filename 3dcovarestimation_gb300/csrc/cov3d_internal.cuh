@@ -116,7 +116,6 @@ struct cov3d_plan {
   cov3d::DevBuf sub_off;       // int (nbins + 1)
   cov3d::DevBuf pt_bin, pt_rank, perm;        // int (M)
   cov3d::DevBuf sorted;        // SortedPoint (M), bin-sorted order
-  cov3d::DevBuf row_order;     // spreading plane schedule per warp
   cov3d::DevBuf sub_bin, sub_first, sub_count;  // int (max subproblems)
   cov3d::DevBuf nsub;          // int scalar
 
@@ -180,7 +179,6 @@ int launch_interp(cov3d_plan *p, const GridArgs &g, int nchan, void *out, int64_
 // spread.cu
 int launch_spread(cov3d_plan *p, const void *values, int64_t in_ps, int64_t in_cs, int nchan, const EpilogueArgs &e,
                   void *grid, int64_t cell_stride, int64_t chan_stride, int shift);
-int build_plane_schedule(cov3d_plan *p);
 int launch_spread_unaggregated(cov3d_plan *p, const void *values, int64_t in_ps, const EpilogueArgs &e,
                                void *grids);
 

@@ -305,7 +305,6 @@ int cov3d_plan_create(int L, int n_trans, double eps, const cov3d_opts *opts, co
   if (st == COV3D_OK) st = grow(p->gc1d, L * 4);
   if (st == COV3D_OK) st = check_cuda(cudaMemcpy(p->gc1d.ptr, gf.data(), L * 4, cudaMemcpyHostToDevice), "cudaMemcpy");
   if (st == COV3D_OK) st = grow(p->acc, 64 * sizeof(double));
-  if (st == COV3D_OK) st = build_plane_schedule(p);
   if (st == COV3D_OK) st = check_cuda(cudaMallocHost(&p->h_acc, 64 * sizeof(double)), "cudaMallocHost");
   if (st != COV3D_OK || !p->ffts || !p->ev_pool || !p->ev_phase) {
     cov3d_plan_destroy(p);
@@ -324,7 +323,7 @@ int cov3d_plan_destroy(cov3d_plan *p) {
     delete p->ffts;
   }
   DevBuf *bufs[] = {&p->gc1d, &p->pts, &p->rot, &p->bin_count, &p->bin_off, &p->sub_off, &p->pt_bin, &p->pt_rank,
-                    &p->perm, &p->sorted, &p->row_order, &p->sub_bin, &p->sub_first, &p->sub_count, &p->nsub, &p->fine, &p->fine2, &p->q,
+                    &p->perm, &p->sorted, &p->sub_bin, &p->sub_first, &p->sub_count, &p->nsub, &p->fine, &p->fine2, &p->q,
                     &p->small, &p->acc, &p->cgw};
   for (DevBuf *b : bufs) release(*b);
   if (p->h_acc) cudaFreeHost(p->h_acc);

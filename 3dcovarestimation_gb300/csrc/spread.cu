@@ -1,8 +1,6 @@
 // Spreading ("type-1" half of the NUFFT; exact adjoint of interp.cu, replacing the
 // reference's grid_sample backward with FP32 global atomics, nufft_plan.py:171-242), over the
 // bin-sorted point records of points_sort.cu.  See spread_kernel for the decomposition.
-#include <algorithm>
-#include <vector>
 
 #include "cov3d_device.cuh"
 
@@ -12,7 +10,6 @@ namespace {
 
 constexpr int kBin = 8;
 constexpr int kSpreadWarps = 16;
-constexpr int kPlanesPerWarp = 4;
 
 struct SpreadParams {
   PointGeom g;
@@ -26,7 +23,7 @@ struct SpreadParams {
   const float2 *vals;
   int64_t ips, ics;
   int ch0;
-  int nch;  // channels in this pass (<= 2 * CP)
+  int nch;  // channels of this launch
   const float *ctf;
   int nyquist;
   float scale;
@@ -34,7 +31,6 @@ struct SpreadParams {
   int64_t cs, chs;
   int shift;
   int max_sub;
-  const int *plane_sched;  // kSpreadWarps x kPlanesPerWarp tasks 2 * plane + row parity (-1 = none)
 };
 
 // Prologue factor of im_backward: CTF multiply, Nyquist zeroing, scale (projection_funcs.py:385-399).
@@ -45,53 +41,59 @@ __device__ __forceinline__ float prologue(const PointGeom &g, int64_t id, const 
   return sc;
 }
 
-// Channel pairs per pass: lanes are (tile column, channel pair), so T * CP <= 32 with
-// T = 8 + W - 1 tile columns; COMP keeps a second (compensation) tile, which leaves room for
-// only one pair at W = 8.
-template <int W, bool COMP>
-struct SpreadCP {
-  static constexpr int T = 8 + W - 1;
-  static constexpr int value = (COMP && W == 8) ? 1 : 32 / T;
-};
+constexpr int kLMin = -8;   // window corners relative to the bin lie in [kLMin, kLMin + 16)
+constexpr int kKeys = 256;  // sort key (l1 - kLMin) * 16 + (l0 - kLMin)
+constexpr int kMaxCPL = 3;  // channel pairs per lane per group
 
-constexpr int kLMin = -8;     // window corners relative to the bin lie in [kLMin, kLMin + 16)
-constexpr int kKeys = 256;    // sort key (l1 - kLMin) * 16 + (l0 - kLMin)
-
-// Per-point record staged once per block: packed window corner (tile-local, biased by 32 so
-// zero-padding corners below the tile stay non-negative) and the 3W kernel weights.
+// Per-point record staged once per block: packed window corner (bin-local, biased by 32 so
+// zero-padding corners below the bin stay non-negative) and the 3W kernel weights.
 template <int W>
 struct PointRec {
   static constexpr int FLOATS = (1 + 3 * W + 3) / 4 * 4;
 };
 
-// One block per subproblem, tile = bin + (W-1)-cell halo of 2*CP channels in shared memory.
+// Lane layout of the row tasks: lane = g * T + c owns tile column c (T = 8 + W - 1 columns)
+// and the channel pairs g, g + G, ..., G = 32 / T lane groups.
+template <int W>
+struct SpreadLanes {
+  static constexpr int T = kBin + W - 1;
+  static constexpr int G = 32 / T;
+};
+
+template <int W>
+__host__ __device__ constexpr int spread_pairs(int cpl) { return SpreadLanes<W>::G * cpl; }
+
+// One block per subproblem (a bin of 8^3 cells and at most max_sub of its points); the cells
+// it can reach form a tile of the bin and a (W-1)-cell halo, T^3 cells.
 //  1. the block counting-sorts its points by the (axis-1, axis-0) corner (l1, l0) of their
 //     window and stages, in that order, each point's record (packed corner, 3W weights) and
-//     CTF-scaled values;
-//  2. each warp owns (plane, row parity) tasks: a whole axis-0 plane of the tile, and within it
-//     the tile rows of one parity (plane_sched balances the work over the 16 warps).  Lane
-//     (q, c) owns tile column c and channel pair q.  For a plane the points with a given l1 and
-//     an l0 that reaches the plane are one contiguous range; all of them hit rows l1 .. l1+W-1,
-//     so the lane accumulates weight * value for its column and its rows in registers and adds
-//     the sums to the tile once per range -- conflict-free 16-byte read-modify-writes, and no
-//     two warps ever touch the same cell, so there are no atomics.  With COMP that addition is
-//     a TwoSum whose rounding error goes to the second tile (the register sums of a range carry
-//     only the rounding of their own terms);
-//  3. the tile is added to the global grid, one complex atomic per cell and channel.
-template <int KT, int W, int CP, bool COMP>
+//     its CTF-scaled channel pairs (im_backward's prologue folded in);
+//  2. a task is one tile row: plane a, row b.  The points whose window covers it are the W
+//     contiguous ranges {l1 = b - o1, l0 in [a - W + 1, a]}, o1 = 0 .. W-1, of the sorted
+//     order.  Lane (g, c) keeps the sums of cell (a, b, c) for its channel pairs in registers:
+//     each range is summed in FP32 and, with COMP, added to the cell's (hi, lo) pair by a
+//     TwoSum, so the error of the cell's accumulation is that of one short FP32 sum per range.
+//     The finished row goes to the global grid with one complex atomic per cell and channel.
+//     Warps take tasks from a shared counter, so the heavy middle rows spread over all warps.
+//  The block needs no shared-memory tile: its shared memory is the staged points only, and
+//  several blocks share an SM.
+template <int KT, int W, int CPL, bool COMP>
 __global__ void __launch_bounds__(kSpreadWarps * 32) spread_kernel(const SpreadParams a) {
-  constexpr int T = kBin + W - 1;
-  static_assert(T * CP <= 32, "one lane per tile column and channel pair");
-  constexpr int TILE4 = T * T * T * CP;
-  constexpr int NR = (W + 1) / 2;  // window rows of one parity, at most
+  constexpr int T = SpreadLanes<W>::T;
+  constexpr int G = SpreadLanes<W>::G;
+  constexpr int NP = G * CPL;  // channel pairs staged per group
+  constexpr int FL = PointRec<W>::FLOATS;
   extern __shared__ float4 smem4[];
-  float4 *hi = smem4;
-  float4 *lo = smem4 + (COMP ? TILE4 : 0);
-  float4 *s_val = smem4 + (COMP ? 2 : 1) * TILE4;  // max_sub * CP, sorted order
-  float *s_rec = reinterpret_cast<float *>(s_val + a.max_sub * CP);  // max_sub * PointRec<W>::FLOATS
-  int *s_key = reinterpret_cast<int *>(s_rec + a.max_sub * PointRec<W>::FLOATS);  // max_sub
-  int *s_cnt = s_key + a.max_sub;  // kKeys
-  int *s_off = s_cnt + kKeys;      // kKeys + 1
+  float4 *s_val = smem4;                                                         // max_sub * NP
+  long long *s_rowoff = reinterpret_cast<long long *>(s_val + a.max_sub * NP);  // T * T
+  float *s_rec = reinterpret_cast<float *>(s_rowoff + T * T);                  // max_sub * FL
+  int *s_key = reinterpret_cast<int *>(s_rec + a.max_sub * FL);                // max_sub
+  int *s_pid = s_key + a.max_sub;                                              // max_sub
+  float *s_sc = reinterpret_cast<float *>(s_pid + a.max_sub);                  // max_sub
+  int *s_cnt = reinterpret_cast<int *>(s_sc + a.max_sub);                      // kKeys
+  int *s_off = s_cnt + kKeys;                                                  // kKeys + 1
+  int *s_coloff = s_off + kKeys + 1;                                           // T
+  int *s_task = s_coloff + T;                                                  // 1
 
   const int sub = blockIdx.x;
   if (sub >= *a.nsub) return;
@@ -105,7 +107,6 @@ __global__ void __launch_bounds__(kSpreadWarps * 32) spread_kernel(const SpreadP
   const int n = a.g.n;
   const int tid = threadIdx.x;
 
-  for (int e = tid; e < (COMP ? 2 : 1) * TILE4; e += blockDim.x) smem4[e] = make_float4(0.f, 0.f, 0.f, 0.f);
   for (int e = tid; e < kKeys; e += blockDim.x) s_cnt[e] = 0;
   __syncthreads();
   // 1a. sort keys and ranks
@@ -142,7 +143,7 @@ __global__ void __launch_bounds__(kSpreadWarps * 32) spread_kernel(const SpreadP
     if (tid == 31) s_off[kKeys] = incl;
   }
   __syncthreads();
-  // 1b. records and scaled values (im_backward prologue folded in) in sorted order
+  // 1b. records, point ids and prologue factors in sorted order
   for (int k = tid; k < cnt; k += blockDim.x) {
     const SortedPoint sp = a.pts[first + k];
     const int kr = s_key[k];
@@ -156,7 +157,7 @@ __global__ void __launch_bounds__(kSpreadWarps * 32) spread_kernel(const SpreadP
       c1 = wrap1(c1, n);
       c2 = wrap1(c2, n);
     }
-    float *rec = s_rec + slot * PointRec<W>::FLOATS;
+    float *rec = s_rec + slot * FL;
     rec[0] = __int_as_float((c0 - ts0 + 32) | ((c1 - ts1 + 32) << 8) | ((c2 - ts2 + 32) << 16));
 #pragma unroll
     for (int r = 0; r < W; ++r) {
@@ -164,97 +165,13 @@ __global__ void __launch_bounds__(kSpreadWarps * 32) spread_kernel(const SpreadP
       rec[1 + W + r] = w1[r];
       rec[1 + 2 * W + r] = w2[r];
     }
-    const int64_t id = sp_id(sp.idf);
+    const int id = sp_id(sp.idf);
     float sc = (a.nyquist && sp_nyquist(sp.idf)) ? 0.0f : a.scale;
     if (a.ctf) sc *= __ldg(a.ctf + id);
-#pragma unroll
-    for (int qq = 0; qq < CP; ++qq) {
-      const float2 *src = a.vals + id * a.ips + (int64_t)(a.ch0 + 2 * qq) * a.ics;
-      const float2 v0 = 2 * qq < a.nch ? __ldg(src) : make_float2(0.f, 0.f);
-      const float2 v1 = 2 * qq + 1 < a.nch ? __ldg(src + a.ics) : make_float2(0.f, 0.f);
-      s_val[slot * CP + qq] = make_float4(v0.x * sc, v0.y * sc, v1.x * sc, v1.y * sc);
-    }
+    s_pid[slot] = id;
+    s_sc[slot] = sc;
   }
-  __syncthreads();
-
-  // 2. tasks of this warp; lane (q, c): channel pair q, tile column c
-  const int warp = tid >> 5, lane = tid & 31;
-  const int q = lane / T, c = lane - (lane / T) * T;
-  const bool lane_live = q < CP;
-  const int qv = lane_live ? q : 0;
-  for (int s = 0; s < kPlanesPerWarp; ++s) {
-    const int task = __ldg(a.plane_sched + warp * kPlanesPerWarp + s);
-    if (task < 0) break;
-    const int pa = task >> 1, par = task & 1;
-    // corners l0 reaching plane pa: [pa - W + 1, pa]
-    const int b0lo = max(pa - W + 1 - kLMin, 0), b0hi = min(pa - kLMin, 15);
-    if (b0lo > b0hi) continue;
-    for (int b1 = 0; b1 < 16; ++b1) {
-      const int ibeg = s_off[(b1 << 4) | b0lo], iend = s_off[((b1 << 4) | b0hi) + 1];
-      if (ibeg >= iend) continue;
-      const int l1 = b1 + kLMin;
-      const int r0 = (par - l1) & 1;  // first window row whose tile row has parity par
-      float4 acc[NR];
-#pragma unroll
-      for (int u = 0; u < NR; ++u) acc[u] = make_float4(0.f, 0.f, 0.f, 0.f);
-      bool touched = false;
-      for (int i = ibeg; i < iend; ++i) {
-        const float *rec = s_rec + i * PointRec<W>::FLOATS;
-        const int packed = __float_as_int(rec[0]);
-        const int o0 = pa - ((packed & 255) - 32);  // in [0, W) by the range above
-        const int jj = c - (((packed >> 16) & 255) - 32);
-        if (!lane_live || jj < 0 || jj >= W) continue;
-        touched = true;
-        const float w02 = rec[1 + o0] * rec[1 + 2 * W + jj];
-        const float4 vv = s_val[i * CP + qv];
-#pragma unroll
-        for (int u = 0; u < NR; ++u) {
-          const int r = r0 + 2 * u;
-          if (r < W) {
-            const float w = w02 * rec[1 + W + r];
-            acc[u].x = fmaf(w, vv.x, acc[u].x);
-            acc[u].y = fmaf(w, vv.y, acc[u].y);
-            acc[u].z = fmaf(w, vv.z, acc[u].z);
-            acc[u].w = fmaf(w, vv.w, acc[u].w);
-          }
-        }
-      }
-      if (!touched) continue;
-#pragma unroll
-      for (int u = 0; u < NR; ++u) {
-        const int r = r0 + 2 * u;
-        const int r1 = l1 + r;
-        if (r >= W || (KT != COV3D_KERNEL_ES && r1 < 0)) continue;
-        const int e = ((pa * T + r1) * T + c) * CP + q;
-        if (!COMP) {
-          float4 x = hi[e];
-          x.x += acc[u].x;
-          x.y += acc[u].y;
-          x.z += acc[u].z;
-          x.w += acc[u].w;
-          hi[e] = x;
-        } else {
-          float4 x = hi[e], err = lo[e];
-          const float d[4] = {acc[u].x, acc[u].y, acc[u].z, acc[u].w};
-          float *xs = &x.x, *es = &err.x;
-#pragma unroll
-          for (int v = 0; v < 4; ++v) {  // TwoSum (Knuth): xs + d = s2 + rounding error, exactly
-            const float s2 = xs[v] + d[v];
-            const float bb = s2 - xs[v];
-            es[v] += (xs[v] - (s2 - bb)) + (d[v] - bb);
-            xs[v] = s2;
-          }
-          hi[e] = x;
-          lo[e] = err;
-        }
-      }
-    }
-  }
-  __syncthreads();
-
-  // 3. add the tile to the global grid: per-row global offsets and per-cell axis-2 offsets first
-  long long *s_rowoff = reinterpret_cast<long long *>(s_val);  // reuses the staged values
-  int *s_coloff = reinterpret_cast<int *>(s_rowoff + T * T);
+  // global offsets of the tile's rows (axes 0, 1) and columns (axis 2)
   for (int e = tid; e < T * T; e += blockDim.x) {
     const int ra = e / T, rb = e - (e / T) * T;
     int m0 = ts0 + ra, m1 = ts1 + rb;
@@ -283,73 +200,142 @@ __global__ void __launch_bounds__(kSpreadWarps * 32) spread_kernel(const SpreadP
     m2 = m2 >= n ? m2 - n : m2;
     s_coloff[e] = ok ? m2 : -1;
   }
-  __syncthreads();
-  for (int e = tid; e < TILE4; e += blockDim.x) {
-    const int qq = e % CP;
-    const int cell = e / CP;
-    const int cc = cell % T, rowi = cell / T;
-    const long long ro = s_rowoff[rowi];
-    const int co = s_coloff[cc];
-    if (ro < 0 || co < 0) continue;
-    float4 x = hi[e];
-    if (COMP) {
-      const float4 c = lo[e];
-      x.x += c.x;
-      x.y += c.y;
-      x.z += c.z;
-      x.w += c.w;
+
+  const int lane = tid & 31;
+  const int g = lane / T, c = lane - (lane / T) * T;
+  const bool lane_live = g < G;
+  const int npairs = (a.nch + 1) / 2;
+  for (int p0 = 0; p0 < npairs; p0 += NP) {  // channel groups of NP pairs
+    __syncthreads();
+    // 1c. this group's scaled channel pairs, in sorted order
+    for (int e = tid; e < cnt * NP; e += blockDim.x) {
+      const int slot = e / NP, pp = p0 + (e - (e / NP) * NP);
+      const float sc = s_sc[slot];
+      const float2 *src = a.vals + (int64_t)s_pid[slot] * a.ips + (int64_t)(a.ch0 + 2 * pp) * a.ics;
+      const float2 v0 = 2 * pp < a.nch ? __ldg(src) : make_float2(0.f, 0.f);
+      const float2 v1 = 2 * pp + 1 < a.nch ? __ldg(src + a.ics) : make_float2(0.f, 0.f);
+      s_val[e] = make_float4(v0.x * sc, v0.y * sc, v1.x * sc, v1.y * sc);
     }
-    float2 *dst = a.grid + (ro + co) * a.cs + (int64_t)(a.ch0 + 2 * qq) * a.chs;
-    if (2 * qq < a.nch && (x.x != 0.0f || x.y != 0.0f)) atomicAdd(dst, make_float2(x.x, x.y));
-    if (2 * qq + 1 < a.nch && (x.z != 0.0f || x.w != 0.0f)) atomicAdd(dst + a.chs, make_float2(x.z, x.w));
+    if (tid == 0) *s_task = 0;
+    __syncthreads();
+
+    // 2. row tasks
+    for (;;) {
+      int task = 0;
+      if (lane == 0) task = atomicAdd(s_task, 1);
+      task = __shfl_sync(0xffffffffu, task, 0);
+      if (task >= T * T) break;
+      const int pa = task / T, r1 = task - (task / T) * T;
+      const int b0lo = max(pa - W + 1 - kLMin, 0), b0hi = min(pa - kLMin, 15);
+      float4 hi[CPL], lo[CPL];
+#pragma unroll
+      for (int u = 0; u < CPL; ++u) {
+        hi[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+        lo[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+      bool any = false;
+      for (int o1 = 0; o1 < W; ++o1) {  // window row o1 of the points with l1 = r1 - o1
+        const int b1 = r1 - o1 - kLMin;
+        if (b1 < 0 || b1 > 15 || b0lo > b0hi) continue;
+        const int ibeg = s_off[(b1 << 4) | b0lo], iend = s_off[((b1 << 4) | b0hi) + 1];
+        if (ibeg >= iend) continue;
+        float4 part[CPL];
+#pragma unroll
+        for (int u = 0; u < CPL; ++u) part[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+        bool got = false;
+        for (int i = ibeg; i < iend; ++i) {
+          const float *rec = s_rec + i * FL;
+          const int packed = __float_as_int(rec[0]);
+          const int o0 = pa - ((packed & 255) - 32);  // in [0, W) by the range
+          const int jj = c - (((packed >> 16) & 255) - 32);
+          if (!lane_live || jj < 0 || jj >= W) continue;
+          got = true;
+          const float w = rec[1 + o0] * rec[1 + W + o1] * rec[1 + 2 * W + jj];
+#pragma unroll
+          for (int u = 0; u < CPL; ++u) {
+            const float4 vv = s_val[i * NP + g + G * u];
+            part[u].x = fmaf(w, vv.x, part[u].x);
+            part[u].y = fmaf(w, vv.y, part[u].y);
+            part[u].z = fmaf(w, vv.z, part[u].z);
+            part[u].w = fmaf(w, vv.w, part[u].w);
+          }
+        }
+        if (!got) continue;
+        any = true;
+#pragma unroll
+        for (int u = 0; u < CPL; ++u) {
+          if (!COMP) {
+            hi[u].x += part[u].x;
+            hi[u].y += part[u].y;
+            hi[u].z += part[u].z;
+            hi[u].w += part[u].w;
+          } else {
+            float *xs = &hi[u].x, *es = &lo[u].x;
+            const float *d = &part[u].x;
+#pragma unroll
+            for (int v = 0; v < 4; ++v) {  // TwoSum (Knuth): xs + d = s2 + rounding error, exactly
+              const float s2 = xs[v] + d[v];
+              const float bb = s2 - xs[v];
+              es[v] += (xs[v] - (s2 - bb)) + (d[v] - bb);
+              xs[v] = s2;
+            }
+          }
+        }
+      }
+      // 3. the finished cell goes to the global grid
+      if (!any) continue;
+      const long long ro = s_rowoff[pa * T + r1];
+      const int co = s_coloff[c];
+      if (ro < 0 || co < 0) continue;
+#pragma unroll
+      for (int u = 0; u < CPL; ++u) {
+        const int pp = p0 + g + G * u;
+        float4 x = hi[u];
+        if (COMP) {
+          x.x += lo[u].x;
+          x.y += lo[u].y;
+          x.z += lo[u].z;
+          x.w += lo[u].w;
+        }
+        float2 *dst = a.grid + (ro + co) * a.cs + (int64_t)(a.ch0 + 2 * pp) * a.chs;
+        if (2 * pp < a.nch && (x.x != 0.0f || x.y != 0.0f)) atomicAdd(dst, make_float2(x.x, x.y));
+        if (2 * pp + 1 < a.nch && (x.z != 0.0f || x.w != 0.0f)) atomicAdd(dst + a.chs, make_float2(x.z, x.w));
+      }
+    }
   }
 }
 
-template <int KT, int W, int CP, bool COMP>
+template <int KT, int W, int CPL, bool COMP>
 int launch_one(const SpreadParams &a, int64_t max_blocks, cudaStream_t st) {
-  constexpr int T = kBin + W - 1;
-  const size_t smem = (size_t)(COMP ? 2 : 1) * T * T * T * CP * sizeof(float4) +
-                      (size_t)a.max_sub * (CP * sizeof(float4) + PointRec<W>::FLOATS * 4 + sizeof(int)) +
-                      (2 * kKeys + 1) * sizeof(int);
+  constexpr int T = SpreadLanes<W>::T;
+  constexpr int NP = spread_pairs<W>(CPL);
+  const size_t smem = (size_t)a.max_sub * (NP * sizeof(float4) + PointRec<W>::FLOATS * 4 + 3 * sizeof(int)) +
+                      (size_t)T * T * sizeof(long long) + (2 * kKeys + 2 + T) * sizeof(int);
   if (smem > 227 * 1024) {
-    set_error("spreading tile of %zu bytes exceeds shared memory", smem);
+    set_error("spreading stage of %zu bytes exceeds shared memory", smem);
     return COV3D_EINVAL;
   }
   if (smem > 32 * 1024) {  // static shared arrays come on top of the dynamic size
-    cudaError_t e = cudaFuncSetAttribute(spread_kernel<KT, W, CP, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(spread_kernel<KT, W, CPL, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return check_cuda(e, "cudaFuncSetAttribute(spread_kernel)");
   }
-  spread_kernel<KT, W, CP, COMP><<<(unsigned)max_blocks, kSpreadWarps * 32, smem, st>>>(a);
+  spread_kernel<KT, W, CPL, COMP><<<(unsigned)max_blocks, kSpreadWarps * 32, smem, st>>>(a);
   return launched("spread_kernel");
 }
 
+// One launch for all channels: the block sorts and stages its points once and spreads the
+// channels in groups of G * CPL pairs, CPL the smallest count that covers them (at most 3).
 template <int KT, int W, bool COMP>
 int launch_wc(SpreadParams a, int nchan, int64_t max_blocks, cudaStream_t st) {
-  constexpr int CPMAX = SpreadCP<W, COMP>::value;
-  int done = 0;
-  while (done < nchan) {
-    const int left = nchan - done;
-    a.ch0 = done;
-    int s = COV3D_OK, ch = 0;
-    if (left >= 2 * CPMAX || left > 4) {
-      ch = left < 2 * CPMAX ? left : 2 * CPMAX;
-      a.nch = ch;
-      s = launch_one<KT, W, CPMAX, COMP>(a, max_blocks, st);
-    } else if (left > 2) {
-      ch = left;
-      a.nch = ch;
-      s = launch_one<KT, W, (CPMAX > 2 ? 2 : CPMAX), COMP>(a, max_blocks, st);
-      if (CPMAX < 2) ch = 2 * CPMAX;
-    } else {
-      ch = left;
-      a.nch = ch;
-      s = launch_one<KT, W, 1, COMP>(a, max_blocks, st);
-    }
-    if (s != COV3D_OK) return s;
-    done += ch;
-  }
-  return COV3D_OK;
+  constexpr int G = SpreadLanes<W>::G;
+  a.ch0 = 0;
+  a.nch = nchan;
+  const int npairs = (nchan + 1) / 2;
+  const int cpl = (npairs + G - 1) / G;
+  if (cpl <= 1) return launch_one<KT, W, 1, COMP>(a, max_blocks, st);
+  if (cpl == 2) return launch_one<KT, W, 2, COMP>(a, max_blocks, st);
+  return launch_one<KT, W, kMaxCPL, COMP>(a, max_blocks, st);
 }
 
 template <int KT, int W>
@@ -398,40 +384,6 @@ __global__ void spread_unagg_kernel(PointGeom g, KernelSpec k, int64_t M, const 
 
 }  // namespace
 
-// Warp tasks: (tile plane a, row parity) pairs, encoded 2 * a + parity.  Plane a is reached by
-// the points whose axis-0 window corner lies in [a - W + 1, a] (clipped to the bin), and a
-// parity holds about half of each window's rows: tasks are assigned greedily, heaviest first,
-// to the least loaded warp, so all warps get equal work.
-int build_plane_schedule(cov3d_plan *p) {
-  const int W = p->kernel == COV3D_KERNEL_NEAREST ? 1 : p->kernel == COV3D_KERNEL_LINEAR ? 2 : p->width;
-  const int T = kBin + W - 1;
-  std::vector<int> order(2 * T), load(kSpreadWarps, 0), count(kSpreadWarps, 0);
-  std::vector<int> sched(kSpreadWarps * kPlanesPerWarp, -1);
-  auto work = [&](int task) {
-    const int x = task >> 1;
-    const int lo = x - W + 1 > 0 ? x - W + 1 : 0;
-    const int hi = x < kBin - 1 ? x : kBin - 1;
-    const int rows = (task & 1) ? W / 2 : (W + 1) / 2;
-    return hi >= lo ? (hi - lo + 1) * rows : 0;
-  };
-  for (int i = 0; i < 2 * T; ++i) order[i] = i;
-  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return work(x) > work(y); });
-  for (int task : order) {
-    int best = -1;
-    for (int w = 0; w < kSpreadWarps; ++w)
-      if (count[w] < kPlanesPerWarp && (best < 0 || load[w] < load[best])) best = w;
-    if (best < 0) {
-      set_error("cannot schedule %d tile planes", T);
-      return COV3D_EINVAL;
-    }
-    sched[best * kPlanesPerWarp + count[best]++] = task;
-    load[best] += work(task);
-  }
-  COV3D_TRY(grow(p->row_order, (int64_t)sched.size() * 4));
-  return check_cuda(cudaMemcpy(p->row_order.ptr, sched.data(), sched.size() * 4, cudaMemcpyHostToDevice),
-                    "cudaMemcpy(plane schedule)");
-}
-
 int launch_spread(cov3d_plan *p, const void *values, int64_t in_ps, int64_t in_cs, int nchan, const EpilogueArgs &e,
                   void *grid, int64_t cell_stride, int64_t chan_stride, int shift) {
   if (p->point_kind == kPointsNone || p->n_points == 0) {
@@ -458,7 +410,6 @@ int launch_spread(cov3d_plan *p, const void *values, int64_t in_ps, int64_t in_c
   a.chs = chan_stride;
   a.shift = shift;
   a.max_sub = p->max_sub;
-  a.plane_sched = p->row_order.as<int>();
   if (p->bins.bs[0] != kBin || p->bins.bs[1] != kBin || p->bins.bs[2] != kBin) {
     set_error("spreading requires %d^3-cell bins", kBin);
     return COV3D_EINVAL;

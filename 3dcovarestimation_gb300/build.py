@@ -6,6 +6,7 @@ changed.  Usage: ``python 3dcovarestimation_gb300/build.py [--force]``.
 
 import concurrent.futures
 import os
+import shlex
 import shutil
 import subprocess
 import sys
@@ -45,7 +46,7 @@ def _compile(src, force, hmt):
     if not force and os.path.exists(obj):
         if os.path.getmtime(obj) >= max(os.path.getmtime(path), hmt):
             return obj, None
-    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-c", path, "-o", obj]
+    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *shlex.split(os.environ.get("COV3D_NVCC_EXTRA", "")), "-c", path, "-o", obj]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         return obj, f"{' '.join(cmd)}\n{res.stdout}\n{res.stderr}"

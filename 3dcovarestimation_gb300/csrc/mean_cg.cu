@@ -87,52 +87,81 @@ __global__ void load_centered_kernel(const float2 *__restrict__ src, const float
   fine[cell] = v;
 }
 
+// The grid kernels walk whole rows (one division per row, none per element) and the reductions
+// run a capped grid of blocks in grid-stride loops, so each reduction costs one FP64 atomic per
+// block rather than one per 256 elements.
+constexpr int kRowBlocks = 1216;  // 8 blocks of 256 threads per SM
+
+inline unsigned capped(int64_t n_items_per_block_unit) {
+  return (unsigned)(n_items_per_block_unit < kRowBlocks ? (n_items_per_block_unit > 0 ? n_items_per_block_unit : 1)
+                                                        : kRowBlocks);
+}
+
+// voxel index of FFT-native storage index s on the padded axis, or -1 for padding
+__device__ __forceinline__ int pad_voxel(int s, int L, int n) {
+  const int h = L / 2;
+  return s < L - h ? s + h : (s >= n - h ? s - n + h : -1);
+}
+// FFT-native storage index of voxel j
+__device__ __forceinline__ int voxel_store(int j, int L, int n) {
+  const int k = j - L / 2;
+  return k < 0 ? k + n : k;
+}
+
 // zero-pad x (L^3, voxel offset k = j - L/2) into FFT-native storage k mod n
 __global__ void pad_kernel(const float2 *__restrict__ x, int L, int n, float2 *__restrict__ fine, const CgState *st) {
   if (stopped(st)) return;
-  const int64_t n3 = (int64_t)n * n * n;
-  const int64_t cell = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (cell >= n3) return;
-  const int h = L / 2;
-  auto vox = [&](int s) { return s < L - h ? s + h : (s >= n - h ? s - n + h : -1); };
-  const int j2 = vox((int)(cell % n)), j1 = vox((int)((cell / n) % n)), j0 = vox((int)(cell / ((int64_t)n * n)));
-  fine[cell] = (j0 < 0 || j1 < 0 || j2 < 0) ? make_float2(0.f, 0.f) : x[((int64_t)j0 * L + j1) * L + j2];
+  for (int64_t row = blockIdx.x; row < (int64_t)n * n; row += gridDim.x) {
+    const int s0 = (int)(row / n), s1 = (int)(row - (int64_t)s0 * n);
+    const int j0 = pad_voxel(s0, L, n), j1 = pad_voxel(s1, L, n);
+    float2 *dst = fine + row * n;
+    if (j0 < 0 || j1 < 0) {
+      for (int s2 = threadIdx.x; s2 < n; s2 += blockDim.x) dst[s2] = make_float2(0.f, 0.f);
+      continue;
+    }
+    const float2 *src = x + ((int64_t)j0 * L + j1) * L;
+    for (int s2 = threadIdx.x; s2 < n; s2 += blockDim.x) {
+      const int j2 = pad_voxel(s2, L, n);
+      dst[s2] = j2 < 0 ? make_float2(0.f, 0.f) : src[j2];
+    }
+  }
 }
 
-// fine[s] *= diag[centered(s)] * scale (divide instead when `divide`)
+// g[s] *= diag[centered(s)] * scale (divide instead when `divide`), g an m^3 FFT-native grid
 __global__ void fine_diag_kernel(float2 *__restrict__ g, const float *__restrict__ diag, int m, int divide, float scale,
                                  const CgState *st) {
   if (stopped(st)) return;
-  const int64_t m3 = (int64_t)m * m * m;
-  const int64_t cell = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (cell >= m3) return;
-  const int s2 = (int)(cell % m), s1 = (int)((cell / m) % m), s0 = (int)(cell / ((int64_t)m * m));
-  const float d =
-      __ldg(diag + ((int64_t)native_to_centered(s0, m) * m + native_to_centered(s1, m)) * m + native_to_centered(s2, m));
-  const float f = divide ? scale / d : scale * d;
-  const float2 v = g[cell];
-  g[cell] = make_float2(v.x * f, v.y * f);
+  for (int64_t row = blockIdx.x; row < (int64_t)m * m; row += gridDim.x) {
+    const int s0 = (int)(row / m), s1 = (int)(row - (int64_t)s0 * m);
+    const float *drow = diag + ((int64_t)native_to_centered(s0, m) * m + native_to_centered(s1, m)) * m;
+    float2 *grow = g + row * m;
+    for (int s2 = threadIdx.x; s2 < m; s2 += blockDim.x) {
+      const float d = __ldg(drow + native_to_centered(s2, m));
+      const float f = divide ? scale / d : scale * d;
+      const float2 v = grow[s2];
+      grow[s2] = make_float2(v.x * f, v.y * f);
+    }
+  }
 }
 
 // out = crop(fine) / n^3; optionally keep only the real part; optionally accumulate <p, out>
 __global__ void crop_kernel(const float2 *__restrict__ fine, int L, int n, float2 *__restrict__ out, int real_only,
                             const float2 *__restrict__ p, CgState *st) {
   if (stopped(st)) return;
-  const int64_t L3 = (int64_t)L * L * L;
-  const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const float inv = 1.0f / ((float)n * (float)n * (float)n);
   double re = 0.0, im = 0.0;
-  if (v < L3) {
-    const int h = L / 2;
-    auto sto = [&](int j) { return j - h < 0 ? j - h + n : j - h; };
-    const int j2 = (int)(v % L), j1 = (int)((v / L) % L), j0 = (int)(v / ((int64_t)L * L));
-    const float inv = 1.0f / ((float)n * (float)n * (float)n);
-    const float2 a = fine[((int64_t)sto(j0) * n + sto(j1)) * n + sto(j2)];
-    const float2 y = make_float2(a.x * inv, real_only ? 0.0f : a.y * inv);
-    out[v] = y;
-    if (p) {  // conj(p) * y
-      const float2 q = p[v];
-      re = (double)q.x * y.x + (double)q.y * y.y;
-      im = (double)q.x * y.y - (double)q.y * y.x;
+  for (int64_t row = blockIdx.x; row < (int64_t)L * L; row += gridDim.x) {
+    const int j0 = (int)(row / L), j1 = (int)(row - (int64_t)j0 * L);
+    const float2 *src = fine + ((int64_t)voxel_store(j0, L, n) * n + voxel_store(j1, L, n)) * n;
+    for (int j2 = threadIdx.x; j2 < L; j2 += blockDim.x) {
+      const float2 a = src[voxel_store(j2, L, n)];
+      const float2 y = make_float2(a.x * inv, real_only ? 0.0f : a.y * inv);
+      out[row * L + j2] = y;
+      if (p) {  // conj(p) * y
+        const float2 q = p[row * L + j2];
+        re += (double)q.x * y.x + (double)q.y * y.y;
+        im += (double)q.x * y.y - (double)q.y * y.x;
+      }
     }
   }
   if (p) block_add2(re, im, &st->pap[0], &st->pap[1]);
@@ -140,14 +169,13 @@ __global__ void crop_kernel(const float2 *__restrict__ fine, int L, int n, float
 
 // r = b - r (r holds A x on entry); accumulate <r, r> and <b, b>
 __global__ void residual_kernel(const float2 *__restrict__ b, float2 *__restrict__ r, int64_t N, CgState *st) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   double rr = 0.0, bb = 0.0;
-  if (i < N) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
     const float2 bv = b[i], ax = r[i];
     const float2 rv = make_float2(bv.x - ax.x, bv.y - ax.y);
     r[i] = rv;
-    rr = (double)rv.x * rv.x + (double)rv.y * rv.y;
-    bb = (double)bv.x * bv.x + (double)bv.y * bv.y;
+    rr += (double)rv.x * rv.x + (double)rv.y * rv.y;
+    bb += (double)bv.x * bv.x + (double)bv.y * bv.y;
   }
   block_add2(rr, bb, &st->rr, &st->b2);
 }
@@ -155,13 +183,12 @@ __global__ void residual_kernel(const float2 *__restrict__ b, float2 *__restrict
 // Re <r, z> into st->rz_new
 __global__ void dot_rz_kernel(const float2 *__restrict__ r, const float2 *__restrict__ z, int64_t N, CgState *st) {
   if (stopped(st)) return;
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  double s = 0.0;
-  if (i < N) {
+  double acc = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
     const float2 a = r[i], c = z[i];
-    s = (double)a.x * c.x + (double)a.y * c.y;
+    acc += (double)a.x * c.x + (double)a.y * c.y;
   }
-  block_add2(s, 0.0, &st->rz_new, nullptr);
+  block_add2(acc, 0.0, &st->rz_new, nullptr);
 }
 
 // alpha = rz / <p, Ap>;  x += alpha p;  r -= alpha Ap;  accumulate <r, r>
@@ -171,9 +198,8 @@ __global__ void update_kernel(float2 *__restrict__ x, float2 *__restrict__ r, co
   const double pr = st->pap[0], pi = st->pap[1];
   const double den = pr * pr + pi * pi;
   const float ar = (float)(st->rz * pr / den), ai = (float)(-st->rz * pi / den);
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   double rr = 0.0;
-  if (i < N) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
     const float2 pv = p[i], av = ap[i];
     float2 xv = x[i], rv = r[i];
     xv.x += ar * pv.x - ai * pv.y;
@@ -182,7 +208,7 @@ __global__ void update_kernel(float2 *__restrict__ x, float2 *__restrict__ r, co
     rv.y -= ar * av.y + ai * av.x;
     x[i] = xv;
     r[i] = rv;
-    rr = (double)rv.x * rv.x + (double)rv.y * rv.y;
+    rr += (double)rv.x * rv.x + (double)rv.y * rv.y;
   }
   block_add2(rr, 0.0, &st->rr_new, nullptr);
 }
@@ -210,8 +236,7 @@ __global__ void check_kernel(CgState *st, double rtol, int preconditioned, doubl
 __global__ void direction_kernel(float2 *__restrict__ p, const float2 *__restrict__ z, int64_t N, const CgState *st) {
   if (stopped(st)) return;
   const float beta = (float)(st->rz_new / st->rz);
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < N) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
     const float2 zv = z[i], pv = p[i];
     p[i] = make_float2(zv.x + beta * pv.x, zv.y + beta * pv.y);
   }
@@ -454,14 +479,14 @@ int mean_init(cov3d_plan *p, const void *d_rhs, const float *d_reg, void *d_b, v
     load_centered_kernel<<<nb(n3), 256, 0, p->stream>>>(static_cast<const float2 *>(d_rhs), nullptr, nullptr, n, fine);
     COV3D_LAUNCHED("load_centered_kernel");
     COV3D_TRY(fft(h, fine, CUFFT_INVERSE));
-    crop_kernel<<<nb(L3), 256, 0, p->stream>>>(fine, L, n, static_cast<float2 *>(d_b), 0, nullptr, nullptr);
+    crop_kernel<<<capped((int64_t)L * L), 256, 0, p->stream>>>(fine, L, n, static_cast<float2 *>(d_b), 0, nullptr, nullptr);
     COV3D_LAUNCHED("crop_kernel");
   }
   if (d_x0) {
     load_centered_kernel<<<nb(n3), 256, 0, p->stream>>>(static_cast<const float2 *>(d_rhs), nullptr, d_reg, n, fine);
     COV3D_LAUNCHED("load_centered_kernel");
     COV3D_TRY(fft(h, fine, CUFFT_INVERSE));
-    crop_kernel<<<nb(L3), 256, 0, p->stream>>>(fine, L, n, static_cast<float2 *>(d_x0), 1, nullptr, nullptr);
+    crop_kernel<<<capped((int64_t)L * L), 256, 0, p->stream>>>(fine, L, n, static_cast<float2 *>(d_x0), 1, nullptr, nullptr);
     COV3D_LAUNCHED("crop_kernel");
   }
   return COV3D_OK;
@@ -508,42 +533,42 @@ int cg_solve(cov3d_plan *p, const float *d_lhs, const void *d_b, void *d_x, doub
 
   // out = A(in) (also <p, out> into st->pap when dotp is given)
   auto apply_A = [&](const float2 *in, float2 *out, const float2 *dotp, const CgState *gate) -> int {
-    pad_kernel<<<nb(n3), 256, 0, s>>>(in, L, n, fine, gate);
+    pad_kernel<<<capped((int64_t)n * n), 256, 0, s>>>(in, L, n, fine, gate);
     COV3D_LAUNCHED("pad_kernel");
     COV3D_TRY(fft(h, fine, CUFFT_FORWARD));
-    fine_diag_kernel<<<nb(n3), 256, 0, s>>>(fine, d_lhs, n, 0, 1.0f, gate);
+    fine_diag_kernel<<<capped((int64_t)n * n), 256, 0, s>>>(fine, d_lhs, n, 0, 1.0f, gate);
     COV3D_LAUNCHED("fine_diag_kernel");
     COV3D_TRY(fft(h, fine, CUFFT_INVERSE));
-    crop_kernel<<<nb(L3), 256, 0, s>>>(fine, L, n, out, 0, dotp, dotp ? st : const_cast<CgState *>(gate));
+    crop_kernel<<<capped((int64_t)L * L), 256, 0, s>>>(fine, L, n, out, 0, dotp, dotp ? st : const_cast<CgState *>(gate));
     return launched("crop_kernel");
   };
   // z = M(r)
   auto apply_M = [&](const float2 *in, float2 *out, const CgState *gate) -> int {
     if (precond == 1) {
-      pad_kernel<<<nb(n3), 256, 0, s>>>(in, L, n, fine, gate);
+      pad_kernel<<<capped((int64_t)n * n), 256, 0, s>>>(in, L, n, fine, gate);
       COV3D_LAUNCHED("pad_kernel");
       COV3D_TRY(fft(h, fine, CUFFT_FORWARD));
-      fine_diag_kernel<<<nb(n3), 256, 0, s>>>(fine, d_lhs, n, 1, 1.0f, gate);
+      fine_diag_kernel<<<capped((int64_t)n * n), 256, 0, s>>>(fine, d_lhs, n, 1, 1.0f, gate);
       COV3D_LAUNCHED("fine_diag_kernel");
       COV3D_TRY(fft(h, fine, CUFFT_INVERSE));
-      crop_kernel<<<nb(L3), 256, 0, s>>>(fine, L, n, out, 0, nullptr, const_cast<CgState *>(gate));
+      crop_kernel<<<capped((int64_t)L * L), 256, 0, s>>>(fine, L, n, out, 0, nullptr, const_cast<CgState *>(gate));
       return launched("crop_kernel");
     }
     copy_kernel<<<nb(L3), 256, 0, s>>>(in, out, L3);
     COV3D_LAUNCHED("copy_kernel");
     COV3D_TRY(fft(hc, out, CUFFT_FORWARD));
-    fine_diag_kernel<<<nb(L3), 256, 0, s>>>(out, d_sym, L, 1, 1.0f / (float)L3, gate);
+    fine_diag_kernel<<<capped((int64_t)L * L), 256, 0, s>>>(out, d_sym, L, 1, 1.0f / (float)L3, gate);
     COV3D_LAUNCHED("fine_diag_kernel");
     return fft(hc, out, CUFFT_INVERSE);
   };
 
   // r = b - A x0;  z = M r;  p = z
   COV3D_TRY(apply_A(x, r, nullptr, nullptr));
-  residual_kernel<<<nb(L3), 256, 0, s>>>(b, r, L3, st);
+  residual_kernel<<<capped(nb(L3)), 256, 0, s>>>(b, r, L3, st);
   COV3D_LAUNCHED("residual_kernel");
   if (precond) {
     COV3D_TRY(apply_M(r, z, nullptr));
-    dot_rz_kernel<<<nb(L3), 256, 0, s>>>(r, z, L3, st);
+    dot_rz_kernel<<<capped(nb(L3)), 256, 0, s>>>(r, z, L3, st);
     COV3D_LAUNCHED("dot_rz_kernel");
     copy_kernel<<<nb(L3), 256, 0, s>>>(z, pv, L3);
   } else {
@@ -564,18 +589,18 @@ int cg_solve(cov3d_plan *p, const float *d_lhs, const void *d_b, void *d_x, doub
 
   for (int it = 0; it < maxiter; ++it) {
     COV3D_TRY(apply_A(pv, ap, pv, st));
-    update_kernel<<<nb(L3), 256, 0, s>>>(x, r, pv, ap, L3, st);
+    update_kernel<<<capped(nb(L3)), 256, 0, s>>>(x, r, pv, ap, L3, st);
     COV3D_LAUNCHED("update_kernel");
     check_kernel<<<1, 1, 0, s>>>(st, rtol, precond ? 1 : 0, d_history, maxiter);
     COV3D_LAUNCHED("check_kernel");
     const float2 *zz = r;
     if (precond) {
       COV3D_TRY(apply_M(r, z, st));
-      dot_rz_kernel<<<nb(L3), 256, 0, s>>>(r, z, L3, st);
+      dot_rz_kernel<<<capped(nb(L3)), 256, 0, s>>>(r, z, L3, st);
       COV3D_LAUNCHED("dot_rz_kernel");
       zz = z;
     }
-    direction_kernel<<<nb(L3), 256, 0, s>>>(pv, zz, L3, st);
+    direction_kernel<<<capped(nb(L3)), 256, 0, s>>>(pv, zz, L3, st);
     COV3D_LAUNCHED("direction_kernel");
     roll_kernel<<<1, 1, 0, s>>>(st);
     COV3D_LAUNCHED("roll_kernel");

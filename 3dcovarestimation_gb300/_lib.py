@@ -37,7 +37,8 @@ class GridLayout(ctypes.Structure):
 class CostArgs(ctypes.Structure):
     _fields_ = [("objective", c_int), ("rank", c_int), ("d_vectors", c_void_p), ("d_log_sqrt", c_void_p),
                 ("d_images", c_void_p), ("d_ctf", c_void_p), ("noise_var", c_double), ("reg_scale", c_double),
-                ("d_fourier_reg", c_void_p), ("use_grid_correction", c_int), ("d_cost", c_void_p)]
+                ("d_fourier_reg", c_void_p), ("use_grid_correction", c_int), ("d_cost", c_void_p),
+                ("gram_bf16", c_int)]
 
 
 _SIGNATURES = {
@@ -72,6 +73,8 @@ _SIGNATURES = {
                                          c_void_p, c_double, c_void_p, c_void_p, c_void_p, c_void_p]),
     "cov3d_wpass": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_int64, c_int64, c_int64, c_void_p, c_void_p,
                             c_void_p, c_void_p, c_int64, c_int64, c_int64]),
+    "cov3d_gram_bf16": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_int64, c_int64, c_int64, c_void_p,
+                                c_void_p, c_void_p, c_void_p]),
     "cov3d_mean_accumulate": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int]),
     "cov3d_regularize_lhs": (c_int, [c_void_p, c_void_p, c_void_p]),
     "cov3d_mean_init": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),

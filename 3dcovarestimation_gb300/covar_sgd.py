@@ -174,8 +174,11 @@ class FusedCovarStep:
     """
 
     def __init__(self, resolution, rank, nufft_disc="nufft", upsampling_factor=2, width=6, eps=1e-6,
-                 compensated=True, device=None, bin_size=0):
+                 compensated=True, device=None, bin_size=0, gram_precision="fp32"):
         kernel = {"nufft": _lib.KERNEL_ES, "bilinear": _lib.KERNEL_LINEAR, "nearest": _lib.KERNEL_NEAREST}[nufft_disc]
+        if gram_precision not in ("fp32", "bf16"):
+            raise ValueError("gram_precision must be 'fp32' or 'bf16'")
+        self.gram_bf16 = gram_precision == "bf16"
         self.plan = _Plan(resolution, rank, eps, kernel, upsampling_factor,
                           width=width if kernel == _lib.KERNEL_ES else 0, compensated=compensated, bin_size=bin_size,
                           device=device)
@@ -210,13 +213,35 @@ class FusedCovarStep:
                              noise_var=float(noise_var), reg_scale=float(reg_scale),
                              d_fourier_reg=fr.data_ptr() if fr is not None else None,
                              use_grid_correction=0 if self.nufft_disc == "nufft_nogc" else 1,
-                             d_cost=self.d_cost.data_ptr())
+                             d_cost=self.d_cost.data_ptr(), gram_bf16=1 if self.gram_bf16 else 0)
         host_cost = _lib.c_double() if sync_cost else None
         with torch.cuda.device(self.device):
             _lib.call("cov3d_covar_cost_grad", self.plan.bind(), _lib.ctypes.byref(args),
                       _lib.ctypes.byref(host_cost) if host_cost is not None else None, _lib.ptr(gv), _lib.ptr(gl),
                       _lib.ptr(per_image))
         return (host_cost.value if host_cost is not None else self.d_cost), gv, gl
+
+
+def gram_bf16(Q, y, plan=None):
+    """Per-image gram (n, r, r), h (n, r), |y|^2 (n) of projections Q (n, r, P) and images y
+    (n, P) with BF16 inputs and FP32 accumulation on the tensor cores (``cov3d_gram_bf16``).
+    ``plan`` (a ``_Plan``) provides the BF16 workspace; one is made when not given."""
+    if not Q.is_cuda:
+        raise ValueError("gram_bf16 takes CUDA tensors")
+    n, r, P = Q.shape
+    dev = Q.device
+    Qc = Q.to(torch.complex64)
+    yc = y.to(torch.complex64).reshape(n, P).contiguous()
+    if plan is None:
+        plan = _Plan(8, 1, 1e-6, _lib.KERNEL_NEAREST, 1, device=dev)
+    gram = torch.empty((n, r, r), dtype=torch.complex64, device=dev)
+    h = torch.empty((n, r), dtype=torch.complex64, device=dev)
+    yy = torch.empty((n,), dtype=torch.float32, device=dev)
+    s = Qc.stride()
+    with torch.cuda.device(dev):
+        _lib.call("cov3d_gram_bf16", plan.bind(), n, P, r, _lib.ptr(Qc), s[0], s[2], s[1], _lib.ptr(yc), _lib.ptr(gram),
+                  _lib.ptr(h), _lib.ptr(yy))
+    return gram, h, yy
 
 
 class CovarTrainer:

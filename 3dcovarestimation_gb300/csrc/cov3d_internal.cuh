@@ -125,6 +125,7 @@ struct cov3d_plan {
   cov3d::DevBuf small;         // per-image small matrices
   cov3d::DevBuf acc;           // double accumulators
   cov3d::DevBuf cgw;           // mean / CG workspace (state, vectors, shell sums)
+  cov3d::DevBuf xbf, gsum;     // BF16 Gram operands and real Gram sums
   double *h_acc = nullptr;     // pinned host mirror of acc (64 doubles)
   std::map<int, cufftHandle> *ffts = nullptr;  // cuFFT plans by channel count
 
@@ -194,6 +195,9 @@ int launch_gc_volume(const cov3d_plan *p, float *out);
 int launch_zero(cov3d_plan *p, void *ptr, int64_t bytes);
 
 // gram_solve.cu
+int launch_gram_bf16(cov3d_plan *p, cudaStream_t st, int B, int P, int r, const void *q, int64_t is, int64_t ps,
+                     int64_t cs, const void *images, void *gram, void *h, float *yy);
+int read_gram_bf16_error(cov3d_plan *p, cudaStream_t st, int B, int r);
 int launch_gram(cudaStream_t st, int B, int P, int r, const void *q, int64_t is, int64_t ps, int64_t cs,
                 const void *images, void *gram, void *h, float *yy);
 int launch_wpass(cudaStream_t st, int B, int P, int r, const void *q, int64_t is, int64_t ps, int64_t cs,

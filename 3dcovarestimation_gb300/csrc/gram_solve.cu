@@ -422,7 +422,11 @@ int covar_cost_grad(cov3d_plan *p, const cov3d_cost_args *a, double *h_cost, dou
   // 4. per-image Gram, 5. FP64 solve -> cost, C, u
   {
     PhaseScope ps(p, kPhaseGram);
-    COV3D_TRY(launch_gram(p->stream, B, P, r, p->q.ptr, (int64_t)P * r, r, 1, a->d_images, gram, h, yy));
+    if (a->gram_bf16) {
+      COV3D_TRY(launch_gram_bf16(p, p->stream, B, P, r, p->q.ptr, (int64_t)P * r, r, 1, a->d_images, gram, h, yy));
+    } else {
+      COV3D_TRY(launch_gram(p->stream, B, P, r, p->q.ptr, (int64_t)P * r, r, 1, a->d_images, gram, h, yy));
+    }
   }
   const double L4 = (double)L * L * L * L;
   {

@@ -324,7 +324,7 @@ int cov3d_plan_destroy(cov3d_plan *p) {
   }
   DevBuf *bufs[] = {&p->gc1d, &p->pts, &p->rot, &p->bin_count, &p->bin_off, &p->sub_off, &p->pt_bin, &p->pt_rank,
                     &p->perm, &p->sorted, &p->sub_bin, &p->sub_first, &p->sub_count, &p->nsub, &p->fine, &p->fine2, &p->q,
-                    &p->small, &p->acc, &p->cgw};
+                    &p->small, &p->acc, &p->cgw, &p->xbf, &p->gsum};
   for (DevBuf *b : bufs) release(*b);
   if (p->h_acc) cudaFreeHost(p->h_acc);
   if (p->ev_pool) {
@@ -549,6 +549,18 @@ int cov3d_gram(void *stream, int n_images, int P, int r, const void *d_q, int64_
   }
   return launch_gram(static_cast<cudaStream_t>(stream), n_images, P, r, d_q, img_stride, point_stride, chan_stride,
                      d_images, d_gram, d_h, d_yy);
+}
+
+int cov3d_gram_bf16(cov3d_plan *p, int n_images, int P, int r, const void *d_q, int64_t img_stride,
+                    int64_t point_stride, int64_t chan_stride, const void *d_images, void *d_gram, void *d_h,
+                    float *d_yy) {
+  if (!valid(p) || n_images < 1 || P < 1 || !d_q || !d_images || !d_gram || !d_h || !d_yy) {
+    set_error("invalid gram_bf16 arguments");
+    return COV3D_EINVAL;
+  }
+  COV3D_TRY(launch_gram_bf16(p, p->stream, n_images, P, r, d_q, img_stride, point_stride, chan_stride, d_images, d_gram,
+                             d_h, d_yy));
+  return read_gram_bf16_error(p, p->stream, n_images, r);
 }
 
 int cov3d_cost_solve(void *stream, int n_images, int r, int objective, const void *d_gram, const void *d_h,

@@ -416,15 +416,15 @@ def save(net: UNet3D, path: str = WEIGHTS_PATH):
 
 def main(argv=None):
     """Train the preconditioner network on the GPU and save its weights (the committed weights
-    were made with the defaults: L=128, 24 problems of 100,000 images, 4 epochs, K=40)."""
+    were made with the defaults: L=128, 48 problems of 100,000 images, 8 epochs, K=60)."""
     import argparse
 
     ap = argparse.ArgumentParser(description=main.__doc__)
     ap.add_argument("--L", type=int, default=128)
     ap.add_argument("--images", type=int, default=100000)
-    ap.add_argument("--problems", type=int, default=24)
-    ap.add_argument("--epochs", type=int, default=4)
-    ap.add_argument("--K", type=int, default=40)
+    ap.add_argument("--problems", type=int, default=48)
+    ap.add_argument("--epochs", type=int, default=8)
+    ap.add_argument("--K", type=int, default=60)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--seed", type=int, default=1000)
     ap.add_argument("--out", default=WEIGHTS_PATH)

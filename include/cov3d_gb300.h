@@ -170,6 +170,8 @@ typedef struct {
   const float *d_fourier_reg; /* (n^3) float32 centered, or NULL (ML regulariser :1373-1376) */
   int use_grid_correction;  /* divide by the kernel's deapodisation factors (init_grid_correction) */
   double *d_cost;           /* optional device scalar receiving the cost (no host sync needed) */
+  int gram_bf16;            /* 1: per-image Gram contractions in BF16 on the tensor cores (FP32
+                               accumulation, cov3d_gram_bf16); 0: FP32 on the CUDA cores */
 } cov3d_cost_args;
 
 /* Outputs: d_grad_vectors (r, L^3) float32, d_grad_log_sqrt (r) float32, optional
@@ -260,6 +262,14 @@ int cov3d_circulant_symbol(cov3d_plan *plan, const float *d_reg_lhs, float *d_sy
  * (with d_x holding the last iterate) when the tolerance was not reached. */
 int cov3d_cg_solve(cov3d_plan *plan, const float *d_reg_lhs, const void *d_b, void *d_x, double rtol, int maxiter,
                    int precond, const float *d_symbol, int *iters, double *relres, double *d_history);
+
+/* No counterpart in the reference (its contraction is a batched complex GEMM at the input
+ * precision): the outputs of cov3d_gram with BF16 inputs and FP32 accumulation on the tensor
+ * cores (tcgen05).  Q and y are rounded to BF16 (relative error 2^-9 per element); the plan
+ * provides the workspace (n_images * (2r+2) * P BF16 values).  Requires 2(r+1) <= 128. */
+int cov3d_gram_bf16(cov3d_plan *plan, int n_images, int P, int r, const void *d_q, int64_t img_stride,
+                    int64_t point_stride, int64_t chan_stride, const void *d_images, void *d_gram, void *d_h,
+                    float *d_yy);
 
 /* ------------------------------------------------------------------ learned CG preconditioner
  * No counterpart in the reference.  Layers of the small 3D U-Net that predicts a correction of

@@ -52,6 +52,7 @@ def parse():
     ap.add_argument("--mean-rtol", type=float, default=1e-5)
     ap.add_argument("--mean-maxiter", type=int, default=20000)
     ap.add_argument("--no-mean", action="store_true", help="skip the mean-CG measurement")
+    ap.add_argument("--no-bf16", action="store_true", help="skip the BF16-Gram variant of the step")
     return ap.parse_args()
 
 
@@ -385,6 +386,39 @@ def run_gb300(args):
     e2e_value = world * B * e2e_steps / e2e_s
     h2d = d_img.numel() * 8 + d_ctf.numel() * 4 + d_rot.numel() * 4
 
+    # the same step with the per-image Gram contractions in BF16 on the tensor cores
+    bf16 = None
+    if not args.no_bf16:
+        step_bf = pkg.FusedCovarStep(L, r, "nufft", 2, width=args.width, device=dev,
+                                     compensated=not args.uncompensated, gram_precision="bf16")
+
+        def step16(k):
+            b = (k * world + rank) % nb
+            step_bf.set_rotations(rot[b])
+            c, _, _ = step_bf(covar.vectors.detach(), covar.log_sqrt_eigenvals.detach(), images[b], ctf[b], noise_var,
+                              reg_scale, fourier_reg, grad_vectors=covar.vectors.grad,
+                              grad_log_sqrt=covar.log_sqrt_eigenvals.grad)
+            return c
+
+        for k in range(2):
+            step16(k)
+        barrier()
+        step_bf.plan.timing(True)
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        nbf = max(3, args.steps // 2)
+        f0.record(stream)
+        for k in range(nbf):
+            step16(k)
+        f1.record(stream)
+        barrier()
+        ph16 = step_bf.plan.timing_read()
+        step_bf.plan.timing(False)
+        ms16 = f0.elapsed_time(f1) / nbf
+        bf16 = {"ms_per_step": ms16, "images_per_s": world * B / (ms16 / 1e3), "steps": nbf,
+                "gram_ms": ph16["gram"][0] / nbf, "gram_ms_fp32": phases["gram"][0] / args.steps,
+                "note": "Gram contractions in BF16 with FP32 accumulation (tcgen05); projections, spreading, "
+                        "solve and update unchanged (FP32 / FP64)"}
+
     if rank != 0:
         if world > 1:
             import torch.distributed as dist
@@ -426,6 +460,8 @@ def run_gb300(args):
         "phases_ms_per_step": {k: v[0] / args.steps for k, v in phases.items() if v[1]},
         "final_cost": float(cost_acc) / (args.warmup + args.steps),
     }
+    if bf16 is not None:
+        line["bf16_gram"] = bf16
     if not args.no_mean:
         line["mean_cg"] = run_mean_cg(pkg, args, dev)
     if not args.no_cpu_baseline:

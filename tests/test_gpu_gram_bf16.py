@@ -69,3 +69,71 @@ def test_fused_step_with_bf16_gram(pkg, dev):
     c16, g16, _ = out["bf16"]
     assert abs(c16 - c32) / abs(c32) < 1e-2
     assert (torch.linalg.vector_norm(g16 - g32) / torch.linalg.vector_norm(g32)).item() < 5e-2
+
+
+def _principal_angles_deg(A, B):
+    qa, _ = np.linalg.qr(A.T)
+    qb, _ = np.linalg.qr(B.T)
+    s = np.clip(np.linalg.svd(qa.T @ qb, compute_uv=False), -1.0, 1.0)
+    return np.degrees(np.arccos(s))
+
+
+def _fsc(a, b):
+    """Fourier shell correlation of two volumes (shells of the centered integer grid)."""
+    L = a.shape[-1]
+    fa, fb = np.fft.fftshift(np.fft.fftn(a)), np.fft.fftshift(np.fft.fftn(b))
+    k = np.arange(L) - L // 2
+    z, y, x = np.meshgrid(k, k, k, indexing="ij")
+    sh = np.rint(np.sqrt(x * x + y * y + z * z)).astype(int)
+    out = []
+    for i in range(L // 2):
+        m = sh == i
+        out.append(np.real(np.vdot(fa[m], fb[m])) / np.sqrt(np.vdot(fa[m], fa[m]).real * np.vdot(fb[m], fb[m]).real))
+    return np.array(out)
+
+
+def test_bf16_training_recovers_the_fp32_subspace(pkg, dev):
+    """Covariance SGD with the BF16 tensor-core Gram against the same run with the FP32 Gram
+    (whose gradient is pinned to the float64 oracle): principal angles between the learned
+    eigen-subspaces and the FSC of the leading eigenvolume."""
+    syn = pkg.synthetic
+    L, r, B, nb, steps = 16, 3, 128, 6, 120
+    g = torch.Generator(device=dev).manual_seed(11)
+    eig = syn.gaussian_blob_volumes(r, L, blobs=12, generator=g, device=dev)
+    eig = syn.orthonormalize(eig.reshape(r, -1)).reshape(r, L, L, L) * torch.tensor([3.0, 2.0, 1.0], device=dev).reshape(
+        r, 1, 1, 1) * L**1.5
+    plan = pkg.NufftPlan((L,) * 3, batch_size=r, device=dev)
+    batches = []
+    for _ in range(nb):
+        R = syn.uniform_rotations(B, generator=g, device=dev)
+        plan.setrot(R)
+        proj = pkg.vol_forward(eig, plan, None, fourier_domain=True)  # (B, r, L, L)
+        z = torch.randn((B, r, 1, 1), generator=g, device=dev)
+        img = (proj * z).sum(1).reshape(B, -1)
+        img = img + torch.randn(img.shape, generator=g, device=dev, dtype=torch.complex64) * 0.5 * img.abs().mean()
+        batches.append((R, img.contiguous()))
+    noise_var = float((0.5 * batches[0][1].abs().mean()) ** 2)
+    learned = {}
+    for prec in ("fp32", "bf16"):
+        torch.manual_seed(0)
+        covar = pkg.Covar(L, r).to(dev)
+        covar.vectors.grad = torch.zeros_like(covar.vectors)
+        covar.log_sqrt_eigenvals.grad = torch.zeros_like(covar.log_sqrt_eigenvals)
+        groups = covar.grad_lr_factor()
+        for gp in groups:
+            gp["lr"] *= 2e-3
+        opt = torch.optim.Adam(groups)
+        step = pkg.FusedCovarStep(L, r, "nufft", 2, device=dev, gram_precision=prec)
+        for k in range(steps):
+            R, img = batches[k % nb]
+            step.set_rotations(R)
+            step(covar.vectors.detach(), covar.log_sqrt_eigenvals.detach(), img, None, noise_var,
+                 grad_vectors=covar.vectors.grad, grad_log_sqrt=covar.log_sqrt_eigenvals.grad)
+            opt.step()
+        learned[prec] = covar.get_vectors_spatial_domain().detach().reshape(r, -1).double().cpu().numpy()
+    ang = _principal_angles_deg(learned["fp32"], learned["bf16"])
+    assert ang.max() < 5.0, ang
+    a, b = learned["fp32"][0].reshape((L,) * 3), learned["bf16"][0].reshape((L,) * 3)
+    if np.dot(a.ravel(), b.ravel()) < 0:
+        b = -b
+    assert _fsc(a, b)[: L // 4].min() > 0.95

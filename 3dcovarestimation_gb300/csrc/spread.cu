@@ -43,7 +43,8 @@ __device__ __forceinline__ float prologue(const PointGeom &g, int64_t id, const 
 
 constexpr int kLMin = -8;   // window corners relative to the bin lie in [kLMin, kLMin + 16)
 constexpr int kKeys = 256;  // sort key (l1 - kLMin) * 16 + (l0 - kLMin)
-constexpr int kMaxCPL = 3;  // channel pairs per lane per group
+constexpr int kMaxCPL = 3;      // channel pairs per lane per group (row tasks)
+constexpr int kRowPairCPL = 5;  // channel pairs per lane per group (row-pair tasks)
 
 // Per-point record staged once per block: packed window corner (bin-local, biased by 32 so
 // zero-padding corners below the bin stay non-negative) and the 3W kernel weights.
@@ -77,11 +78,13 @@ __host__ __device__ constexpr int spread_pairs(int cpl) { return SpreadLanes<W>:
 //     Warps take tasks from a shared counter, so the heavy middle rows spread over all warps.
 //  The block needs no shared-memory tile: its shared memory is the staged points only, and
 //  several blocks share an SM.
-template <int KT, int W, int CPL, bool COMP>
-__global__ void __launch_bounds__(kSpreadWarps * 32) spread_kernel(const SpreadParams a) {
+template <int KT, int W, int CPL, bool COMP, bool RP>
+__global__ void __launch_bounds__(kSpreadWarps * 32, RP ? 1 : 2) spread_kernel(const SpreadParams a) {
   constexpr int T = SpreadLanes<W>::T;
-  constexpr int G = SpreadLanes<W>::G;
-  constexpr int NP = G * CPL;  // channel pairs staged per group
+  constexpr int G = RP ? 1 : SpreadLanes<W>::G;  // lane groups over channel pairs
+  constexpr int NP = G * CPL;                     // channel pairs staged per group
+  constexpr int TP = (T + 1) / 2;                 // row pairs per plane (RP)
+  static_assert(!RP || 2 * T <= 32, "two rows of lanes per warp");
   constexpr int FL = PointRec<W>::FLOATS;
   extern __shared__ float4 smem4[];
   float4 *s_val = smem4;                                                         // max_sub * NP
@@ -202,8 +205,10 @@ __global__ void __launch_bounds__(kSpreadWarps * 32) spread_kernel(const SpreadP
   }
 
   const int lane = tid & 31;
+  // RP: lane = (row of the pair, column), every lane all NP pairs; else lane = (pair group, column)
   const int g = lane / T, c = lane - (lane / T) * T;
-  const bool lane_live = g < G;
+  const bool lane_live = RP ? g < 2 : g < G;
+  const int gv = (RP || !lane_live) ? 0 : g;  // idle lanes compute pair 0 and drop it
   const int npairs = (a.nch + 1) / 2;
   for (int p0 = 0; p0 < npairs; p0 += NP) {  // channel groups of NP pairs
     __syncthreads();
@@ -219,13 +224,17 @@ __global__ void __launch_bounds__(kSpreadWarps * 32) spread_kernel(const SpreadP
     if (tid == 0) *s_task = 0;
     __syncthreads();
 
-    // 2. row tasks
+    // 2. row tasks (RP: row-pair tasks)
+    constexpr int ntasks = RP ? T * TP : T * T;
     for (;;) {
       int task = 0;
       if (lane == 0) task = atomicAdd(s_task, 1);
       task = __shfl_sync(0xffffffffu, task, 0);
-      if (task >= T * T) break;
-      const int pa = task / T, r1 = task - (task / T) * T;
+      if (task >= ntasks) break;
+      const int pa = RP ? task / TP : task / T;
+      const int rb = RP ? (task - pa * TP) * 2 : task - pa * T;  // first row of the task
+      const int r1 = RP ? rb + g : rb;                            // this lane's row
+      const bool row_live = lane_live && r1 < T;
       const int b0lo = max(pa - W + 1 - kLMin, 0), b0hi = min(pa - kLMin, 15);
       float4 hi[CPL], lo[CPL];
 #pragma unroll
@@ -234,11 +243,14 @@ __global__ void __launch_bounds__(kSpreadWarps * 32) spread_kernel(const SpreadP
         lo[u] = make_float4(0.f, 0.f, 0.f, 0.f);
       }
       bool any = false;
-      for (int o1 = 0; o1 < W; ++o1) {  // window row o1 of the points with l1 = r1 - o1
-        const int b1 = r1 - o1 - kLMin;
+      const int lhi = RP ? rb + 1 : rb;
+      for (int l1 = lhi; l1 > rb - W; --l1) {  // points with window corner l1 cover row l1 + o1
+        const int b1 = l1 - kLMin;
         if (b1 < 0 || b1 > 15 || b0lo > b0hi) continue;
         const int ibeg = s_off[(b1 << 4) | b0lo], iend = s_off[((b1 << 4) | b0hi) + 1];
         if (ibeg >= iend) continue;
+        const int o1 = r1 - l1;
+        const bool in = row_live && o1 >= 0 && o1 < W;
         float4 part[CPL];
 #pragma unroll
         for (int u = 0; u < CPL; ++u) part[u] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -248,12 +260,12 @@ __global__ void __launch_bounds__(kSpreadWarps * 32) spread_kernel(const SpreadP
           const int packed = __float_as_int(rec[0]);
           const int o0 = pa - ((packed & 255) - 32);  // in [0, W) by the range
           const int jj = c - (((packed >> 16) & 255) - 32);
-          if (!lane_live || jj < 0 || jj >= W) continue;
+          if (!in || jj < 0 || jj >= W) continue;
           got = true;
           const float w = rec[1 + o0] * rec[1 + W + o1] * rec[1 + 2 * W + jj];
 #pragma unroll
           for (int u = 0; u < CPL; ++u) {
-            const float4 vv = s_val[i * NP + g + G * u];
+            const float4 vv = s_val[i * NP + gv + G * u];
             part[u].x = fmaf(w, vv.x, part[u].x);
             part[u].y = fmaf(w, vv.y, part[u].y);
             part[u].z = fmaf(w, vv.z, part[u].z);
@@ -283,13 +295,13 @@ __global__ void __launch_bounds__(kSpreadWarps * 32) spread_kernel(const SpreadP
         }
       }
       // 3. the finished cell goes to the global grid
-      if (!any) continue;
+      if (!any || !row_live) continue;
       const long long ro = s_rowoff[pa * T + r1];
       const int co = s_coloff[c];
       if (ro < 0 || co < 0) continue;
 #pragma unroll
       for (int u = 0; u < CPL; ++u) {
-        const int pp = p0 + g + G * u;
+        const int pp = p0 + gv + G * u;
         float4 x = hi[u];
         if (COMP) {
           x.x += lo[u].x;
@@ -305,10 +317,10 @@ __global__ void __launch_bounds__(kSpreadWarps * 32) spread_kernel(const SpreadP
   }
 }
 
-template <int KT, int W, int CPL, bool COMP>
+template <int KT, int W, int CPL, bool COMP, bool RP>
 int launch_one(const SpreadParams &a, int64_t max_blocks, cudaStream_t st) {
   constexpr int T = SpreadLanes<W>::T;
-  constexpr int NP = spread_pairs<W>(CPL);
+  constexpr int NP = (RP ? 1 : SpreadLanes<W>::G) * CPL;
   const size_t smem = (size_t)a.max_sub * (NP * sizeof(float4) + PointRec<W>::FLOATS * 4 + 3 * sizeof(int)) +
                       (size_t)T * T * sizeof(long long) + (2 * kKeys + 2 + T) * sizeof(int);
   if (smem > 227 * 1024) {
@@ -316,26 +328,28 @@ int launch_one(const SpreadParams &a, int64_t max_blocks, cudaStream_t st) {
     return COV3D_EINVAL;
   }
   if (smem > 32 * 1024) {  // static shared arrays come on top of the dynamic size
-    cudaError_t e = cudaFuncSetAttribute(spread_kernel<KT, W, CPL, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(spread_kernel<KT, W, CPL, COMP, RP>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return check_cuda(e, "cudaFuncSetAttribute(spread_kernel)");
   }
-  spread_kernel<KT, W, CPL, COMP><<<(unsigned)max_blocks, kSpreadWarps * 32, smem, st>>>(a);
+  spread_kernel<KT, W, CPL, COMP, RP><<<(unsigned)max_blocks, kSpreadWarps * 32, smem, st>>>(a);
   return launched("spread_kernel");
 }
 
-// One launch for all channels: the block sorts and stages its points once and spreads the
-// channels in groups of G * CPL pairs, CPL the smallest count that covers them (at most 3).
+// One launch for all channels: the block sorts and stages its points once.  With three or more
+// channel pairs, row-pair tasks with every lane holding kRowPairCPL pairs (groups of that many);
+// otherwise row tasks with the pairs spread over lane groups.
 template <int KT, int W, bool COMP>
 int launch_wc(SpreadParams a, int nchan, int64_t max_blocks, cudaStream_t st) {
   constexpr int G = SpreadLanes<W>::G;
   a.ch0 = 0;
   a.nch = nchan;
   const int npairs = (nchan + 1) / 2;
+  if (npairs >= 3 && 2 * SpreadLanes<W>::T <= 32) return launch_one<KT, W, kRowPairCPL, COMP, true>(a, max_blocks, st);
   const int cpl = (npairs + G - 1) / G;
-  if (cpl <= 1) return launch_one<KT, W, 1, COMP>(a, max_blocks, st);
-  if (cpl == 2) return launch_one<KT, W, 2, COMP>(a, max_blocks, st);
-  return launch_one<KT, W, kMaxCPL, COMP>(a, max_blocks, st);
+  if (cpl <= 1) return launch_one<KT, W, 1, COMP, false>(a, max_blocks, st);
+  if (cpl == 2) return launch_one<KT, W, 2, COMP, false>(a, max_blocks, st);
+  return launch_one<KT, W, kMaxCPL, COMP, false>(a, max_blocks, st);
 }
 
 template <int KT, int W>

@@ -222,6 +222,31 @@ class FusedCovarStep:
         return (host_cost.value if host_cost is not None else self.d_cost), gv, gl
 
 
+def compute_updated_fourier_reg(eigenvecs1, eigenvecs2, filter_gain, current_fourier_reg, L,
+                                optimize_in_fourier_domain, mask=None):
+    """Half-set Fourier regulariser from the covariance FSC of the two half-set estimates and
+    the dataset's shell-pair gain (reference ``covar_sgd.py:1155-1187``): returns
+    (regulariser (L, L, L), covariance FSC (S, S))."""
+    from .fsc_utils import covar_fsc, expand_fourier_shell
+
+    correction = 1 / filter_gain
+    correction[:, L // 2:] = correction[L // 2, L // 2]
+    correction[L // 2:, :] = correction[L // 2, L // 2]
+    if mask is not None:
+        mask = mask.clone().to(eigenvecs1.device)
+        eigenvecs1 = eigenvecs1 * mask
+        eigenvecs2 = eigenvecs2 * mask
+    fsc = covar_fsc(eigenvecs1, eigenvecs2)
+    eps = 1e-6
+    fsc = torch.clamp(fsc, eps, 1 - eps)
+    reg = 1 / ((fsc / (1 - fsc)) * correction)
+    reg[reg < 0] = 0
+    reg = expand_fourier_shell(reg.diag().sqrt().unsqueeze(0), L, 3)
+    if not optimize_in_fourier_domain:
+        reg = reg / L**2
+    return reg, fsc
+
+
 def gram_bf16(Q, y, plan=None):
     """Per-image gram (n, r, r), h (n, r), |y|^2 (n) of projections Q (n, r, P) and images y
     (n, P) with BF16 inputs and FP32 accumulation on the tensor cores (``cov3d_gram_bf16``).
@@ -263,6 +288,25 @@ class CovarTrainer:
         self.scheduler_patiece = 0
         self.fourier_reg = None
         self.training_log = {"epoch_ind": [], "lr_history": [], "cost_val": [], "epoch_run_time": []}
+
+    def compute_fourier_reg_term(self, eigenvecs: torch.Tensor) -> None:
+        """Fourier regulariser from an estimate of the eigenvectors: noise_var over their radial
+        PSD, upsampled to the fine grid (reference ``covar_sgd.py:420-430``)."""
+        from .fsc_utils import rpsd, upsample_and_expand_fourier_shell
+
+        us = self.covar.upsampling_factor
+        eigen_rpsd = rpsd(*eigenvecs) * (us**3)
+        self.fourier_reg = self.noise_var / upsample_and_expand_fourier_shell(eigen_rpsd, self.covar.resolution * us, 3)
+
+    def update_fourier_reg_halfsets(self, fourier_reg: torch.Tensor) -> None:
+        """Install a regulariser computed from the half-sets, resampled to the fine grid
+        (reference ``covar_sgd.py:432-447``; this trainer optimises in the Fourier domain)."""
+        from .fsc_utils import average_fourier_shell, upsample_and_expand_fourier_shell
+
+        fourier_reg = fourier_reg.to(self.device)
+        us = self.covar.upsampling_factor
+        radial = average_fourier_shell(fourier_reg) / (us**3)
+        self.fourier_reg = upsample_and_expand_fourier_shell(radial, self.covar.resolution * us, 3)
 
     def setup_training(self, lr: Optional[float] = None, momentum: float = 0.9, optim_type: str = "Adam",
                        reg: float = 1, nufft_disc: str = "nufft", orthogonal_projection: bool = False,

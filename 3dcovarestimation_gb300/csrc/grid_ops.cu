@@ -100,27 +100,32 @@ __global__ void unpack_grad_kernel(const float2 *__restrict__ fine, const float 
 // conjugate-Wirtinger derivative coef * fr * G to the fine-grid gradient, accumulates its value.
 __global__ void ml_reg_kernel(const float2 *__restrict__ grid, float2 *__restrict__ gg, const float *__restrict__ fr,
                               int nchan, int n, double coef, double *__restrict__ cost) {
+  // capped grid walking whole rows (no per-element division); the channel sum of one cell is
+  // FP32, the running sum over cells FP64, one FP64 atomic per block
   const int64_t n3 = (int64_t)n * n * n;
-  const int64_t cell = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int half = n / 2;
+  const float cfs = (float)coef;
   double part = 0.0;
-  if (cell < n3) {
-    const int half = n / 2;
-    int s2 = (int)(cell % n), s1 = (int)((cell / n) % n), s0 = (int)(cell / ((int64_t)n * n));
-    s0 += half;
-    s1 += half;
-    s2 += half;
-    s0 = s0 >= n ? s0 - n : s0;
-    s1 = s1 >= n ? s1 - n : s1;
-    s2 = s2 >= n ? s2 - n : s2;
-    const float w = __ldg(fr + ((int64_t)s0 * n + s1) * n + s2);
-    const float cf = (float)coef * w;
-    for (int c = 0; c < nchan; ++c) {
-      const float2 x = grid[c * n3 + cell];
-      float2 y = gg[c * n3 + cell];
-      y.x = fmaf(cf, x.x, y.x);
-      y.y = fmaf(cf, x.y, y.y);
-      gg[c * n3 + cell] = y;
-      part += (double)w * ((double)x.x * x.x + (double)x.y * x.y);
+  for (int64_t row = blockIdx.x; row < (int64_t)n * n; row += gridDim.x) {
+    int s0 = (int)(row / n), s1 = (int)(row - (int64_t)s0 * n);
+    s0 = s0 + half >= n ? s0 + half - n : s0 + half;
+    s1 = s1 + half >= n ? s1 + half - n : s1 + half;
+    const float *frow = fr + ((int64_t)s0 * n + s1) * n;
+    for (int s2 = threadIdx.x; s2 < n; s2 += blockDim.x) {
+      const int c2 = s2 + half >= n ? s2 + half - n : s2 + half;
+      const float w = __ldg(frow + c2);
+      const float cf = cfs * w;
+      const int64_t cell = row * n + s2;
+      float p32 = 0.0f;
+      for (int c = 0; c < nchan; ++c) {
+        const float2 x = grid[c * n3 + cell];
+        float2 y = gg[c * n3 + cell];
+        y.x = fmaf(cf, x.x, y.x);
+        y.y = fmaf(cf, x.y, y.y);
+        gg[c * n3 + cell] = y;
+        p32 = fmaf(x.x, x.x, fmaf(x.y, x.y, p32));
+      }
+      part += (double)(w * p32);
     }
   }
 #pragma unroll
@@ -176,8 +181,11 @@ int launch_unpack_grad(cov3d_plan *p, const void *fine, const float *vectors, co
 int launch_ml_reg(cov3d_plan *p, const void *grid, void *ggrid, const float *fr, int nchan, double coef,
                   double *cost_acc) {
   const int64_t n3 = (int64_t)p->n * p->n * p->n;
-  ml_reg_kernel<<<nblocks(n3), 256, 0, p->stream>>>(static_cast<const float2 *>(grid), static_cast<float2 *>(ggrid),
-                                                    fr, nchan, p->n, coef, cost_acc);
+  const int64_t rows = (int64_t)p->n * p->n;
+  const unsigned blocks = (unsigned)(rows < 1216 ? rows : 1216);
+  (void)n3;
+  ml_reg_kernel<<<blocks, 256, 0, p->stream>>>(static_cast<const float2 *>(grid), static_cast<float2 *>(ggrid), fr,
+                                               nchan, p->n, coef, cost_acc);
   return launched("ml_reg_kernel");
 }
 

@@ -303,3 +303,36 @@ def reconstruct_mean(dataset, init_vol: Optional[torch.Tensor] = None, mask: Opt
     if return_lhs_rhs:
         return vol, acc.rhs, acc.lhs
     return vol
+
+
+def regularize_mean_from_halfsets(mean_half1: torch.Tensor, rhs1: torch.Tensor, lhs1: torch.Tensor,
+                                  mean_half2: torch.Tensor, rhs2: torch.Tensor, lhs2: torch.Tensor,
+                                  mask: Optional[torch.Tensor] = None, do_grid_correction: Optional[bool] = True,
+                                  precond: Union[None, str, torch.Tensor] = None, rtol: float = 1e-6) -> torch.Tensor:
+    """Mean from the two half-set backprojections with the FSC-based shell regulariser
+    (reference ``mean.py:359-421``)."""
+    from .fsc_utils import average_fourier_shell, upsample_and_expand_fourier_shell, vol_fsc
+
+    L = mean_half1.shape[-1]
+    us = lhs1.shape[-1] // L
+    filter_gain = centered_fft3(centered_ifft3(lhs1 + lhs2, cropping_size=(L,) * 3)).abs() / 2
+    averaged_filter_gain = average_fourier_shell(1 / filter_gain)
+    fsc = torch.clamp(vol_fsc(mean_half1, mean_half2), 1e-3, 1 - 1e-3)
+    reg = 1 / ((fsc / (1 - fsc)) * averaged_filter_gain)
+    reg = upsample_and_expand_fourier_shell(reg.unsqueeze(0), rhs1.shape[-1], 3)
+    return solve_mean(rhs1 + rhs2, lhs1 + lhs2 + reg, L, us, mask=mask, do_grid_correction=do_grid_correction,
+                      rtol=rtol, precond=precond)
+
+
+def reconstruct_mean_from_halfsets(dataset, idx: Optional[torch.Tensor] = None, **reconstruction_kwargs):
+    """Means of the two halves of the dataset, then ``regularize_mean_from_halfsets``
+    (reference ``mean.py:262-291``; halves are the first and second half of ``idx``)."""
+    if idx is None:
+        idx = torch.arange(len(dataset))
+    kw = dict(reconstruction_kwargs)
+    kw["return_lhs_rhs"] = True
+    mask = kw.get("mask", None)
+    m1, rhs1, lhs1 = reconstruct_mean(dataset, idx=idx[: len(idx) // 2], **kw)
+    m2, rhs2, lhs2 = reconstruct_mean(dataset, idx=idx[len(idx) // 2:], **kw)
+    return regularize_mean_from_halfsets(m1, rhs1, lhs1, m2, rhs2, lhs2, mask=mask,
+                                         do_grid_correction=kw.get("do_grid_correction", True))

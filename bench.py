@@ -53,6 +53,7 @@ def parse():
     ap.add_argument("--mean-maxiter", type=int, default=20000)
     ap.add_argument("--no-mean", action="store_true", help="skip the mean-CG measurement")
     ap.add_argument("--no-bf16", action="store_true", help="skip the BF16-Gram variant of the step")
+    ap.add_argument("--no-wiener", action="store_true", help="skip the Wiener-coordinate measurement")
     return ap.parse_args()
 
 
@@ -419,6 +420,34 @@ def run_gb300(args):
                 "note": "Gram contractions in BF16 with FP32 accumulation (tcgen05); projections, spreading, "
                         "solve and update unchanged (FP32 / FP64)"}
 
+    # Wiener / latent-MAP coordinates of the resident images with the current eigenvolumes
+    # (wiener_coords.latentMAP's per-batch work: projections + FP32 Gram + FP64 Cholesky solve)
+    wiener = None
+    if not args.no_wiener:
+        wc = import_module("3dcovarestimation_gb300.wiener_coords")
+        eigv = covar.get_vectors_spatial_domain().detach()
+        lam = torch.exp(2 * covar.log_sqrt_eigenvals.detach()).to(torch.float64)
+        linv = torch.diag(1.0 / (lam + 1e-6))
+        wplan = pkg.NufftPlan((L,) * 3, batch_size=r, device=dev, width=args.width)
+
+        def wbatch(b):
+            wplan.setrot(rot[b])
+            q = pkg.vol_forward(eigv, wplan, ctf[b].reshape(B, L, L), fourier_domain=True)
+            return wc.compute_latentMAP_batch(images[b], q, noise_var, linv)[0]
+
+        wbatch(0)
+        barrier()
+        w0, w1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        w0.record(stream)
+        for b in range(nb):
+            wbatch(b)
+        w1.record(stream)
+        barrier()
+        wms = w0.elapsed_time(w1)
+        wiener = {"images_per_s": nb * B / (wms / 1e3), "images": nb * B, "batch": B,
+                  "note": "per batch: ES type-2 projections of the r eigenvolumes with CTF, FP32 Gram, FP64 "
+                          "Cholesky solve per image (Fourier-domain images)"}
+
     if rank != 0:
         if world > 1:
             import torch.distributed as dist
@@ -462,6 +491,8 @@ def run_gb300(args):
     }
     if bf16 is not None:
         line["bf16_gram"] = bf16
+    if wiener is not None:
+        line["wiener_coords"] = wiener
     if not args.no_mean:
         line["mean_cg"] = run_mean_cg(pkg, args, dev)
     if not args.no_cpu_baseline:

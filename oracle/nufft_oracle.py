@@ -671,3 +671,157 @@ def fine_diagonal_preconditioner(reg_lhs, L):
         return centered_ifft3(centered_fft3(r.reshape(L, L, L), pad_to=n) / reg_lhs, crop_to=L).reshape(-1)
 
     return M
+
+
+# ----------------------------------------------------------------------------- half-set regularisation
+
+
+def shell_average_batch(x):
+    """``average_fourier_shell`` over the last three axes of (..., L, L, L) (fsc_utils.py:116-135,
+    199-208): shape (..., S)."""
+    L = x.shape[-1]
+    idx, ns = shell_index(L, 3)
+    flat = x.reshape(x.shape[:-3] + (-1,))
+    out = np.zeros(x.shape[:-3] + (ns,), dtype=x.dtype)
+    for i in range(ns):
+        sel = (idx == i).reshape(-1)
+        out[..., i] = flat[..., sel].sum(-1) / sel.sum()
+    return out
+
+
+def shell_sizes(L):
+    idx, ns = shell_index(L, 3)
+    return np.array([(idx == i).sum() for i in range(ns)], np.float64)
+
+
+def expand_shells(shells, L):
+    """``expand_fourier_shell`` (fsc_utils.py:166-184, 223-234) of (..., S) to (..., L, L, L)."""
+    idx, ns = shell_index(L, 3)
+    shells = np.asarray(shells)
+    out = np.zeros(shells.shape[:-1] + (L, L, L), dtype=shells.dtype)
+    for i in range(min(ns, shells.shape[-1])):
+        out[..., idx == i] = shells[..., i:i + 1]
+    return out
+
+
+def upsample_expand_shells(shells, L):
+    """``upsample_and_expand_fourier_shell`` (fsc_utils.py:237-255): linear resampling of the
+    shell profile (align_corners=False) to the shell count of an L^3 grid, then expansion."""
+    from .unet_oracle import _lin_matrix
+
+    shells = np.atleast_2d(np.asarray(shells, np.float64))
+    ns = shell_index(L, 3)[1]
+    up = shells @ _lin_matrix(shells.shape[-1], ns).T
+    up = up[0] if up.shape[0] == 1 else up
+    return expand_shells(up, L)
+
+
+def rpsd_batch(signals):
+    """``rpsd`` (fsc_utils.py:137-147, 211-220): shell averages of |centered_fft3|^2."""
+    return shell_average_batch(np.abs(centered_fft3(np.asarray(signals))) ** 2)
+
+
+def vol_fsc(a, b):
+    """``vol_fsc`` (fsc_utils.py:272-291)."""
+    fa, fb = centered_fft3(a), centered_fft3(b)
+    c, p1, p2 = shell_average_batch(np.stack([np.real(fa * np.conj(fb)), np.abs(fa) ** 2, np.abs(fb) ** 2]))
+    return c / np.sqrt(p1 * p2)
+
+
+def covar_correlate(f1, f2):
+    """``covar_correlate`` (fsc_utils.py:312-340): sum_i s_i^T conj(s_i) with s_i the shell
+    averages of f1[i] * conj(f2) (r x S)."""
+    ns = shell_index(f1.shape[-1], 3)[1]
+    out = np.zeros((ns, ns), np.complex128)
+    for i in range(f1.shape[0]):
+        s = shell_average_batch(f1[i][None] * np.conj(f2))
+        out += s.T @ np.conj(s)
+    return out
+
+
+def covar_rpsd(e):
+    f = centered_fft3(np.asarray(e))
+    sz = shell_sizes(e.shape[-1])
+    return np.real(covar_correlate(f, f)) * np.outer(sz, sz)
+
+
+def covar_fsc(e1, e2):
+    """``covar_fsc`` (fsc_utils.py:343-367)."""
+    f1, f2 = centered_fft3(np.asarray(e1)), centered_fft3(np.asarray(e2))
+    c = np.real(covar_correlate(f1, f2))
+    r1, r2 = np.real(covar_correlate(f1, f1)), np.real(covar_correlate(f2, f2))
+    return c / np.sqrt(r1 * r2)
+
+
+def total_gain(pts, filters, L):
+    """``CovarDataset.get_total_gain`` (dataset.py:322-356): |sum im_backward(ctf, ctf)| / L with
+    the nearest plan at upsampling 1 (the magnitude per batch of 16 images, as the reference)."""
+    f = np.asarray(filters, np.float64)
+    out = np.zeros((L, L, L))
+    for lo in range(0, len(f), 16):
+        sl = slice(lo, lo + 16)
+        sig = im_backward_fourier_prologue(f[sl].astype(np.complex128), f[sl], L).reshape(len(f[sl]), -1)
+        out += np.abs(spread_discretized(sig, pts[sl], L, mode="nearest")[0] / L)
+    return out / L
+
+
+def total_covar_gain(pts, filters, L):
+    """``CovarDataset.get_total_covar_gain`` (dataset.py:358-421): sum over images of the outer
+    product of the shell averages of |per-image adjoint of ctf^2| / L^2."""
+    f = np.asarray(filters, np.float64).copy()
+    if L % 2 == 0:
+        f[:, 0, :] = 0
+        f[:, :, 0] = 0
+    g = np.abs(spread_discretized((f**2).reshape(len(f), -1).astype(np.complex128), pts, L, mode="nearest",
+                                  aggregate=False)[:, 0]) / L**2
+    s = shell_average_batch(g)
+    return s.T @ s
+
+
+def updated_fourier_reg(e1, e2, filter_gain, L, fourier_domain=True):
+    """``compute_updated_fourier_reg`` (covar_sgd.py:1155-1187) without a mask."""
+    with np.errstate(divide="ignore"):
+        corr = 1.0 / np.asarray(filter_gain, np.float64)
+    corr[:, L // 2:] = corr[L // 2, L // 2]
+    corr[L // 2:, :] = corr[L // 2, L // 2]
+    fsc = np.clip(covar_fsc(e1, e2), 1e-6, 1 - 1e-6)
+    reg = 1.0 / ((fsc / (1 - fsc)) * corr)
+    reg[reg < 0] = 0
+    out = expand_shells(np.sqrt(np.diag(reg))[None], L)[0]
+    return (out if fourier_domain else out / L**2), fsc
+
+
+def fourier_reg_term(e, upsample, L, noise_var):
+    """``CovarTrainer.compute_fourier_reg_term`` (covar_sgd.py:420-430)."""
+    rp = rpsd_batch(e) * upsample**3
+    return noise_var / upsample_expand_shells(rp, L * upsample)
+
+
+def fourier_reg_halfsets(reg, upsample, L):
+    """``CovarTrainer.update_fourier_reg_halfsets`` (covar_sgd.py:432-447), Fourier domain."""
+    radial = shell_average_batch(np.asarray(reg)) / upsample**3
+    return upsample_expand_shells(radial, L * upsample)
+
+
+def regularize_mean_from_halfsets(m1, rhs1, lhs1, m2, rhs2, lhs2, rtol=1e-6):
+    """``regularize_mean_from_halfsets`` (mean.py:359-421) without a mask.  Returns (volume,
+    iterations)."""
+    L = m1.shape[-1]
+    n = lhs1.shape[-1]
+    us = n // L
+    gain = np.abs(centered_fft3(centered_ifft3(lhs1 + lhs2, crop_to=L))) / 2
+    avg_gain = shell_average_batch(1.0 / gain)
+    fsc = np.clip(vol_fsc(m1, m2), 1e-3, 1 - 1e-3)
+    reg = 1.0 / ((fsc / (1 - fsc)) * avg_gain)
+    reg = upsample_expand_shells(reg[None], n)
+    reg_lhs = regularize_lhs(lhs1 + lhs2 + reg)
+    rhs = rhs1 + rhs2
+    vol = np.real(centered_ifft3(rhs / reg_lhs, crop_to=L))
+    it = -1
+    if us > 1:
+        b = centered_ifft3(rhs, crop_to=L).reshape(-1)
+        x, it, _ = conjugate_gradient(padding_operator(reg_lhs, L), b, x0=vol.reshape(-1).astype(np.complex128),
+                                      rtol=rtol)
+        vol = x.reshape((L,) * 3).real
+    vol = np.real(centered_ifft3(centered_fft3(vol) * sphere_mask(L)))
+    return vol / grid_correction_discretized(L, us, "nearest"), it

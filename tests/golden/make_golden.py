@@ -23,6 +23,13 @@ Cases (reference file:line of the function that produced each output):
 * ``cg_*.npz``           regularize_lhs + correct_upsampling_padding +
                          complex_conjugate_gradient (mean.py:43-142)
 * ``mean_*.npz``         reconstruct_mean (mean.py:145-259), whole pipeline
+* ``halfsets_*.npz``     fsc_utils (average_fourier_shell, rpsd, expand_fourier_shell,
+                         upsample_and_expand_fourier_shell, vol_fsc, covar_rpsd, covar_fsc;
+                         fsc_utils.py:116-367), CovarTrainer.compute_fourier_reg_term /
+                         update_fourier_reg_halfsets (covar_sgd.py:420-447),
+                         compute_updated_fourier_reg (covar_sgd.py:1155-1187),
+                         regularize_mean_from_halfsets (mean.py:359-421), CovarDataset
+                         get_total_gain / get_total_covar_gain (dataset.py:322-421)
 """
 
 import io
@@ -35,7 +42,7 @@ import numpy as np
 import torch
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"  # optional second argument: one case
 
 sys.path.insert(0, HERE)
 import ref_shim  # noqa: E402
@@ -255,7 +262,83 @@ def case_mean(L=10, us=2, N=96, seed=21):
          iters=np.array(handler.iters))
 
 
+class _GainDataset:
+    """Stand-in for CovarDataset with what get_total_gain / get_total_covar_gain read."""
+
+    def __init__(self, pts, filters, L):
+        self.pts_rot, self.filters, self.resolution, self.dtype = pts, filters, L, filters.dtype
+
+    def __len__(self):
+        return len(self.pts_rot)
+
+    def __getitem__(self, idx):
+        return None, self.pts_rot[idx], self.filters[idx].clone(), idx
+
+
+def case_halfsets(L=10, r=3, seed=31):
+    from types import SimpleNamespace
+
+    from cov3d import dataset, fsc_utils
+
+    rng = np.random.default_rng(seed)
+    n = 2 * L
+    e1 = rng.standard_normal((r, L, L, L))
+    e2 = e1 + 0.3 * rng.standard_normal((r, L, L, L))
+    v1 = rng.standard_normal((L, L, L))
+    v2 = v1 + 0.5 * rng.standard_normal((L, L, L))
+    spec = rng.uniform(0.5, 2.0, (L, L, L))
+    shells = rng.uniform(0.5, 2.0, 9)
+    t = torch.tensor
+    out = dict(L=L, r=r, e1=e1, e2=e2, v1=v1, v2=v2, spec=spec, shells=shells)
+    out["avg_shell"] = fsc_utils.average_fourier_shell(t(spec)).numpy()
+    out["rpsd"] = fsc_utils.rpsd(*t(e1)).numpy()
+    out["expand"] = fsc_utils.expand_fourier_shell(t(shells), L, 3).numpy()
+    out["upexpand"] = fsc_utils.upsample_and_expand_fourier_shell(t(shells), n, 3).numpy()
+    out["vol_fsc"] = fsc_utils.vol_fsc(t(v1), t(v2)).numpy()
+    out["covar_rpsd"] = fsc_utils.covar_rpsd(t(e1)).numpy()
+    out["covar_fsc"] = fsc_utils.covar_fsc(t(e1), t(e2)).numpy()
+    # dataset gains from 40 images with poses
+    N = 40
+    rotvecs = random_rotvecs(rng, N)
+    pts, _ = ref_points(rotvecs, np.zeros((N, 2), np.float32), L)
+    filters = rng.uniform(0.2, 1.5, (N, L, L))
+    ds = _GainDataset(pts, t(filters), L)
+    out["gain_filters"], out["gain_pts"] = filters, pts.numpy()
+    out["total_gain"] = dataset.CovarDataset.get_total_gain(ds, batch_size=16, device="cpu").numpy()
+    covar_gain = dataset.CovarDataset.get_total_covar_gain(ds, batch_size=16, device="cpu")
+    out["total_covar_gain"] = covar_gain.numpy()
+    reg, cfsc = covar_sgd.compute_updated_fourier_reg(t(e1), t(e2), covar_gain, None, L, True)
+    out["updated_reg"], out["updated_reg_fsc"] = reg.numpy(), cfsc.numpy()
+    reg_s, _ = covar_sgd.compute_updated_fourier_reg(t(e1), t(e2), covar_gain, None, L, False)
+    out["updated_reg_spatial"] = reg_s.numpy()
+    fake = SimpleNamespace(covar=SimpleNamespace(upsampling_factor=2, resolution=L), noise_var=0.7,
+                           device="cpu", optimize_in_fourier_domain=True)
+    covar_sgd.CovarTrainer.compute_fourier_reg_term(fake, t(e1))
+    out["fourier_reg_term"] = fake.fourier_reg.numpy()
+    covar_sgd.CovarTrainer.update_fourier_reg_halfsets(fake, reg)
+    out["fourier_reg_halfsets"] = fake.fourier_reg.numpy()
+    # mean from half-sets (half-set backprojections of the mean_L10 case)
+    g = np.load(os.path.join(HERE, "mean_L10.npz"))
+    lhs = g["lhs"]
+    rhs = g["rhs"]
+    lhs1, lhs2 = 0.45 * lhs, 0.55 * lhs + 0.02 * np.abs(lhs).mean()
+    rhs1, rhs2 = 0.5 * rhs, 0.5 * rhs + 0.05 * c32(rng, rhs.shape) * np.abs(rhs).mean()
+    m1 = rng.standard_normal((L, L, L))
+    m2 = m1 + 0.4 * rng.standard_normal((L, L, L))
+    handler = _CGCounter()
+    mean.logger.addHandler(handler)
+    mean.logger.setLevel(logging.DEBUG)
+    vol = mean.regularize_mean_from_halfsets(t(m1), t(rhs1), t(lhs1), t(m2), t(rhs2), t(lhs2))
+    mean.logger.removeHandler(handler)
+    out.update(m1=m1, m2=m2, lhs1=lhs1, lhs2=lhs2, rhs1=rhs1, rhs2=rhs2, mean_halfsets=vol.numpy(),
+               mean_halfsets_iters=np.array(handler.iters))
+    save(f"halfsets_L{L}.npz", **out)
+
+
 if __name__ == "__main__":
+    if len(sys.argv) > 2:
+        globals()[sys.argv[2]]()
+        sys.exit(0)
     case_poses()
     case_disc(10, 2, "bilinear", 5, 2, seed=1)
     case_disc(10, 2, "nearest", 5, 2, seed=2)
@@ -266,3 +349,4 @@ if __name__ == "__main__":
     case_latent()
     case_cg()
     case_mean()
+    case_halfsets()

@@ -178,3 +178,28 @@ def test_preconditioned_cg_reaches_the_same_solution():
         x, it, h = O.conjugate_gradient(A, b, x0=x0, rtol=1e-10, precond=M)
         assert rel(x, ref) < 1e-8
         assert h[-1] < 1e-10
+
+
+def test_halfset_regularisation_functions():
+    """fsc_utils, the Fourier regularisers, the dataset gains and regularize_mean_from_halfsets
+    against the reference run in float64 (the last to CG tolerance, like the mean pipeline)."""
+    g = load_golden("halfsets_L10.npz")
+    L = int(g["L"])
+    assert rel(O.shell_average_batch(g["spec"]), g["avg_shell"]) < 1e-12
+    assert rel(O.rpsd_batch(g["e1"]), g["rpsd"]) < 1e-12
+    assert rel(O.expand_shells(g["shells"], L), g["expand"]) < 1e-12
+    assert rel(O.upsample_expand_shells(g["shells"], 2 * L), g["upexpand"]) < 1e-12
+    assert rel(O.vol_fsc(g["v1"], g["v2"]), g["vol_fsc"]) < 1e-12
+    assert rel(O.covar_rpsd(g["e1"]), g["covar_rpsd"]) < 1e-12
+    assert rel(O.covar_fsc(g["e1"], g["e2"]), g["covar_fsc"]) < 1e-12
+    assert rel(O.total_gain(g["gain_pts"], g["gain_filters"], L), g["total_gain"]) < 1e-12
+    assert rel(O.total_covar_gain(g["gain_pts"], g["gain_filters"], L), g["total_covar_gain"]) < 1e-12
+    reg, fsc = O.updated_fourier_reg(g["e1"], g["e2"], g["total_covar_gain"], L, True)
+    assert rel(reg, g["updated_reg"]) < 1e-12 and rel(fsc, g["updated_reg_fsc"]) < 1e-12
+    assert rel(O.updated_fourier_reg(g["e1"], g["e2"], g["total_covar_gain"], L, False)[0],
+               g["updated_reg_spatial"]) < 1e-12
+    assert rel(O.fourier_reg_term(g["e1"], 2, L, 0.7), g["fourier_reg_term"]) < 1e-12
+    assert rel(O.fourier_reg_halfsets(g["updated_reg"], 2, L), g["fourier_reg_halfsets"]) < 1e-12
+    vol, it = O.regularize_mean_from_halfsets(g["m1"], g["rhs1"], g["lhs1"], g["m2"], g["rhs2"], g["lhs2"])
+    assert rel(vol, g["mean_halfsets"]) < 1e-5
+    assert abs(it - int(g["mean_halfsets_iters"][0])) <= 2

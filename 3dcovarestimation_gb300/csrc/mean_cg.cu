@@ -127,6 +127,28 @@ __global__ void pad_kernel(const float2 *__restrict__ x, int L, int n, float2 *_
   }
 }
 
+// pad_kernel restricted to the L support planes (the other planes of `fine` stay zero)
+__global__ void pad_support_kernel(const float2 *__restrict__ x, int L, int n, float2 *__restrict__ fine,
+                                   const CgState *st) {
+  if (stopped(st)) return;
+  const int h = L / 2;
+  for (int64_t row = blockIdx.x; row < (int64_t)L * n; row += gridDim.x) {
+    const int sp = (int)(row / n), s1 = (int)(row - (int64_t)sp * n);
+    const int s0 = sp < L - h ? sp : n - L + sp;
+    const int j0 = pad_voxel(s0, L, n), j1 = pad_voxel(s1, L, n);
+    float2 *dst = fine + ((int64_t)s0 * n + s1) * n;
+    if (j1 < 0) {
+      for (int s2 = threadIdx.x; s2 < n; s2 += blockDim.x) dst[s2] = make_float2(0.f, 0.f);
+      continue;
+    }
+    const float2 *src = x + ((int64_t)j0 * L + j1) * L;
+    for (int s2 = threadIdx.x; s2 < n; s2 += blockDim.x) {
+      const int j2 = pad_voxel(s2, L, n);
+      dst[s2] = j2 < 0 ? make_float2(0.f, 0.f) : src[j2];
+    }
+  }
+}
+
 // g[s] *= diag[centered(s)] * scale (divide instead when `divide`), g an m^3 FFT-native grid
 __global__ void fine_diag_kernel(float2 *__restrict__ g, const float *__restrict__ diag, int m, int divide, float scale,
                                  const CgState *st) {
@@ -422,6 +444,41 @@ static int get_fft_coarse(cov3d_plan *p, cufftHandle *out) {
   return check_cufft(cufftSetStream(it->second, p->stream), "cufftSetStream");
 }
 
+// Pruned transforms of the padding operator (even L): a batched 2D FFT over the L/2 support
+// planes of one half (keys -2) and a 1D FFT along axis 0 over all n^2 lines (key -3).
+static int get_fft_planes(cov3d_plan *p, cufftHandle *out) {
+  auto it = p->ffts->find(-2);
+  if (it == p->ffts->end()) {
+    cufftHandle h;
+    int dims[2] = {p->n, p->n};
+    COV3D_TRY(check_cufft(cufftPlanMany(&h, 2, dims, nullptr, 1, p->n * p->n, nullptr, 1, p->n * p->n, CUFFT_C2C,
+                                        p->L / 2),
+                          "cufftPlanMany(planes)"));
+    it = p->ffts->emplace(-2, h).first;
+  }
+  *out = it->second;
+  return check_cufft(cufftSetStream(it->second, p->stream), "cufftSetStream");
+}
+
+static int get_fft_axis0(cov3d_plan *p, cufftHandle *out) {
+  auto it = p->ffts->find(-3);
+  if (it == p->ffts->end()) {
+    cufftHandle h;
+    int dims[1] = {p->n};
+    const int nn = p->n * p->n;
+    COV3D_TRY(check_cufft(cufftPlanMany(&h, 1, dims, dims, nn, 1, dims, nn, 1, CUFFT_C2C, nn), "cufftPlanMany(axis0)"));
+    it = p->ffts->emplace(-3, h).first;
+  }
+  *out = it->second;
+  return check_cufft(cufftSetStream(it->second, p->stream), "cufftSetStream");
+}
+
+static int fft2(cufftHandle h, const float2 *in, float2 *out, int dir) {
+  return check_cufft(cufftExecC2C(h, reinterpret_cast<cufftComplex *>(const_cast<float2 *>(in)),
+                                  reinterpret_cast<cufftComplex *>(out), dir),
+                     "cufftExecC2C");
+}
+
 static int fft(cufftHandle h, float2 *g, int dir) {
   return check_cufft(cufftExecC2C(h, reinterpret_cast<cufftComplex *>(g), reinterpret_cast<cufftComplex *>(g), dir),
                      "cufftExecC2C");
@@ -526,34 +583,56 @@ int cg_solve(cov3d_plan *p, const float *d_lhs, const void *d_b, void *d_x, doub
   const float2 *b = static_cast<const float2 *>(d_b);
   float2 *x = static_cast<float2 *>(d_x);
   cudaStream_t s = p->stream;
-  cufftHandle h, hc = 0;
+  cufftHandle h, hc = 0, hp = 0, h0 = 0;
   COV3D_TRY(get_fft(p, 1, &h));
   if (precond == 2) COV3D_TRY(get_fft_coarse(p, &hc));
+  // even L: pruned transforms (the input has L nonzero planes, only L planes of the output are
+  // kept): 2D FFTs over the support planes and an out-of-place 1D FFT along axis 0 into `full`,
+  // whose other planes the 2D inverse never needs; `fine` keeps zeros off its support planes
+  const bool pruned = (L % 2 == 0) && n >= L + 2;
+  float2 *full = fine;
+  if (pruned) {
+    COV3D_TRY(grow(p->fine2, n3 * 8));
+    full = p->fine2.as<float2>();
+    COV3D_TRY(get_fft_planes(p, &hp));
+    COV3D_TRY(get_fft_axis0(p, &h0));
+    COV3D_CUDA(cudaMemsetAsync(fine, 0, (size_t)n3 * 8, s));
+  }
+  const int64_t half_off = (int64_t)(n - L / 2) * n * n;  // second block of support planes
   COV3D_CUDA(cudaMemsetAsync(st, 0, sizeof(CgState), s));
 
-  // out = A(in) (also <p, out> into st->pap when dotp is given)
-  auto apply_A = [&](const float2 *in, float2 *out, const float2 *dotp, const CgState *gate) -> int {
-    pad_kernel<<<capped((int64_t)n * n), 256, 0, s>>>(in, L, n, fine, gate);
-    COV3D_LAUNCHED("pad_kernel");
-    COV3D_TRY(fft(h, fine, CUFFT_FORWARD));
-    fine_diag_kernel<<<capped((int64_t)n * n), 256, 0, s>>>(fine, d_lhs, n, 0, 1.0f, gate);
-    COV3D_LAUNCHED("fine_diag_kernel");
-    COV3D_TRY(fft(h, fine, CUFFT_INVERSE));
-    crop_kernel<<<capped((int64_t)L * L), 256, 0, s>>>(fine, L, n, out, 0, dotp, dotp ? st : const_cast<CgState *>(gate));
-    return launched("crop_kernel");
-  };
-  // z = M(r)
-  auto apply_M = [&](const float2 *in, float2 *out, const CgState *gate) -> int {
-    if (precond == 1) {
+  // out = crop(ifft3(diag^(+-1) * fft3(pad(in)))), with <p, out> into st->pap when dotp is given
+  auto apply_op = [&](const float2 *in, float2 *out, int divide, const float2 *dotp, const CgState *gate) -> int {
+    if (pruned) {
+      pad_support_kernel<<<capped((int64_t)L * n), 256, 0, s>>>(in, L, n, fine, gate);
+      COV3D_LAUNCHED("pad_support_kernel");
+      COV3D_TRY(fft2(hp, fine, fine, CUFFT_FORWARD));
+      COV3D_TRY(fft2(hp, fine + half_off, fine + half_off, CUFFT_FORWARD));
+      COV3D_TRY(fft2(h0, fine, full, CUFFT_FORWARD));
+    } else {
       pad_kernel<<<capped((int64_t)n * n), 256, 0, s>>>(in, L, n, fine, gate);
       COV3D_LAUNCHED("pad_kernel");
       COV3D_TRY(fft(h, fine, CUFFT_FORWARD));
-      fine_diag_kernel<<<capped((int64_t)n * n), 256, 0, s>>>(fine, d_lhs, n, 1, 1.0f, gate);
-      COV3D_LAUNCHED("fine_diag_kernel");
-      COV3D_TRY(fft(h, fine, CUFFT_INVERSE));
-      crop_kernel<<<capped((int64_t)L * L), 256, 0, s>>>(fine, L, n, out, 0, nullptr, const_cast<CgState *>(gate));
-      return launched("crop_kernel");
     }
+    fine_diag_kernel<<<capped((int64_t)n * n), 256, 0, s>>>(full, d_lhs, n, divide, 1.0f, gate);
+    COV3D_LAUNCHED("fine_diag_kernel");
+    if (pruned) {
+      COV3D_TRY(fft2(h0, full, full, CUFFT_INVERSE));
+      COV3D_TRY(fft2(hp, full, full, CUFFT_INVERSE));
+      COV3D_TRY(fft2(hp, full + half_off, full + half_off, CUFFT_INVERSE));
+    } else {
+      COV3D_TRY(fft(h, fine, CUFFT_INVERSE));
+    }
+    crop_kernel<<<capped((int64_t)L * L), 256, 0, s>>>(full, L, n, out, 0, dotp,
+                                                        dotp ? st : const_cast<CgState *>(gate));
+    return launched("crop_kernel");
+  };
+  auto apply_A = [&](const float2 *in, float2 *out, const float2 *dotp, const CgState *gate) -> int {
+    return apply_op(in, out, 0, dotp, gate);
+  };
+  // z = M(r)
+  auto apply_M = [&](const float2 *in, float2 *out, const CgState *gate) -> int {
+    if (precond == 1) return apply_op(in, out, 1, nullptr, gate);
     copy_kernel<<<nb(L3), 256, 0, s>>>(in, out, L3);
     COV3D_LAUNCHED("copy_kernel");
     COV3D_TRY(fft(hc, out, CUFFT_FORWARD));

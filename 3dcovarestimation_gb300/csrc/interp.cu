@@ -162,7 +162,9 @@ __global__ void __launch_bounds__(kInterpWarps * 32) interp_kernel(const InterpP
     const int cell2 = l2 + j;
     const bool lane_ok = lane < LANES && cell2 >= 0;
     const float4 *base = tile4 + cell2 * CP + q;
-    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    // two packed FP32 accumulators (FFMA2: one instruction per channel pair of values; the
+    // same rounding as two fmaf)
+    float2 a01 = make_float2(0.f, 0.f), a23 = make_float2(0.f, 0.f);
 #pragma unroll
     for (int i0 = 0; i0 < W; ++i0) {
       const int r0 = l0 + i0;
@@ -174,15 +176,14 @@ __global__ void __launch_bounds__(kInterpWarps * 32) interp_kernel(const InterpP
         if (KT != COV3D_KERNEL_ES && r1 < 0) continue;
         if (lane_ok) {
           const float w = w0j * w1[i1];
+          const float2 ww = make_float2(w, w);
           const float4 v = base[(r0 * T + r1) * T * CP];
-          acc.x = fmaf(w, v.x, acc.x);
-          acc.y = fmaf(w, v.y, acc.y);
-          acc.z = fmaf(w, v.z, acc.z);
-          acc.w = fmaf(w, v.w, acc.w);
+          a01 = __ffma2_rn(ww, make_float2(v.x, v.y), a01);
+          a23 = __ffma2_rn(ww, make_float2(v.z, v.w), a23);
         }
       }
     }
-    wred[lane] = acc;
+    wred[lane] = make_float4(a01.x, a01.y, a23.x, a23.y);
     __syncwarp();
     if (lane < CP) {
       float4 s = wred[lane];

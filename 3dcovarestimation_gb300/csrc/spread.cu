@@ -251,9 +251,12 @@ __global__ void __launch_bounds__(kSpreadWarps * 32, RP ? 1 : 2) spread_kernel(c
         if (ibeg >= iend) continue;
         const int o1 = r1 - l1;
         const bool in = row_live && o1 >= 0 && o1 < W;
-        float4 part[CPL];
+        float2 part01[CPL], part23[CPL];  // packed FP32 (FFMA2), same rounding as fmaf
 #pragma unroll
-        for (int u = 0; u < CPL; ++u) part[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int u = 0; u < CPL; ++u) {
+          part01[u] = make_float2(0.f, 0.f);
+          part23[u] = make_float2(0.f, 0.f);
+        }
         bool got = false;
         for (int i = ibeg; i < iend; ++i) {
           const float *rec = s_rec + i * FL;
@@ -263,27 +266,27 @@ __global__ void __launch_bounds__(kSpreadWarps * 32, RP ? 1 : 2) spread_kernel(c
           if (!in || jj < 0 || jj >= W) continue;
           got = true;
           const float w = rec[1 + o0] * rec[1 + W + o1] * rec[1 + 2 * W + jj];
+          const float2 ww = make_float2(w, w);
 #pragma unroll
           for (int u = 0; u < CPL; ++u) {
             const float4 vv = s_val[i * NP + gv + G * u];
-            part[u].x = fmaf(w, vv.x, part[u].x);
-            part[u].y = fmaf(w, vv.y, part[u].y);
-            part[u].z = fmaf(w, vv.z, part[u].z);
-            part[u].w = fmaf(w, vv.w, part[u].w);
+            part01[u] = __ffma2_rn(ww, make_float2(vv.x, vv.y), part01[u]);
+            part23[u] = __ffma2_rn(ww, make_float2(vv.z, vv.w), part23[u]);
           }
         }
         if (!got) continue;
         any = true;
 #pragma unroll
         for (int u = 0; u < CPL; ++u) {
+          const float4 pu = make_float4(part01[u].x, part01[u].y, part23[u].x, part23[u].y);
           if (!COMP) {
-            hi[u].x += part[u].x;
-            hi[u].y += part[u].y;
-            hi[u].z += part[u].z;
-            hi[u].w += part[u].w;
+            hi[u].x += pu.x;
+            hi[u].y += pu.y;
+            hi[u].z += pu.z;
+            hi[u].w += pu.w;
           } else {
             float *xs = &hi[u].x, *es = &lo[u].x;
-            const float *d = &part[u].x;
+            const float *d = &pu.x;
 #pragma unroll
             for (int v = 0; v < 4; ++v) {  // TwoSum (Knuth): xs + d = s2 + rounding error, exactly
               const float s2 = xs[v] + d[v];

@@ -258,20 +258,30 @@ __global__ void __launch_bounds__(kSpreadWarps * 32, RP ? 1 : 2) spread_kernel(c
           part23[u] = make_float2(0.f, 0.f);
         }
         bool got = false;
-        for (int i = ibeg; i < iend; ++i) {
-          const float *rec = s_rec + i * FL;
-          const int packed = __float_as_int(rec[0]);
-          const int o0 = pa - ((packed & 255) - 32);  // in [0, W) by the range
-          const int jj = c - (((packed >> 16) & 255) - 32);
-          if (!in || jj < 0 || jj >= W) continue;
-          got = true;
-          const float w = rec[1 + o0] * rec[1 + W + o1] * rec[1 + 2 * W + jj];
-          const float2 ww = make_float2(w, w);
+        // two points per iteration, no per-lane branch: a lane whose column is outside a
+        // point's window (or whose row the range does not reach) multiplies by a zero weight
+        const int o1c = min(max(o1, 0), W - 1);
+        for (int i = ibeg; i < iend; i += 2) {
+          const int ib = i + 1 < iend ? i + 1 : i;
+          const float *ra = s_rec + i * FL, *rb = s_rec + ib * FL;
+          const int pa_ = __float_as_int(ra[0]), pb_ = __float_as_int(rb[0]);
+          const int o0a = pa - ((pa_ & 255) - 32), o0b = pa - ((pb_ & 255) - 32);  // in [0, W)
+          const int ja = c - (((pa_ >> 16) & 255) - 32), jb = c - (((pb_ >> 16) & 255) - 32);
+          const bool va = in && ja >= 0 && ja < W;
+          const bool vb = in && jb >= 0 && jb < W && ib != i;
+          const float wa = ra[1 + o0a] * ra[1 + W + o1c] * ra[1 + 2 * W + min(max(ja, 0), W - 1)];
+          const float wb = rb[1 + o0b] * rb[1 + W + o1c] * rb[1 + 2 * W + min(max(jb, 0), W - 1)];
+          const float2 wwa = make_float2(va ? wa : 0.f, va ? wa : 0.f);
+          const float2 wwb = make_float2(vb ? wb : 0.f, vb ? wb : 0.f);
+          got |= va | vb;
 #pragma unroll
           for (int u = 0; u < CPL; ++u) {
-            const float4 vv = s_val[i * NP + gv + G * u];
-            part01[u] = __ffma2_rn(ww, make_float2(vv.x, vv.y), part01[u]);
-            part23[u] = __ffma2_rn(ww, make_float2(vv.z, vv.w), part23[u]);
+            const float4 xa = s_val[i * NP + gv + G * u];
+            const float4 xb = s_val[ib * NP + gv + G * u];
+            part01[u] = __ffma2_rn(wwa, make_float2(xa.x, xa.y), part01[u]);
+            part23[u] = __ffma2_rn(wwa, make_float2(xa.z, xa.w), part23[u]);
+            part01[u] = __ffma2_rn(wwb, make_float2(xb.x, xb.y), part01[u]);
+            part23[u] = __ffma2_rn(wwb, make_float2(xb.z, xb.w), part23[u]);
           }
         }
         if (!got) continue;

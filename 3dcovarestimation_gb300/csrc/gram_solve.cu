@@ -117,6 +117,140 @@ __global__ void __launch_bounds__(1024) gram_kernel(const float2 *__restrict__ Q
   }
 }
 
+// (i, j) of product k of the upper triangle (0 <= i <= j < R1), row-major
+template <int R1>
+__host__ __device__ constexpr int tri_i(int k) {
+  int i = 0;
+  while (k >= R1 - i) {
+    k -= R1 - i;
+    ++i;
+  }
+  return i;
+}
+template <int R1>
+__host__ __device__ constexpr int tri_j(int k) {
+  int i = 0;
+  while (k >= R1 - i) {
+    k -= R1 - i;
+    ++i;
+  }
+  return i + k;
+}
+
+constexpr int kGramSubsets = 8;   // product subsets per image (2 warps each)
+constexpr int kGramLanes = 64;    // threads per subset, striding over the pixels
+constexpr int kGramRun = 32;      // pixels summed in plain FP32 before the Kahan update
+
+// part[KK] += conj(v[i]) * v[j] for product k = S + kGramSubsets * KK, indices fixed at
+// compile time so the pixel stays in registers
+template <int R1, int S, int KK, int PER>
+struct GramAcc {
+  __device__ __forceinline__ static void run(const float2 (&v)[R1], float2 (&part)[PER]) {
+    constexpr int k = S + kGramSubsets * KK;
+    if constexpr (k < R1 * (R1 + 1) / 2) {
+      constexpr int i = tri_i<R1>(k), j = tri_j<R1>(k);
+      const float2 a = v[i], c = v[j];
+      part[KK].x = fmaf(a.x, c.x, fmaf(a.y, c.y, part[KK].x));
+      part[KK].y = fmaf(a.x, c.y, fmaf(-a.y, c.x, part[KK].y));
+    }
+    if constexpr (KK + 1 < PER) GramAcc<R1, S, KK + 1, PER>::run(v, part);
+  }
+};
+
+// One run of pixels for the products k = S, S + kGramSubsets, ... of this subset:
+// part[kk] += conj(v[i]) * v[j] with v the pixel's r projections and y (registers)
+template <int R, int S, int PER>
+__device__ __forceinline__ void gram_run(const float2 *__restrict__ Qb, const float2 *__restrict__ Yb, int64_t q_ps,
+                                         int p0, int pend, int lane, float2 (&part)[PER]) {
+  constexpr int R1 = R + 1;
+  for (int p = p0 + lane; p < pend; p += kGramLanes) {
+    float2 v[R1];
+#pragma unroll
+    for (int i = 0; i < R; ++i) v[i] = Qb[(int64_t)p * q_ps + i];
+    v[R] = Yb[p];
+    GramAcc<R1, S, 0, PER>::run(v, part);
+  }
+}
+
+// Per-image Gram for the fused step's layout (point-major Q, channel stride 1): one block per
+// image, eight product subsets of two warps; each thread holds one pixel's r projections and y
+// in registers at a time.
+template <int R>
+__global__ void __launch_bounds__(kGramSubsets * kGramLanes, 1) gram_pixel_kernel(
+    const float2 *__restrict__ Q, int64_t q_is, int64_t q_ps, const float2 *__restrict__ Y, int P,
+    float2 *__restrict__ gram, float2 *__restrict__ h, float *__restrict__ yy) {
+  constexpr int R1 = R + 1, NPR = R1 * (R1 + 1) / 2, PER = (NPR + kGramSubsets - 1) / kGramSubsets;
+  const int b = blockIdx.x;
+  const int sub = threadIdx.x / kGramLanes, lane = threadIdx.x % kGramLanes;
+  float2 sum[PER], comp[PER];
+#pragma unroll
+  for (int kk = 0; kk < PER; ++kk) {
+    sum[kk] = make_float2(0.f, 0.f);
+    comp[kk] = make_float2(0.f, 0.f);
+  }
+  const float2 *Qb = Q + (int64_t)b * q_is;
+  const float2 *Yb = Y + (int64_t)b * P;
+  for (int p0 = 0; p0 < P; p0 += kGramLanes * kGramRun) {
+    float2 part[PER];
+#pragma unroll
+    for (int kk = 0; kk < PER; ++kk) part[kk] = make_float2(0.f, 0.f);
+    const int pend = min(P, p0 + kGramLanes * kGramRun);
+    switch (sub) {
+      case 0: gram_run<R, 0, PER>(Qb, Yb, q_ps, p0, pend, lane, part); break;
+      case 1: gram_run<R, 1, PER>(Qb, Yb, q_ps, p0, pend, lane, part); break;
+      case 2: gram_run<R, 2, PER>(Qb, Yb, q_ps, p0, pend, lane, part); break;
+      case 3: gram_run<R, 3, PER>(Qb, Yb, q_ps, p0, pend, lane, part); break;
+      case 4: gram_run<R, 4, PER>(Qb, Yb, q_ps, p0, pend, lane, part); break;
+      case 5: gram_run<R, 5, PER>(Qb, Yb, q_ps, p0, pend, lane, part); break;
+      case 6: gram_run<R, 6, PER>(Qb, Yb, q_ps, p0, pend, lane, part); break;
+      default: gram_run<R, 7, PER>(Qb, Yb, q_ps, p0, pend, lane, part); break;
+    }
+#pragma unroll
+    for (int kk = 0; kk < PER; ++kk) {  // Kahan update of the running totals
+      float yx = part[kk].x - comp[kk].x, tx = sum[kk].x + yx;
+      comp[kk].x = (tx - sum[kk].x) - yx;
+      sum[kk].x = tx;
+      float yv = part[kk].y - comp[kk].y, ty = sum[kk].y + yv;
+      comp[kk].y = (ty - sum[kk].y) - yv;
+      sum[kk].y = ty;
+    }
+  }
+  // reduce over the 64 lanes of the subset: shuffles within each warp, then the two warps
+  __shared__ float2 red[kGramSubsets][2][PER];
+  const int w = lane >> 5;
+#pragma unroll
+  for (int kk = 0; kk < PER; ++kk) {
+    float x = sum[kk].x, y = sum[kk].y;
+    for (int o = 16; o > 0; o >>= 1) {
+      x += __shfl_xor_sync(0xffffffffu, x, o);
+      y += __shfl_xor_sync(0xffffffffu, y, o);
+    }
+    if ((lane & 31) == 0) red[sub][w][kk] = make_float2(x, y);
+  }
+  __syncthreads();
+  if (lane < PER) {
+    const int kk = lane;
+    const int k = sub + kGramSubsets * kk;
+    if (k < NPR) {
+      const float2 t = make_float2(red[sub][0][kk].x + red[sub][1][kk].x, red[sub][0][kk].y + red[sub][1][kk].y);
+      int i = 0, kr = k;
+      while (kr >= R1 - i) {
+        kr -= R1 - i;
+        ++i;
+      }
+      const int j = i + kr;
+      if (j < R) {
+        gram[((int64_t)b * R + i) * R + j] = t;
+        if (i != j) gram[((int64_t)b * R + j) * R + i] = make_float2(t.x, -t.y);
+      } else if (i < R) {
+        h[(int64_t)b * R + i] = t;
+      } else {
+        yy[b] = t.x;
+      }
+    }
+  }
+}
+
 struct cd {
   double x, y;
 };
@@ -293,6 +427,39 @@ __global__ void __launch_bounds__(256) wpass_kernel(const float2 *Q, int64_t q_i
   }
 }
 
+// wpass for the fused step's layout (point-major, channel stride 1, W over Q in place): one
+// thread per pixel holds its r projections and y in registers (16-byte loads), C and u are
+// broadcast from shared memory, the r outputs are written back over the pixel's Q.
+template <int R>
+__global__ void __launch_bounds__(256) wpass_pixel_kernel(float2 *QW, int64_t q_is, int64_t q_ps,
+                                                          const float2 *__restrict__ Y, const float2 *__restrict__ C,
+                                                          const float2 *__restrict__ u, int P) {
+  __shared__ float2 sC[R * R], su[R];
+  const int b = blockIdx.y;
+  for (int e = threadIdx.x; e < R * R; e += blockDim.x) sC[e] = C[(int64_t)b * R * R + e];
+  for (int e = threadIdx.x; e < R; e += blockDim.x) su[e] = u[(int64_t)b * R + e];
+  __syncthreads();
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= P) return;
+  float2 *qp = QW + (int64_t)b * q_is + (int64_t)p * q_ps;
+  float2 q[R];
+#pragma unroll
+  for (int j = 0; j < R; ++j) q[j] = qp[j];
+  const float2 yv = Y[(int64_t)b * P + p];
+#pragma unroll
+  for (int i = 0; i < R; ++i) {
+    const float2 ui = su[i];
+    float2 acc = make_float2(ui.x * yv.x - ui.y * yv.y, ui.x * yv.y + ui.y * yv.x);
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+      const float2 c = sC[i * R + j];
+      acc.x = fmaf(c.x, q[j].x, fmaf(-c.y, q[j].y, acc.x));
+      acc.y = fmaf(c.x, q[j].y, fmaf(c.y, q[j].x, acc.y));
+    }
+    qp[i] = acc;  // every q[j] is already in registers
+  }
+}
+
 __global__ void finalize_kernel(const double *acc, int r, double inv_count, double *d_cost, float *glog) {
   const int i = threadIdx.x;
   if (i == 0 && d_cost) *d_cost = acc[0] * inv_count + acc[1];
@@ -307,6 +474,12 @@ int launch_gram(cudaStream_t st, int B, int P, int r, const void *q, int64_t is,
     set_error("rank %d out of range (1..%d)", r, kMaxRank);
     return COV3D_EINVAL;
   }
+  if (cs == 1 && ps == r && r == 10) {
+    gram_pixel_kernel<10><<<B, kGramSubsets * kGramLanes, 0, st>>>(
+        static_cast<const float2 *>(q), is, ps, static_cast<const float2 *>(images), P, static_cast<float2 *>(gram),
+        static_cast<float2 *>(h), yy);
+    return launched("gram_pixel_kernel");
+  }
   const int J = r * (r + 1) / 2 + r + 1;
   const int threads = J > 256 ? ((J + 31) / 32) * 32 : 256;
   const size_t smem = (size_t)kGramChunk * (r + 1) * sizeof(float2);
@@ -317,6 +490,18 @@ int launch_gram(cudaStream_t st, int B, int P, int r, const void *q, int64_t is,
 
 int launch_wpass(cudaStream_t st, int B, int P, int r, const void *q, int64_t is, int64_t ps, int64_t cs,
                  const void *images, const void *C, const void *u, void *w, int64_t wis, int64_t wps, int64_t wcs) {
+  if (q == w && is == wis && ps == wps && cs == 1 && wcs == 1 && ps == r && (r == 10 || r == 20)) {
+    dim3 g((P + 255) / 256, B);
+    float2 *qw = static_cast<float2 *>(w);
+    const float2 *y = static_cast<const float2 *>(images);
+    const float2 *cc = static_cast<const float2 *>(C), *uu = static_cast<const float2 *>(u);
+    if (r == 10) {
+      wpass_pixel_kernel<10><<<g, 256, 0, st>>>(qw, is, ps, y, cc, uu, P);
+    } else {
+      wpass_pixel_kernel<20><<<g, 256, 0, st>>>(qw, is, ps, y, cc, uu, P);
+    }
+    return launched("wpass_pixel_kernel");
+  }
   const size_t smem = (size_t)(r * r + r + kGramChunk * (r + 1)) * sizeof(float2);
   dim3 grid((P + kGramChunk - 1) / kGramChunk, B);
   wpass_kernel<<<grid, 256, smem, st>>>(static_cast<const float2 *>(q), is, ps, cs,

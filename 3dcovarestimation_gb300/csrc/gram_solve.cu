@@ -310,13 +310,16 @@ struct SolveArgs {
   int *bad;            // set to 1 if a factorisation failed
 };
 
+// RMAX sizes the per-thread working arrays (local memory): the smallest class that holds r keeps
+// them small enough to stay in L1
+template <int RMAX>
 __global__ void solve_kernel(const SolveArgs a) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= a.B) return;
   const int r = a.r;
-  cd m[kMaxRank * kMaxRank];
-  cd z[kMaxRank];
-  cd bb[kMaxRank];
+  cd m[RMAX * RMAX];
+  cd z[RMAX];
+  cd bb[RMAX];
   const float2 *G = a.gram + (int64_t)b * r * r;
   const float2 *hb = a.h + (int64_t)b * r;
   double cost = 0.0;
@@ -535,7 +538,14 @@ int launch_solve(cudaStream_t st, int B, int r, int objective, const void *gram,
   sa.z_out = static_cast<float2 *>(z);
   sa.m_out = static_cast<float2 *>(m);
   sa.bad = bad;
-  solve_kernel<<<(B + 63) / 64, 64, 0, st>>>(sa);
+  const unsigned blocks = (unsigned)((B + 31) / 32);
+  if (r <= 10) {
+    solve_kernel<10><<<blocks, 32, 0, st>>>(sa);
+  } else if (r <= 16) {
+    solve_kernel<16><<<blocks, 32, 0, st>>>(sa);
+  } else {
+    solve_kernel<kMaxRank><<<blocks, 32, 0, st>>>(sa);
+  }
   return launched("solve_kernel");
 }
 

@@ -71,28 +71,36 @@ __global__ void unpack_complex_kernel(const float2 *__restrict__ fine, const flo
 __global__ void unpack_grad_kernel(const float2 *__restrict__ fine, const float *__restrict__ vectors,
                                    const float *__restrict__ logs, const float *__restrict__ gc, int nchan, int L,
                                    int n, float *__restrict__ gvec, double *__restrict__ glog) {
+  // capped grid walking voxel rows; one FP64 atomic per block and channel for d/dlog_sqrt
   const int64_t L3 = (int64_t)L * L * L;
-  const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const bool live = v < L3;
-  int64_t cell = 0;
-  float g = 1.0f;
-  if (live) {
-    const int j2 = (int)(v % L), j1 = (int)((v / L) % L), j0 = (int)(v / ((int64_t)L * L));
-    cell = ((int64_t)voxel_to_storage(j0, L, n) * n + voxel_to_storage(j1, L, n)) * n + voxel_to_storage(j2, L, n);
-    if (gc) g = 1.0f / (__ldg(gc + j0) * __ldg(gc + j1) * __ldg(gc + j2));
-  }
+  const int64_t n3 = (int64_t)n * n * n;
   for (int c = 0; c < nchan; ++c) {
+    const float e = expf(__ldg(logs + c));
     double part = 0.0;
-    if (live) {
-      const float e = expf(__ldg(logs + c));
-      const float dV = 2.0f * fine[(int64_t)c * n * n * n + cell].x * g;
-      const float vec = __ldg(vectors + c * L3 + v);
-      gvec[c * L3 + v] = dV * e;
-      part = (double)dV * (double)(vec * e);
+    for (int64_t row = blockIdx.x; row < (int64_t)L * L; row += gridDim.x) {
+      const int j0 = (int)(row / L), j1 = (int)(row - (int64_t)j0 * L);
+      const float2 *src = fine + (int64_t)c * n3 + ((int64_t)voxel_to_storage(j0, L, n) * n + voxel_to_storage(j1, L, n)) * n;
+      const float g01 = gc ? 1.0f / (__ldg(gc + j0) * __ldg(gc + j1)) : 1.0f;
+      for (int j2 = threadIdx.x; j2 < L; j2 += blockDim.x) {
+        const float g = gc ? g01 / __ldg(gc + j2) : 1.0f;
+        const int64_t v = row * L + j2;
+        const float dV = 2.0f * src[voxel_to_storage(j2, L, n)].x * g;
+        const float vec = __ldg(vectors + c * L3 + v);
+        gvec[c * L3 + v] = dV * e;
+        part += (double)(dV * (vec * e));
+      }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
-    if ((threadIdx.x & 31) == 0 && part != 0.0) atomicAdd(glog + c, part);
+    __shared__ double wp[32];
+    if ((threadIdx.x & 31) == 0) wp[threadIdx.x >> 5] = part;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0.0;
+      for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t += wp[i];
+      if (t != 0.0) atomicAdd(glog + c, t);
+    }
+    __syncthreads();
   }
 }
 
@@ -172,7 +180,9 @@ int launch_unpack_complex(cov3d_plan *p, const void *fine, int nchan, int use_gc
 int launch_unpack_grad(cov3d_plan *p, const void *fine, const float *vectors, const float *log_scale, int use_gc,
                        int nchan, float *grad_vec, double *grad_log_acc) {
   const int64_t L3 = (int64_t)p->L * p->L * p->L;
-  unpack_grad_kernel<<<nblocks(L3), 256, 0, p->stream>>>(static_cast<const float2 *>(fine), vectors, log_scale,
+  const int64_t rows = (int64_t)p->L * p->L;
+  (void)L3;
+  unpack_grad_kernel<<<(unsigned)(rows < 1216 ? rows : 1216), 256, 0, p->stream>>>(static_cast<const float2 *>(fine), vectors, log_scale,
                                                          use_gc ? p->gc1d.as<float>() : nullptr, nchan, p->L, p->n,
                                                          grad_vec, grad_log_acc);
   return launched("unpack_grad_kernel");

@@ -159,6 +159,10 @@ class PhaseScope {
 PointGeom make_geom(const cov3d_plan *p);
 KernelSpec make_kernel(const cov3d_plan *p);
 int get_fft(cov3d_plan *p, int nchan, cufftHandle *out);
+int get_fft_planes(cov3d_plan *p, cufftHandle *out);
+int get_fft_axis0(cov3d_plan *p, cufftHandle *out);
+int fft2(cufftHandle h, const float2 *in, float2 *out, int dir);
+inline bool prunable(const cov3d_plan *p) { return p->L % 2 == 0 && p->n >= p->L + 2; }
 
 // points_sort.cu
 int sort_points(cov3d_plan *p);

@@ -594,17 +594,37 @@ int covar_cost_grad(cov3d_plan *p, const cov3d_cost_args *a, double *h_cost, dou
   COV3D_CUDA(cudaMemsetAsync(acc, 0, 64 * sizeof(double), p->stream));
   COV3D_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), p->stream));
 
-  // 1. pack the deapodised, scaled eigenvolumes into the fine grid; 2. forward FFT
+  // 1. pack the deapodised, scaled eigenvolumes into the fine grid; 2. forward FFT.  Even L:
+  // pruned transforms, staged in fine2 (zeroed before the spread anyway): 2D FFTs over each
+  // channel's L support planes, then the axis-0 FFT out of place into fine.
+  const bool pruned = prunable(p);
+  cufftHandle fft = 0, fplanes = 0, faxis0 = 0;
+  if (pruned) {
+    COV3D_TRY(grow(p->fine2, n3 * r * 8));
+    COV3D_TRY(get_fft_planes(p, &fplanes));
+    COV3D_TRY(get_fft_axis0(p, &faxis0));
+  } else {
+    COV3D_TRY(get_fft(p, r, &fft));
+  }
+  const int64_t half_off = (int64_t)(p->n - L / 2) * p->n * p->n;
   {
     PhaseScope ps(p, kPhasePack);
-    COV3D_TRY(launch_pack(p, a->d_vectors, nullptr, a->d_log_sqrt, a->use_grid_correction, r, p->fine.ptr));
+    COV3D_TRY(launch_pack(p, a->d_vectors, nullptr, a->d_log_sqrt, a->use_grid_correction, r,
+                          pruned ? p->fine2.ptr : p->fine.ptr));
   }
-  cufftHandle fft;
-  COV3D_TRY(get_fft(p, r, &fft));
   {
     PhaseScope ps(p, kPhaseFftFwd);
-    COV3D_TRY(check_cufft(cufftExecC2C(fft, p->fine.as<cufftComplex>(), p->fine.as<cufftComplex>(), CUFFT_FORWARD),
-                          "cufftExecC2C(forward)"));
+    if (pruned) {
+      for (int c = 0; c < r; ++c) {
+        float2 *src = p->fine2.as<float2>() + c * n3;
+        COV3D_TRY(fft2(fplanes, src, src, CUFFT_FORWARD));
+        COV3D_TRY(fft2(fplanes, src + half_off, src + half_off, CUFFT_FORWARD));
+        COV3D_TRY(fft2(faxis0, src, p->fine.as<float2>() + c * n3, CUFFT_FORWARD));
+      }
+    } else {
+      COV3D_TRY(check_cufft(cufftExecC2C(fft, p->fine.as<cufftComplex>(), p->fine.as<cufftComplex>(), CUFFT_FORWARD),
+                            "cufftExecC2C(forward)"));
+    }
   }
   // 3. interpolate at the central slices with the fused projection epilogue -> Q (B*P, r)
   const int shift = p->n - p->n / 2;
@@ -650,8 +670,17 @@ int covar_cost_grad(cov3d_plan *p, const cov3d_cost_args *a, double *h_cost, dou
   // 9. adjoint FFT, 10. crop + deapodise + chain rule to the Covar parameters
   {
     PhaseScope ps(p, kPhaseFftInv);
-    COV3D_TRY(check_cufft(cufftExecC2C(fft, p->fine2.as<cufftComplex>(), p->fine2.as<cufftComplex>(), CUFFT_INVERSE),
-                          "cufftExecC2C(inverse)"));
+    if (pruned) {  // axis 0 over all lines, then 2D only on the support planes the crop reads
+      for (int c = 0; c < r; ++c) {
+        float2 *g = p->fine2.as<float2>() + c * n3;
+        COV3D_TRY(fft2(faxis0, g, g, CUFFT_INVERSE));
+        COV3D_TRY(fft2(fplanes, g, g, CUFFT_INVERSE));
+        COV3D_TRY(fft2(fplanes, g + half_off, g + half_off, CUFFT_INVERSE));
+      }
+    } else {
+      COV3D_TRY(check_cufft(cufftExecC2C(fft, p->fine2.as<cufftComplex>(), p->fine2.as<cufftComplex>(), CUFFT_INVERSE),
+                            "cufftExecC2C(inverse)"));
+    }
   }
   {
     PhaseScope ps(p, kPhaseUnpack);

@@ -209,6 +209,43 @@ int launch_zero(cov3d_plan *p, void *ptr, int64_t bytes) {
   return check_cuda(cudaMemsetAsync(ptr, 0, (size_t)bytes, p->stream), "cudaMemsetAsync");
 }
 
+// Pruned transforms (even L): the zero-padded volume has L nonzero planes of n (the first and
+// last L/2 in FFT-native order) and only those planes of an inverse transform are cropped, so a
+// 3D transform is a batched 2D FFT over the L/2 support planes of each half (key -2) and a 1D FFT
+// along axis 0 over all n^2 lines (key -3).
+int get_fft_planes(cov3d_plan *p, cufftHandle *out) {
+  auto it = p->ffts->find(-2);
+  if (it == p->ffts->end()) {
+    cufftHandle h;
+    int dims[2] = {p->n, p->n};
+    COV3D_TRY(check_cufft(cufftPlanMany(&h, 2, dims, nullptr, 1, p->n * p->n, nullptr, 1, p->n * p->n, CUFFT_C2C,
+                                        p->L / 2),
+                          "cufftPlanMany(planes)"));
+    it = p->ffts->emplace(-2, h).first;
+  }
+  *out = it->second;
+  return check_cufft(cufftSetStream(it->second, p->stream), "cufftSetStream");
+}
+
+int get_fft_axis0(cov3d_plan *p, cufftHandle *out) {
+  auto it = p->ffts->find(-3);
+  if (it == p->ffts->end()) {
+    cufftHandle h;
+    int dims[1] = {p->n};
+    const int nn = p->n * p->n;
+    COV3D_TRY(check_cufft(cufftPlanMany(&h, 1, dims, dims, nn, 1, dims, nn, 1, CUFFT_C2C, nn), "cufftPlanMany(axis0)"));
+    it = p->ffts->emplace(-3, h).first;
+  }
+  *out = it->second;
+  return check_cufft(cufftSetStream(it->second, p->stream), "cufftSetStream");
+}
+
+int fft2(cufftHandle h, const float2 *in, float2 *out, int dir) {
+  return check_cufft(cufftExecC2C(h, reinterpret_cast<cufftComplex *>(const_cast<float2 *>(in)),
+                                  reinterpret_cast<cufftComplex *>(out), dir),
+                     "cufftExecC2C");
+}
+
 int get_fft(cov3d_plan *p, int nchan, cufftHandle *out) {
   auto it = p->ffts->find(nchan);
   if (it != p->ffts->end()) {

@@ -444,41 +444,6 @@ static int get_fft_coarse(cov3d_plan *p, cufftHandle *out) {
   return check_cufft(cufftSetStream(it->second, p->stream), "cufftSetStream");
 }
 
-// Pruned transforms of the padding operator (even L): a batched 2D FFT over the L/2 support
-// planes of one half (keys -2) and a 1D FFT along axis 0 over all n^2 lines (key -3).
-static int get_fft_planes(cov3d_plan *p, cufftHandle *out) {
-  auto it = p->ffts->find(-2);
-  if (it == p->ffts->end()) {
-    cufftHandle h;
-    int dims[2] = {p->n, p->n};
-    COV3D_TRY(check_cufft(cufftPlanMany(&h, 2, dims, nullptr, 1, p->n * p->n, nullptr, 1, p->n * p->n, CUFFT_C2C,
-                                        p->L / 2),
-                          "cufftPlanMany(planes)"));
-    it = p->ffts->emplace(-2, h).first;
-  }
-  *out = it->second;
-  return check_cufft(cufftSetStream(it->second, p->stream), "cufftSetStream");
-}
-
-static int get_fft_axis0(cov3d_plan *p, cufftHandle *out) {
-  auto it = p->ffts->find(-3);
-  if (it == p->ffts->end()) {
-    cufftHandle h;
-    int dims[1] = {p->n};
-    const int nn = p->n * p->n;
-    COV3D_TRY(check_cufft(cufftPlanMany(&h, 1, dims, dims, nn, 1, dims, nn, 1, CUFFT_C2C, nn), "cufftPlanMany(axis0)"));
-    it = p->ffts->emplace(-3, h).first;
-  }
-  *out = it->second;
-  return check_cufft(cufftSetStream(it->second, p->stream), "cufftSetStream");
-}
-
-static int fft2(cufftHandle h, const float2 *in, float2 *out, int dir) {
-  return check_cufft(cufftExecC2C(h, reinterpret_cast<cufftComplex *>(const_cast<float2 *>(in)),
-                                  reinterpret_cast<cufftComplex *>(out), dir),
-                     "cufftExecC2C");
-}
-
 static int fft(cufftHandle h, float2 *g, int dir) {
   return check_cufft(cufftExecC2C(h, reinterpret_cast<cufftComplex *>(g), reinterpret_cast<cufftComplex *>(g), dir),
                      "cufftExecC2C");

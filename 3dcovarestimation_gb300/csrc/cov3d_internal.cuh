@@ -194,7 +194,7 @@ int launch_unpack_complex(cov3d_plan *p, const void *fine, int nchan, int use_gc
 int launch_unpack_grad(cov3d_plan *p, const void *fine, const float *vectors, const float *log_scale, int use_gc,
                        int nchan, float *grad_vec, double *grad_log_acc);
 int launch_ml_reg(cov3d_plan *p, const void *grid, void *ggrid, const float *fr, int nchan, double coef,
-                  double *cost_acc);
+                  double *cost_acc, int init);
 int launch_gc_volume(const cov3d_plan *p, float *out);
 int launch_zero(cov3d_plan *p, void *ptr, int64_t bytes);
 

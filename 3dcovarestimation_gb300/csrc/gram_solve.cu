@@ -656,16 +656,18 @@ int covar_cost_grad(cov3d_plan *p, const cov3d_cost_args *a, double *h_cost, dou
     COV3D_TRY(launch_wpass(p->stream, B, P, r, p->q.ptr, (int64_t)P * r, r, 1, a->d_images, C, u, p->q.ptr,
                            (int64_t)P * r, r, 1));
   }
-  {
-    PhaseScope ps(p, kPhaseSpread);
-    COV3D_TRY(launch_zero(p, p->fine2.ptr, n3 * r * 8));
-    COV3D_TRY(launch_spread(p, p->q.ptr, r, 1, r, ep, p->fine2.ptr, 1, n3, shift));
-  }
-  // 8. regulariser on the fine grid
-  if (a->d_fourier_reg && a->reg_scale != 0.0) {
+  // 7'. the regulariser (value and gradient coef * fr * G) initialises the gradient grid, so the
+  // spread adds onto it and no zeroing pass is needed; without one, the grid is zeroed
+  const bool with_reg = a->d_fourier_reg && a->reg_scale != 0.0;
+  if (with_reg) {
     PhaseScope ps(p, kPhaseReg);
     COV3D_TRY(launch_ml_reg(p, p->fine.ptr, p->fine2.ptr, a->d_fourier_reg, r, a->reg_scale / (2.0 * a->noise_var),
-                            acc + 1));
+                            acc + 1, 1));
+  }
+  {
+    PhaseScope ps(p, kPhaseSpread);
+    if (!with_reg) COV3D_TRY(launch_zero(p, p->fine2.ptr, n3 * r * 8));
+    COV3D_TRY(launch_spread(p, p->q.ptr, r, 1, r, ep, p->fine2.ptr, 1, n3, shift));
   }
   // 9. adjoint FFT, 10. crop + deapodise + chain rule to the Covar parameters
   {

@@ -105,9 +105,10 @@ __global__ void unpack_grad_kernel(const float2 *__restrict__ fine, const float 
 }
 
 // ML Fourier regulariser reg_scale * sum |G|^2 fr / (2 s2) (covar_sgd.py:1373-1376): adds its
-// conjugate-Wirtinger derivative coef * fr * G to the fine-grid gradient, accumulates its value.
+// conjugate-Wirtinger derivative coef * fr * G to the fine-grid gradient (or, with `init`,
+// writes it there, so the grid needs no zeroing before the spread), accumulates its value.
 __global__ void ml_reg_kernel(const float2 *__restrict__ grid, float2 *__restrict__ gg, const float *__restrict__ fr,
-                              int nchan, int n, double coef, double *__restrict__ cost) {
+                              int nchan, int n, double coef, double *__restrict__ cost, int init) {
   // capped grid walking whole rows (no per-element division); the channel sum of one cell is
   // FP32, the running sum over cells FP64, one FP64 atomic per block
   const int64_t n3 = (int64_t)n * n * n;
@@ -127,7 +128,7 @@ __global__ void ml_reg_kernel(const float2 *__restrict__ grid, float2 *__restric
       float p32 = 0.0f;
       for (int c = 0; c < nchan; ++c) {
         const float2 x = grid[c * n3 + cell];
-        float2 y = gg[c * n3 + cell];
+        float2 y = init ? make_float2(0.f, 0.f) : gg[c * n3 + cell];
         y.x = fmaf(cf, x.x, y.x);
         y.y = fmaf(cf, x.y, y.y);
         gg[c * n3 + cell] = y;
@@ -189,13 +190,13 @@ int launch_unpack_grad(cov3d_plan *p, const void *fine, const float *vectors, co
 }
 
 int launch_ml_reg(cov3d_plan *p, const void *grid, void *ggrid, const float *fr, int nchan, double coef,
-                  double *cost_acc) {
+                  double *cost_acc, int init) {
   const int64_t n3 = (int64_t)p->n * p->n * p->n;
   const int64_t rows = (int64_t)p->n * p->n;
   const unsigned blocks = (unsigned)(rows < 1216 ? rows : 1216);
   (void)n3;
   ml_reg_kernel<<<blocks, 256, 0, p->stream>>>(static_cast<const float2 *>(grid), static_cast<float2 *>(ggrid), fr,
-                                               nchan, p->n, coef, cost_acc);
+                                               nchan, p->n, coef, cost_acc, init);
   return launched("ml_reg_kernel");
 }
 

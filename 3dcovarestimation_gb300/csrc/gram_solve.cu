@@ -313,9 +313,7 @@ struct SolveArgs {
 // RMAX sizes the per-thread working arrays (local memory): the smallest class that holds r keeps
 // them small enough to stay in L1
 template <int RMAX>
-__global__ void solve_kernel(const SolveArgs a) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= a.B) return;
+__device__ double solve_one(const SolveArgs &a, const int b) {
   const int r = a.r;
   cd m[RMAX * RMAX];
   cd z[RMAX];
@@ -338,7 +336,7 @@ __global__ void solve_kernel(const SolveArgs a) {
     const double logdet = chol_logdet(m, r);
     if (!(logdet == logdet)) {
       atomicExch(a.bad, 1);
-      return;
+      return 0.0;
     }
     for (int i = 0; i < r; ++i) z[i] = bb[i];
     chol_solve(m, r, z);
@@ -386,7 +384,25 @@ __global__ void solve_kernel(const SolveArgs a) {
   }
   cost *= a.cscale;
   if (a.cost_b) a.cost_b[b] = cost;
-  if (a.cost_sum) atomicAdd(a.cost_sum, cost);
+  return cost;
+}
+
+// one thread per image; the images' costs are summed per block (one FP64 atomic per block
+// instead of one per image on the same address)
+template <int RMAX>
+__global__ void solve_kernel(const SolveArgs a) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  double cost = b < a.B ? solve_one<RMAX>(a, b) : 0.0;
+  if (!a.cost_sum) return;
+  for (int o = 16; o > 0; o >>= 1) cost += __shfl_xor_sync(0xffffffffu, cost, o);
+  __shared__ double wsum[32];
+  if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = cost;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int i = 0; i < (int)((blockDim.x + 31) >> 5); ++i) t += wsum[i];
+    atomicAdd(a.cost_sum, t);
+  }
 }
 
 // W = C Q + u y on chunks of pixels of one image (Q element (p, i) at

@@ -163,24 +163,30 @@ __global__ void __launch_bounds__(kInterpWarps * 32) interp_kernel(const InterpP
     const bool lane_ok = lane < LANES && cell2 >= 0;
     const float4 *base = tile4 + cell2 * CP + q;
     // two packed FP32 accumulators (FFMA2: one instruction per channel pair of values; the
-    // same rounding as two fmaf)
+    // same rounding as two fmaf); each window plane is summed over its rows with the axis-1
+    // weights first, then added with its axis-0 weight times this lane's axis-2 weight
     float2 a01 = make_float2(0.f, 0.f), a23 = make_float2(0.f, 0.f);
+    if (lane_ok) {
+      float2 ww1[W];
 #pragma unroll
-    for (int i0 = 0; i0 < W; ++i0) {
-      const int r0 = l0 + i0;
-      if (KT != COV3D_KERNEL_ES && r0 < 0) continue;
-      const float w0j = w0[i0] * wj;
+      for (int i1 = 0; i1 < W; ++i1) ww1[i1] = make_float2(w1[i1], w1[i1]);
 #pragma unroll
-      for (int i1 = 0; i1 < W; ++i1) {
-        const int r1 = l1 + i1;
-        if (KT != COV3D_KERNEL_ES && r1 < 0) continue;
-        if (lane_ok) {
-          const float w = w0j * w1[i1];
-          const float2 ww = make_float2(w, w);
+      for (int i0 = 0; i0 < W; ++i0) {
+        const int r0 = l0 + i0;
+        if (KT != COV3D_KERNEL_ES && r0 < 0) continue;
+        float2 p01 = make_float2(0.f, 0.f), p23 = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int i1 = 0; i1 < W; ++i1) {
+          const int r1 = l1 + i1;
+          if (KT != COV3D_KERNEL_ES && r1 < 0) continue;
           const float4 v = base[(r0 * T + r1) * T * CP];
-          a01 = __ffma2_rn(ww, make_float2(v.x, v.y), a01);
-          a23 = __ffma2_rn(ww, make_float2(v.z, v.w), a23);
+          p01 = __ffma2_rn(ww1[i1], make_float2(v.x, v.y), p01);
+          p23 = __ffma2_rn(ww1[i1], make_float2(v.z, v.w), p23);
         }
+        const float w0j = w0[i0] * wj;
+        const float2 ww0 = make_float2(w0j, w0j);
+        a01 = __ffma2_rn(ww0, p01, a01);
+        a23 = __ffma2_rn(ww0, p23, a23);
       }
     }
     wred[lane] = make_float4(a01.x, a01.y, a23.x, a23.y);

@@ -53,6 +53,19 @@ struct PointRec {
   static constexpr int FLOATS = (1 + 3 * W + 3) / 4 * 4;
 };
 
+// TwoSum (Knuth) on both lanes of a float2: s + d = s' + e exactly, e added to the error sum
+// err.  Differences are fused multiply-adds with -1, which round exactly like a subtraction.
+__device__ __forceinline__ void two_sum2(float2 &s, float2 &err, const float2 d) {
+  const float2 m1 = make_float2(-1.0f, -1.0f);
+  const float2 s2 = __fadd2_rn(s, d);
+  const float2 bb = __ffma2_rn(s, m1, s2);   // s2 - s
+  const float2 sb = __ffma2_rn(bb, m1, s2);  // s2 - bb
+  const float2 e1 = __ffma2_rn(sb, m1, s);   // s - (s2 - bb)
+  const float2 e2 = __ffma2_rn(bb, m1, d);   // d - bb
+  err = __fadd2_rn(err, __fadd2_rn(e1, e2));
+  s = s2;
+}
+
 // Lane layout of the row tasks: lane = g * T + c owns tile column c (T = 8 + W - 1 columns)
 // and the channel pairs g, g + G, ..., G = 32 / T lane groups.
 template <int W>
@@ -236,11 +249,11 @@ __global__ void __launch_bounds__(kSpreadWarps * 32, RP ? 1 : 2) spread_kernel(c
       const int r1 = RP ? rb + g : rb;                            // this lane's row
       const bool row_live = lane_live && r1 < T;
       const int b0lo = max(pa - W + 1 - kLMin, 0), b0hi = min(pa - kLMin, 15);
-      float4 hi[CPL], lo[CPL];
+      // cell sums of channel pairs (0, 1) and (2, 3) of each pair group, and their TwoSum errors
+      float2 hi01[CPL], hi23[CPL], lo01[CPL], lo23[CPL];
 #pragma unroll
       for (int u = 0; u < CPL; ++u) {
-        hi[u] = make_float4(0.f, 0.f, 0.f, 0.f);
-        lo[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+        hi01[u] = hi23[u] = lo01[u] = lo23[u] = make_float2(0.f, 0.f);
       }
       bool any = false;
       const int lhi = RP ? rb + 1 : rb;
@@ -288,22 +301,12 @@ __global__ void __launch_bounds__(kSpreadWarps * 32, RP ? 1 : 2) spread_kernel(c
         any = true;
 #pragma unroll
         for (int u = 0; u < CPL; ++u) {
-          const float4 pu = make_float4(part01[u].x, part01[u].y, part23[u].x, part23[u].y);
           if (!COMP) {
-            hi[u].x += pu.x;
-            hi[u].y += pu.y;
-            hi[u].z += pu.z;
-            hi[u].w += pu.w;
+            hi01[u] = __fadd2_rn(hi01[u], part01[u]);
+            hi23[u] = __fadd2_rn(hi23[u], part23[u]);
           } else {
-            float *xs = &hi[u].x, *es = &lo[u].x;
-            const float *d = &pu.x;
-#pragma unroll
-            for (int v = 0; v < 4; ++v) {  // TwoSum (Knuth): xs + d = s2 + rounding error, exactly
-              const float s2 = xs[v] + d[v];
-              const float bb = s2 - xs[v];
-              es[v] += (xs[v] - (s2 - bb)) + (d[v] - bb);
-              xs[v] = s2;
-            }
+            two_sum2(hi01[u], lo01[u], part01[u]);
+            two_sum2(hi23[u], lo23[u], part23[u]);
           }
         }
       }
@@ -315,16 +318,11 @@ __global__ void __launch_bounds__(kSpreadWarps * 32, RP ? 1 : 2) spread_kernel(c
 #pragma unroll
       for (int u = 0; u < CPL; ++u) {
         const int pp = p0 + gv + G * u;
-        float4 x = hi[u];
-        if (COMP) {
-          x.x += lo[u].x;
-          x.y += lo[u].y;
-          x.z += lo[u].z;
-          x.w += lo[u].w;
-        }
+        const float2 x01 = COMP ? __fadd2_rn(hi01[u], lo01[u]) : hi01[u];
+        const float2 x23 = COMP ? __fadd2_rn(hi23[u], lo23[u]) : hi23[u];
         float2 *dst = a.grid + (ro + co) * a.cs + (int64_t)(a.ch0 + 2 * pp) * a.chs;
-        if (2 * pp < a.nch && (x.x != 0.0f || x.y != 0.0f)) atomicAdd(dst, make_float2(x.x, x.y));
-        if (2 * pp + 1 < a.nch && (x.z != 0.0f || x.w != 0.0f)) atomicAdd(dst + a.chs, make_float2(x.z, x.w));
+        if (2 * pp < a.nch && (x01.x != 0.0f || x01.y != 0.0f)) atomicAdd(dst, x01);
+        if (2 * pp + 1 < a.nch && (x23.x != 0.0f || x23.y != 0.0f)) atomicAdd(dst + a.chs, x23);
       }
     }
   }

@@ -46,11 +46,17 @@ constexpr int kKeys = 256;  // sort key (l1 - kLMin) * 16 + (l0 - kLMin)
 constexpr int kMaxCPL = 3;      // channel pairs per lane per group (row tasks)
 constexpr int kRowPairCPL = 5;  // channel pairs per lane per group (row-pair tasks)
 
-// Per-point record staged once per block: packed window corner (bin-local, biased by 32 so
-// zero-padding corners below the bin stay non-negative) and the 3W kernel weights.
+// Per-point record staged once per block, in float2 units (each weight twice, the operand of a
+// packed multiply): the axis-0 weights by tile plane and the axis-2 weights by tile column, zero
+// outside the point's window, and the W axis-1 weights followed by a zero.  A lane's weight is
+// then rec[plane] * rec[W1 + o1] * rec[W2 + column], with no corner arithmetic and no select:
+// lanes outside the window read zeros.
 template <int W>
 struct PointRec {
-  static constexpr int FLOATS = (1 + 3 * W + 3) / 4 * 4;
+  static constexpr int T = kBin + W - 1;
+  static constexpr int W1 = T;              // axis-1 weights, then the zero slot W1 + W
+  static constexpr int W2 = T + W + 1;      // axis-2 weights by column
+  static constexpr int F2 = (2 * T + W + 2) / 2 * 2;  // float2 per record (even)
 };
 
 // TwoSum (Knuth) on both lanes of a float2: s + d = s' + e exactly, e added to the error sum
@@ -98,12 +104,13 @@ __global__ void __launch_bounds__(kSpreadWarps * 32, RP ? 1 : 2) spread_kernel(c
   constexpr int NP = G * CPL;                     // channel pairs staged per group
   constexpr int TP = (T + 1) / 2;                 // row pairs per plane (RP)
   static_assert(!RP || 2 * T <= 32, "two rows of lanes per warp");
-  constexpr int FL = PointRec<W>::FLOATS;
+  using Rec = PointRec<W>;
+  constexpr int F2 = Rec::F2;
   extern __shared__ float4 smem4[];
   float4 *s_val = smem4;                                                         // max_sub * NP
   long long *s_rowoff = reinterpret_cast<long long *>(s_val + a.max_sub * NP);  // T * T
-  float *s_rec = reinterpret_cast<float *>(s_rowoff + T * T);                  // max_sub * FL
-  int *s_key = reinterpret_cast<int *>(s_rec + a.max_sub * FL);                // max_sub
+  float2 *s_rec = reinterpret_cast<float2 *>(s_rowoff + T * T);                // max_sub * F2
+  int *s_key = reinterpret_cast<int *>(s_rec + a.max_sub * F2);                // max_sub
   int *s_pid = s_key + a.max_sub;                                              // max_sub
   float *s_sc = reinterpret_cast<float *>(s_pid + a.max_sub);                  // max_sub
   int *s_cnt = reinterpret_cast<int *>(s_sc + a.max_sub);                      // kKeys
@@ -173,14 +180,21 @@ __global__ void __launch_bounds__(kSpreadWarps * 32, RP ? 1 : 2) spread_kernel(c
       c1 = wrap1(c1, n);
       c2 = wrap1(c2, n);
     }
-    float *rec = s_rec + slot * FL;
-    rec[0] = __int_as_float((c0 - ts0 + 32) | ((c1 - ts1 + 32) << 8) | ((c2 - ts2 + 32) << 16));
+    (void)c1;
+    float2 *rec = s_rec + slot * F2;
+    const int l0 = c0 - ts0, l2 = c2 - ts2;  // bin-local corners, >= 1 - W (zero padding below)
+#pragma unroll
+    for (int e = 0; e < T; ++e) {
+      rec[e] = make_float2(0.f, 0.f);
+      rec[Rec::W2 + e] = make_float2(0.f, 0.f);
+    }
 #pragma unroll
     for (int r = 0; r < W; ++r) {
-      rec[1 + r] = w0[r];
-      rec[1 + W + r] = w1[r];
-      rec[1 + 2 * W + r] = w2[r];
+      if (l0 + r >= 0 && l0 + r < T) rec[l0 + r] = make_float2(w0[r], w0[r]);
+      if (l2 + r >= 0 && l2 + r < T) rec[Rec::W2 + l2 + r] = make_float2(w2[r], w2[r]);
+      rec[Rec::W1 + r] = make_float2(w1[r], w1[r]);
     }
+    rec[Rec::W1 + W] = make_float2(0.f, 0.f);
     const int id = sp_id(sp.idf);
     float sc = (a.nyquist && sp_nyquist(sp.idf)) ? 0.0f : a.scale;
     if (a.ctf) sc *= __ldg(a.ctf + id);
@@ -257,6 +271,7 @@ __global__ void __launch_bounds__(kSpreadWarps * 32, RP ? 1 : 2) spread_kernel(c
       }
       bool any = false;
       const int lhi = RP ? rb + 1 : rb;
+      const float2 *w2c = s_rec + Rec::W2 + c;  // this lane's column weight, record 0
       for (int l1 = lhi; l1 > rb - W; --l1) {  // points with window corner l1 cover row l1 + o1
         const int b1 = l1 - kLMin;
         if (b1 < 0 || b1 > 15 || b0lo > b0hi) continue;
@@ -264,40 +279,41 @@ __global__ void __launch_bounds__(kSpreadWarps * 32, RP ? 1 : 2) spread_kernel(c
         if (ibeg >= iend) continue;
         const int o1 = r1 - l1;
         const bool in = row_live && o1 >= 0 && o1 < W;
+        const int k1 = Rec::W1 + (in ? o1 : W);  // the zero slot for rows the range misses
         float2 part01[CPL], part23[CPL];  // packed FP32 (FFMA2), same rounding as fmaf
 #pragma unroll
         for (int u = 0; u < CPL; ++u) {
           part01[u] = make_float2(0.f, 0.f);
           part23[u] = make_float2(0.f, 0.f);
         }
-        bool got = false;
-        // two points per iteration, no per-lane branch: a lane whose column is outside a
-        // point's window (or whose row the range does not reach) multiplies by a zero weight
-        const int o1c = min(max(o1, 0), W - 1);
-        for (int i = ibeg; i < iend; i += 2) {
-          const int ib = i + 1 < iend ? i + 1 : i;
-          const float *ra = s_rec + i * FL, *rb = s_rec + ib * FL;
-          const int pa_ = __float_as_int(ra[0]), pb_ = __float_as_int(rb[0]);
-          const int o0a = pa - ((pa_ & 255) - 32), o0b = pa - ((pb_ & 255) - 32);  // in [0, W)
-          const int ja = c - (((pa_ >> 16) & 255) - 32), jb = c - (((pb_ >> 16) & 255) - 32);
-          const bool va = in && ja >= 0 && ja < W;
-          const bool vb = in && jb >= 0 && jb < W && ib != i;
-          const float wa = ra[1 + o0a] * ra[1 + W + o1c] * ra[1 + 2 * W + min(max(ja, 0), W - 1)];
-          const float wb = rb[1 + o0b] * rb[1 + W + o1c] * rb[1 + 2 * W + min(max(jb, 0), W - 1)];
-          const float2 wwa = make_float2(va ? wa : 0.f, va ? wa : 0.f);
-          const float2 wwb = make_float2(vb ? wb : 0.f, vb ? wb : 0.f);
-          got |= va | vb;
+        // two points per iteration; a lane whose column or row is outside a point's window
+        // multiplies by a zero weight
+        int i = ibeg;
+        for (; i + 1 < iend; i += 2) {
+          const float2 *ra = s_rec + i * F2, *rb2 = ra + F2;
+          const float2 wa = __fmul2_rn(__fmul2_rn(ra[pa], ra[k1]), w2c[i * F2]);
+          const float2 wb = __fmul2_rn(__fmul2_rn(rb2[pa], rb2[k1]), w2c[(i + 1) * F2]);
 #pragma unroll
           for (int u = 0; u < CPL; ++u) {
             const float4 xa = s_val[i * NP + gv + G * u];
-            const float4 xb = s_val[ib * NP + gv + G * u];
-            part01[u] = __ffma2_rn(wwa, make_float2(xa.x, xa.y), part01[u]);
-            part23[u] = __ffma2_rn(wwa, make_float2(xa.z, xa.w), part23[u]);
-            part01[u] = __ffma2_rn(wwb, make_float2(xb.x, xb.y), part01[u]);
-            part23[u] = __ffma2_rn(wwb, make_float2(xb.z, xb.w), part23[u]);
+            const float4 xb = s_val[(i + 1) * NP + gv + G * u];
+            part01[u] = __ffma2_rn(wa, make_float2(xa.x, xa.y), part01[u]);
+            part23[u] = __ffma2_rn(wa, make_float2(xa.z, xa.w), part23[u]);
+            part01[u] = __ffma2_rn(wb, make_float2(xb.x, xb.y), part01[u]);
+            part23[u] = __ffma2_rn(wb, make_float2(xb.z, xb.w), part23[u]);
           }
         }
-        if (!got) continue;
+        if (i < iend) {
+          const float2 *ra = s_rec + i * F2;
+          const float2 wa = __fmul2_rn(__fmul2_rn(ra[pa], ra[k1]), w2c[i * F2]);
+#pragma unroll
+          for (int u = 0; u < CPL; ++u) {
+            const float4 xa = s_val[i * NP + gv + G * u];
+            part01[u] = __ffma2_rn(wa, make_float2(xa.x, xa.y), part01[u]);
+            part23[u] = __ffma2_rn(wa, make_float2(xa.z, xa.w), part23[u]);
+          }
+        }
+        if (!in) continue;
         any = true;
 #pragma unroll
         for (int u = 0; u < CPL; ++u) {
@@ -332,7 +348,7 @@ template <int KT, int W, int CPL, bool COMP, bool RP>
 int launch_one(const SpreadParams &a, int64_t max_blocks, cudaStream_t st) {
   constexpr int T = SpreadLanes<W>::T;
   constexpr int NP = (RP ? 1 : SpreadLanes<W>::G) * CPL;
-  const size_t smem = (size_t)a.max_sub * (NP * sizeof(float4) + PointRec<W>::FLOATS * 4 + 3 * sizeof(int)) +
+  const size_t smem = (size_t)a.max_sub * (NP * sizeof(float4) + PointRec<W>::F2 * sizeof(float2) + 3 * sizeof(int)) +
                       (size_t)T * T * sizeof(long long) + (2 * kKeys + 2 + T) * sizeof(int);
   if (smem > 227 * 1024) {
     set_error("spreading stage of %zu bytes exceeds shared memory", smem);

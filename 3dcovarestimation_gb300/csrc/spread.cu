@@ -45,6 +45,7 @@ constexpr int kLMin = -8;   // window corners relative to the bin lie in [kLMin,
 constexpr int kKeys = 256;  // sort key (l1 - kLMin) * 16 + (l0 - kLMin)
 constexpr int kMaxCPL = 3;      // channel pairs per lane per group (row tasks)
 constexpr int kRowPairCPL = 5;  // channel pairs per lane per group (row-pair tasks)
+constexpr int kFoldRanges = 2;  // window-corner rows l1 summed in FP32 between compensated folds
 
 // Per-point record staged once per block, in float2 units (each weight twice, the operand of a
 // packed multiply): the axis-0 weights by tile plane and the axis-2 weights by tile column, zero
@@ -91,8 +92,9 @@ __host__ __device__ constexpr int spread_pairs(int cpl) { return SpreadLanes<W>:
 //  2. a task is one tile row: plane a, row b.  The points whose window covers it are the W
 //     contiguous ranges {l1 = b - o1, l0 in [a - W + 1, a]}, o1 = 0 .. W-1, of the sorted
 //     order.  Lane (g, c) keeps the sums of cell (a, b, c) for its channel pairs in registers:
-//     each range is summed in FP32 and, with COMP, added to the cell's (hi, lo) pair by a
-//     TwoSum, so the error of the cell's accumulation is that of one short FP32 sum per range.
+//     each group of kFoldRanges ranges is summed in FP32 and, with COMP, added to the cell's
+//     (hi, lo) pair by a TwoSum, so the error of the cell's accumulation is that of one short
+//     FP32 sum per group.
 //     The finished row goes to the global grid with one complex atomic per cell and channel.
 //     Warps take tasks from a shared counter, so the heavy middle rows spread over all warps.
 //  The block needs no shared-memory tile: its shared memory is the staged points only, and
@@ -272,45 +274,52 @@ __global__ void __launch_bounds__(kSpreadWarps * 32, RP ? 1 : 2) spread_kernel(c
       bool any = false;
       const int lhi = RP ? rb + 1 : rb;
       const float2 *w2c = s_rec + Rec::W2 + c;  // this lane's column weight, record 0
-      for (int l1 = lhi; l1 > rb - W; --l1) {  // points with window corner l1 cover row l1 + o1
-        const int b1 = l1 - kLMin;
-        if (b1 < 0 || b1 > 15 || b0lo > b0hi) continue;
-        const int ibeg = s_off[(b1 << 4) | b0lo], iend = s_off[((b1 << 4) | b0hi) + 1];
-        if (ibeg >= iend) continue;
-        const int o1 = r1 - l1;
-        const bool in = row_live && o1 >= 0 && o1 < W;
-        const int k1 = Rec::W1 + (in ? o1 : W);  // the zero slot for rows the range misses
+      // points with window corner l1 cover row l1 + o1; the ranges of kFoldRanges consecutive
+      // l1 are summed in FP32 before one compensated fold
+      for (int l1g = lhi; l1g > rb - W; l1g -= kFoldRanges) {
         float2 part01[CPL], part23[CPL];  // packed FP32 (FFMA2), same rounding as fmaf
 #pragma unroll
         for (int u = 0; u < CPL; ++u) {
           part01[u] = make_float2(0.f, 0.f);
           part23[u] = make_float2(0.f, 0.f);
         }
-        // two points per iteration; a lane whose column or row is outside a point's window
-        // multiplies by a zero weight
-        int i = ibeg;
-        for (; i + 1 < iend; i += 2) {
-          const float2 *ra = s_rec + i * F2, *rb2 = ra + F2;
-          const float2 wa = __fmul2_rn(__fmul2_rn(ra[pa], ra[k1]), w2c[i * F2]);
-          const float2 wb = __fmul2_rn(__fmul2_rn(rb2[pa], rb2[k1]), w2c[(i + 1) * F2]);
+        bool in = false;
 #pragma unroll
-          for (int u = 0; u < CPL; ++u) {
-            const float4 xa = s_val[i * NP + gv + G * u];
-            const float4 xb = s_val[(i + 1) * NP + gv + G * u];
-            part01[u] = __ffma2_rn(wa, make_float2(xa.x, xa.y), part01[u]);
-            part23[u] = __ffma2_rn(wa, make_float2(xa.z, xa.w), part23[u]);
-            part01[u] = __ffma2_rn(wb, make_float2(xb.x, xb.y), part01[u]);
-            part23[u] = __ffma2_rn(wb, make_float2(xb.z, xb.w), part23[u]);
+        for (int sr = 0; sr < kFoldRanges; ++sr) {
+          const int l1 = l1g - sr;
+          const int b1 = l1 - kLMin;
+          if (l1 <= rb - W || b1 < 0 || b1 > 15 || b0lo > b0hi) continue;
+          const int ibeg = s_off[(b1 << 4) | b0lo], iend = s_off[((b1 << 4) | b0hi) + 1];
+          const int o1 = r1 - l1;
+          const bool in1 = row_live && o1 >= 0 && o1 < W;
+          in |= in1 && ibeg < iend;
+          const int k1 = Rec::W1 + (in1 ? o1 : W);  // the zero slot for rows the range misses
+          // two points per iteration; a lane whose column or row is outside a point's window
+          // multiplies by a zero weight
+          int i = ibeg;
+          for (; i + 1 < iend; i += 2) {
+            const float2 *ra = s_rec + i * F2, *rb2 = ra + F2;
+            const float2 wa = __fmul2_rn(__fmul2_rn(ra[pa], ra[k1]), w2c[i * F2]);
+            const float2 wb = __fmul2_rn(__fmul2_rn(rb2[pa], rb2[k1]), w2c[(i + 1) * F2]);
+#pragma unroll
+            for (int u = 0; u < CPL; ++u) {
+              const float4 xa = s_val[i * NP + gv + G * u];
+              const float4 xb = s_val[(i + 1) * NP + gv + G * u];
+              part01[u] = __ffma2_rn(wa, make_float2(xa.x, xa.y), part01[u]);
+              part23[u] = __ffma2_rn(wa, make_float2(xa.z, xa.w), part23[u]);
+              part01[u] = __ffma2_rn(wb, make_float2(xb.x, xb.y), part01[u]);
+              part23[u] = __ffma2_rn(wb, make_float2(xb.z, xb.w), part23[u]);
+            }
           }
-        }
-        if (i < iend) {
-          const float2 *ra = s_rec + i * F2;
-          const float2 wa = __fmul2_rn(__fmul2_rn(ra[pa], ra[k1]), w2c[i * F2]);
+          if (i < iend) {
+            const float2 *ra = s_rec + i * F2;
+            const float2 wa = __fmul2_rn(__fmul2_rn(ra[pa], ra[k1]), w2c[i * F2]);
 #pragma unroll
-          for (int u = 0; u < CPL; ++u) {
-            const float4 xa = s_val[i * NP + gv + G * u];
-            part01[u] = __ffma2_rn(wa, make_float2(xa.x, xa.y), part01[u]);
-            part23[u] = __ffma2_rn(wa, make_float2(xa.z, xa.w), part23[u]);
+            for (int u = 0; u < CPL; ++u) {
+              const float4 xa = s_val[i * NP + gv + G * u];
+              part01[u] = __ffma2_rn(wa, make_float2(xa.x, xa.y), part01[u]);
+              part23[u] = __ffma2_rn(wa, make_float2(xa.z, xa.w), part23[u]);
+            }
           }
         }
         if (!in) continue;

@@ -43,22 +43,187 @@ __device__ __forceinline__ float prologue(const PointGeom &g, int64_t id, const 
 
 constexpr int kLMin = -8;   // window corners relative to the bin lie in [kLMin, kLMin + 16)
 constexpr int kKeys = 256;  // sort key (l1 - kLMin) * 16 + (l0 - kLMin)
-constexpr int kMaxCPL = 3;      // channel pairs per lane per group (row tasks)
-constexpr int kRowPairCPL = 5;  // channel pairs per lane per group (row-pair tasks)
 constexpr int kFoldRanges = 2;  // window-corner rows l1 summed in FP32 between compensated folds
 
 // Per-point record staged once per block, in float2 units (each weight twice, the operand of a
 // packed multiply): the axis-0 weights by tile plane and the axis-2 weights by tile column, zero
-// outside the point's window, and the W axis-1 weights followed by a zero.  A lane's weight is
-// then rec[plane] * rec[W1 + o1] * rec[W2 + column], with no corner arithmetic and no select:
+// outside the point's window (the column slot T is always zero, for idle lanes), and the W
+// axis-1 weights with ROWS - 1 zeros before them and max(ROWS - 1, 1) after.  A lane's weight
+// for tile row b of a point with window corner l1 is then
+// rec[plane] * rec[W1 + b - l1] * rec[W2 + column], with no corner arithmetic and no select:
 // lanes outside the window read zeros.
-template <int W>
+template <int W, int ROWS>
 struct PointRec {
   static constexpr int T = kBin + W - 1;
-  static constexpr int W1 = T;              // axis-1 weights, then the zero slot W1 + W
-  static constexpr int W2 = T + W + 1;      // axis-2 weights by column
-  static constexpr int F2 = (2 * T + W + 2) / 2 * 2;  // float2 per record (even)
+  static constexpr int W1 = T + ROWS - 1;            // axis-1 weight o1 at W1 + o1
+  static constexpr int Z1 = ROWS > 1 ? ROWS - 1 : 1;  // zeros after the axis-1 weights
+  static constexpr int W2 = W1 + W + Z1;             // axis-2 weights by column
+  static constexpr int F2 = (W2 + T + 2) / 2 * 2;    // float2 per record (even)
 };
+
+// Shared memory after the staged channel values: tile row offsets, point records, sort keys,
+// point ids, prologue factors, key counters and offsets, column offsets, the task counter.
+struct StageSmem {
+  long long *rowoff;  // T * T
+  float2 *rec;        // max_sub * F2
+  int *key, *pid;     // max_sub each
+  float *sc;          // max_sub
+  int *cnt, *off;     // kKeys, kKeys + 1
+  int *coloff;        // T
+  int *task;          // 1
+};
+
+__host__ __device__ constexpr size_t stage_bytes(int max_sub, int T, int F2) {
+  return (size_t)T * T * sizeof(long long) + (size_t)max_sub * (F2 * sizeof(float2) + 3 * sizeof(int)) +
+         (size_t)(2 * kKeys + 2 + T) * sizeof(int);
+}
+
+__device__ __forceinline__ StageSmem carve(void *base, int max_sub, int T, int F2) {
+  StageSmem s;
+  s.rowoff = static_cast<long long *>(base);
+  s.rec = reinterpret_cast<float2 *>(s.rowoff + T * T);
+  s.key = reinterpret_cast<int *>(s.rec + max_sub * F2);
+  s.pid = s.key + max_sub;
+  s.sc = reinterpret_cast<float *>(s.pid + max_sub);
+  s.cnt = reinterpret_cast<int *>(s.sc + max_sub);
+  s.off = s.cnt + kKeys;
+  s.coloff = s.off + kKeys + 1;
+  s.task = s.coloff + T;
+  return s;
+}
+
+// A subproblem: its points [first, first + cnt) of the sorted order and the tile origin.
+struct SubTile {
+  int first, cnt, ts0, ts1, ts2;
+};
+
+__device__ __forceinline__ SubTile sub_tile(const SpreadParams &a, int sub) {
+  const int bin = a.sub_bin[sub];
+  const int nb12 = a.bins.nb[1] * a.bins.nb[2];
+  SubTile t;
+  t.first = a.sub_first[sub];
+  t.cnt = a.sub_count[sub];
+  t.ts0 = (bin / nb12) * kBin;
+  t.ts1 = ((bin / a.bins.nb[2]) % a.bins.nb[1]) * kBin;
+  t.ts2 = (bin % a.bins.nb[2]) * kBin;
+  return t;
+}
+
+// Stage 1 of both spreading kernels: the block counting-sorts its points by the (axis-1,
+// axis-0) corner (l1, l0) of their window and stages, in that order, each point's record, id
+// and prologue factor (im_backward's Nyquist zeroing, CTF and scale), then the global offsets
+// of the tile's rows and columns.  The caller synchronises before reading them.
+template <int KT, int W, int ROWS>
+__device__ __forceinline__ void stage_subproblem(const SpreadParams &a, const StageSmem &s, const SubTile &st) {
+  using Rec = PointRec<W, ROWS>;
+  constexpr int T = Rec::T;
+  constexpr int F2 = Rec::F2;
+  const int n = a.g.n;
+  const int tid = threadIdx.x;
+  for (int e = tid; e < kKeys; e += blockDim.x) s.cnt[e] = 0;
+  __syncthreads();
+  // sort keys and ranks
+  for (int k = tid; k < st.cnt; k += blockDim.x) {
+    const SortedPoint sp = a.pts[st.first + k];
+    int c0 = first_cell<KT, W>(sp.t0), c1 = first_cell<KT, W>(sp.t1);
+    if (KT == COV3D_KERNEL_ES) {
+      c0 = wrap1(c0, n);
+      c1 = wrap1(c1, n);
+    }
+    const int key = (min(max(c1 - st.ts1 - kLMin, 0), 15) << 4) | min(max(c0 - st.ts0 - kLMin, 0), 15);
+    s.key[k] = key | (atomicAdd(s.cnt + key, 1) << 8);
+  }
+  __syncthreads();
+  if (tid < 32) {  // exclusive scan of the 256 counters by one warp, 8 per lane
+    int v[kKeys / 32], sum = 0;
+#pragma unroll
+    for (int u = 0; u < kKeys / 32; ++u) {
+      v[u] = s.cnt[tid * (kKeys / 32) + u];
+      sum += v[u];
+    }
+    int incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, incl, o);
+      if (tid >= o) incl += t;
+    }
+    int base = incl - sum;
+#pragma unroll
+    for (int u = 0; u < kKeys / 32; ++u) {
+      s.off[tid * (kKeys / 32) + u] = base;
+      base += v[u];
+    }
+    if (tid == 31) s.off[kKeys] = incl;
+  }
+  __syncthreads();
+  // records, point ids and prologue factors in sorted order
+  for (int k = tid; k < st.cnt; k += blockDim.x) {
+    const SortedPoint sp = a.pts[st.first + k];
+    const int kr = s.key[k];
+    const int slot = s.off[kr & 255] + (kr >> 8);
+    float w0[W], w1[W], w2[W];
+    int c0 = taps<KT, W>(sp.t0, a.k.beta, w0);
+    taps<KT, W>(sp.t1, a.k.beta, w1);
+    int c2 = taps<KT, W>(sp.t2, a.k.beta, w2);
+    if (KT == COV3D_KERNEL_ES) {
+      c0 = wrap1(c0, n);
+      c2 = wrap1(c2, n);
+    }
+    float2 *rec = s.rec + slot * F2;
+    const int l0 = c0 - st.ts0, l2 = c2 - st.ts2;  // bin-local corners, >= 1 - W (zero padding below)
+    const float2 z = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int e = 0; e < T; ++e) {
+      rec[e] = z;
+      rec[Rec::W2 + e] = z;
+    }
+    rec[Rec::W2 + T] = z;
+#pragma unroll
+    for (int e = T; e < Rec::W1; ++e) rec[e] = z;
+#pragma unroll
+    for (int e = Rec::W1 + W; e < Rec::W2; ++e) rec[e] = z;
+#pragma unroll
+    for (int r = 0; r < W; ++r) {
+      if (l0 + r >= 0 && l0 + r < T) rec[l0 + r] = make_float2(w0[r], w0[r]);
+      if (l2 + r >= 0 && l2 + r < T) rec[Rec::W2 + l2 + r] = make_float2(w2[r], w2[r]);
+      rec[Rec::W1 + r] = make_float2(w1[r], w1[r]);
+    }
+    const int id = sp_id(sp.idf);
+    float sc = (a.nyquist && sp_nyquist(sp.idf)) ? 0.0f : a.scale;
+    if (a.ctf) sc *= __ldg(a.ctf + id);
+    s.pid[slot] = id;
+    s.sc[slot] = sc;
+  }
+  // global offsets of the tile's rows (axes 0, 1) and columns (axis 2)
+  for (int e = tid; e < T * T; e += blockDim.x) {
+    const int ra = e / T, rb = e - (e / T) * T;
+    int m0 = st.ts0 + ra, m1 = st.ts1 + rb;
+    bool ok = true;
+    if (KT == COV3D_KERNEL_ES) {
+      m0 = m0 >= n ? m0 - n : m0;
+      m1 = m1 >= n ? m1 - n : m1;
+    } else {
+      ok = m0 < n && m1 < n;
+    }
+    m0 += a.shift;
+    m1 += a.shift;
+    m0 = m0 >= n ? m0 - n : m0;
+    m1 = m1 >= n ? m1 - n : m1;
+    s.rowoff[e] = ok ? ((int64_t)m0 * n + m1) * n : -1;
+  }
+  for (int e = tid; e < T; e += blockDim.x) {
+    int m2 = st.ts2 + e;
+    bool ok = true;
+    if (KT == COV3D_KERNEL_ES) {
+      m2 = m2 >= n ? m2 - n : m2;
+    } else {
+      ok = m2 < n;
+    }
+    m2 += a.shift;
+    m2 = m2 >= n ? m2 - n : m2;
+    s.coloff[e] = ok ? m2 : -1;
+  }
+}
 
 // TwoSum (Knuth) on both lanes of a float2: s + d = s' + e exactly, e added to the error sum
 // err.  Differences are fused multiply-adds with -1, which round exactly like a subtraction.
@@ -81,189 +246,57 @@ struct SpreadLanes {
   static constexpr int G = 32 / T;
 };
 
-template <int W>
-__host__ __device__ constexpr int spread_pairs(int cpl) { return SpreadLanes<W>::G * cpl; }
-
-// One block per subproblem (a bin of 8^3 cells and at most max_sub of its points); the cells
-// it can reach form a tile of the bin and a (W-1)-cell halo, T^3 cells.
-//  1. the block counting-sorts its points by the (axis-1, axis-0) corner (l1, l0) of their
-//     window and stages, in that order, each point's record (packed corner, 3W weights) and
-//     its CTF-scaled channel pairs (im_backward's prologue folded in);
-//  2. a task is one tile row: plane a, row b.  The points whose window covers it are the W
-//     contiguous ranges {l1 = b - o1, l0 in [a - W + 1, a]}, o1 = 0 .. W-1, of the sorted
-//     order.  Lane (g, c) keeps the sums of cell (a, b, c) for its channel pairs in registers:
-//     each group of kFoldRanges ranges is summed in FP32 and, with COMP, added to the cell's
-//     (hi, lo) pair by a TwoSum, so the error of the cell's accumulation is that of one short
-//     FP32 sum per group.
-//     The finished row goes to the global grid with one complex atomic per cell and channel.
-//     Warps take tasks from a shared counter, so the heavy middle rows spread over all warps.
-//  The block needs no shared-memory tile: its shared memory is the staged points only, and
-//  several blocks share an SM.
-template <int KT, int W, int CPL, bool COMP, bool RP>
-__global__ void __launch_bounds__(kSpreadWarps * 32, RP ? 1 : 2) spread_kernel(const SpreadParams a) {
+// Row tasks, for few channels.  One block per subproblem (a bin of 8^3 cells and at most
+// max_sub of its points); the cells it can reach form a tile of the bin and a (W-1)-cell halo,
+// T^3 cells.  After stage_subproblem, a task is one tile row: plane a, row b.  The points whose
+// window covers it are the W contiguous ranges {l1 = b - o1, l0 in [a - W + 1, a]},
+// o1 = 0 .. W-1, of the sorted order.  Lane (g, c) keeps the sums of cell (a, b, c) for its
+// channel pairs in registers: each group of kFoldRanges ranges is summed in FP32 and, with COMP,
+// added to the cell's (hi, lo) pair by a TwoSum, so the error of the cell's accumulation is that
+// of one short FP32 sum per group.  The finished row goes to the global grid with one complex
+// atomic per cell and channel.  Warps take tasks from a shared counter.  The block needs no
+// shared-memory tile: its shared memory is the staged points only.
+template <int KT, int W, int CPL, bool COMP>
+__global__ void __launch_bounds__(kSpreadWarps * 32, W < 8 ? 2 : 1) spread_kernel(const SpreadParams a) {
   constexpr int T = SpreadLanes<W>::T;
-  constexpr int G = RP ? 1 : SpreadLanes<W>::G;  // lane groups over channel pairs
-  constexpr int NP = G * CPL;                     // channel pairs staged per group
-  constexpr int TP = (T + 1) / 2;                 // row pairs per plane (RP)
-  static_assert(!RP || 2 * T <= 32, "two rows of lanes per warp");
-  using Rec = PointRec<W>;
+  constexpr int G = SpreadLanes<W>::G;  // lane groups over channel pairs
+  constexpr int NP = G * CPL;           // channel pairs staged per group
+  using Rec = PointRec<W, 1>;
   constexpr int F2 = Rec::F2;
   extern __shared__ float4 smem4[];
-  float4 *s_val = smem4;                                                         // max_sub * NP
-  long long *s_rowoff = reinterpret_cast<long long *>(s_val + a.max_sub * NP);  // T * T
-  float2 *s_rec = reinterpret_cast<float2 *>(s_rowoff + T * T);                // max_sub * F2
-  int *s_key = reinterpret_cast<int *>(s_rec + a.max_sub * F2);                // max_sub
-  int *s_pid = s_key + a.max_sub;                                              // max_sub
-  float *s_sc = reinterpret_cast<float *>(s_pid + a.max_sub);                  // max_sub
-  int *s_cnt = reinterpret_cast<int *>(s_sc + a.max_sub);                      // kKeys
-  int *s_off = s_cnt + kKeys;                                                  // kKeys + 1
-  int *s_coloff = s_off + kKeys + 1;                                           // T
-  int *s_task = s_coloff + T;                                                  // 1
-
+  float4 *s_val = smem4;  // max_sub * NP
+  const StageSmem s = carve(s_val + a.max_sub * NP, a.max_sub, T, F2);
   const int sub = blockIdx.x;
   if (sub >= *a.nsub) return;
-  const int bin = a.sub_bin[sub];
-  const int first = a.sub_first[sub];
-  const int cnt = a.sub_count[sub];
-  const int nb12 = a.bins.nb[1] * a.bins.nb[2];
-  const int ts0 = (bin / nb12) * kBin;
-  const int ts1 = ((bin / a.bins.nb[2]) % a.bins.nb[1]) * kBin;
-  const int ts2 = (bin % a.bins.nb[2]) * kBin;
-  const int n = a.g.n;
-  const int tid = threadIdx.x;
+  const SubTile st = sub_tile(a, sub);
+  stage_subproblem<KT, W, 1>(a, s, st);
 
-  for (int e = tid; e < kKeys; e += blockDim.x) s_cnt[e] = 0;
-  __syncthreads();
-  // 1a. sort keys and ranks
-  for (int k = tid; k < cnt; k += blockDim.x) {
-    const SortedPoint sp = a.pts[first + k];
-    int c0 = first_cell<KT, W>(sp.t0), c1 = first_cell<KT, W>(sp.t1);
-    if (KT == COV3D_KERNEL_ES) {
-      c0 = wrap1(c0, n);
-      c1 = wrap1(c1, n);
-    }
-    const int key = (min(max(c1 - ts1 - kLMin, 0), 15) << 4) | min(max(c0 - ts0 - kLMin, 0), 15);
-    s_key[k] = key | (atomicAdd(s_cnt + key, 1) << 8);
-  }
-  __syncthreads();
-  if (tid < 32) {  // exclusive scan of the 256 counters by one warp, 8 per lane
-    int v[kKeys / 32], sum = 0;
-#pragma unroll
-    for (int u = 0; u < kKeys / 32; ++u) {
-      v[u] = s_cnt[tid * (kKeys / 32) + u];
-      sum += v[u];
-    }
-    int incl = sum;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int t = __shfl_up_sync(0xffffffffu, incl, o);
-      if (tid >= o) incl += t;
-    }
-    int base = incl - sum;
-#pragma unroll
-    for (int u = 0; u < kKeys / 32; ++u) {
-      s_off[tid * (kKeys / 32) + u] = base;
-      base += v[u];
-    }
-    if (tid == 31) s_off[kKeys] = incl;
-  }
-  __syncthreads();
-  // 1b. records, point ids and prologue factors in sorted order
-  for (int k = tid; k < cnt; k += blockDim.x) {
-    const SortedPoint sp = a.pts[first + k];
-    const int kr = s_key[k];
-    const int slot = s_off[kr & 255] + (kr >> 8);
-    float w0[W], w1[W], w2[W];
-    int c0 = taps<KT, W>(sp.t0, a.k.beta, w0);
-    int c1 = taps<KT, W>(sp.t1, a.k.beta, w1);
-    int c2 = taps<KT, W>(sp.t2, a.k.beta, w2);
-    if (KT == COV3D_KERNEL_ES) {
-      c0 = wrap1(c0, n);
-      c1 = wrap1(c1, n);
-      c2 = wrap1(c2, n);
-    }
-    (void)c1;
-    float2 *rec = s_rec + slot * F2;
-    const int l0 = c0 - ts0, l2 = c2 - ts2;  // bin-local corners, >= 1 - W (zero padding below)
-#pragma unroll
-    for (int e = 0; e < T; ++e) {
-      rec[e] = make_float2(0.f, 0.f);
-      rec[Rec::W2 + e] = make_float2(0.f, 0.f);
-    }
-#pragma unroll
-    for (int r = 0; r < W; ++r) {
-      if (l0 + r >= 0 && l0 + r < T) rec[l0 + r] = make_float2(w0[r], w0[r]);
-      if (l2 + r >= 0 && l2 + r < T) rec[Rec::W2 + l2 + r] = make_float2(w2[r], w2[r]);
-      rec[Rec::W1 + r] = make_float2(w1[r], w1[r]);
-    }
-    rec[Rec::W1 + W] = make_float2(0.f, 0.f);
-    const int id = sp_id(sp.idf);
-    float sc = (a.nyquist && sp_nyquist(sp.idf)) ? 0.0f : a.scale;
-    if (a.ctf) sc *= __ldg(a.ctf + id);
-    s_pid[slot] = id;
-    s_sc[slot] = sc;
-  }
-  // global offsets of the tile's rows (axes 0, 1) and columns (axis 2)
-  for (int e = tid; e < T * T; e += blockDim.x) {
-    const int ra = e / T, rb = e - (e / T) * T;
-    int m0 = ts0 + ra, m1 = ts1 + rb;
-    bool ok = true;
-    if (KT == COV3D_KERNEL_ES) {
-      m0 = m0 >= n ? m0 - n : m0;
-      m1 = m1 >= n ? m1 - n : m1;
-    } else {
-      ok = m0 < n && m1 < n;
-    }
-    m0 += a.shift;
-    m1 += a.shift;
-    m0 = m0 >= n ? m0 - n : m0;
-    m1 = m1 >= n ? m1 - n : m1;
-    s_rowoff[e] = ok ? ((int64_t)m0 * n + m1) * n : -1;
-  }
-  for (int e = tid; e < T; e += blockDim.x) {
-    int m2 = ts2 + e;
-    bool ok = true;
-    if (KT == COV3D_KERNEL_ES) {
-      m2 = m2 >= n ? m2 - n : m2;
-    } else {
-      ok = m2 < n;
-    }
-    m2 += a.shift;
-    m2 = m2 >= n ? m2 - n : m2;
-    s_coloff[e] = ok ? m2 : -1;
-  }
-
-  const int lane = tid & 31;
-  // RP: lane = (row of the pair, column), every lane all NP pairs; else lane = (pair group, column)
+  const int tid = threadIdx.x, lane = tid & 31;
   const int g = lane / T, c = lane - (lane / T) * T;
-  const bool lane_live = RP ? g < 2 : g < G;
-  const int gv = (RP || !lane_live) ? 0 : g;  // idle lanes compute pair 0 and drop it
+  const bool lane_live = g < G;
+  const int gv = lane_live ? g : 0;  // idle lanes compute pair 0 and drop it
   const int npairs = (a.nch + 1) / 2;
   for (int p0 = 0; p0 < npairs; p0 += NP) {  // channel groups of NP pairs
     __syncthreads();
-    // 1c. this group's scaled channel pairs, in sorted order
-    for (int e = tid; e < cnt * NP; e += blockDim.x) {
+    // this group's scaled channel pairs, in sorted order
+    for (int e = tid; e < st.cnt * NP; e += blockDim.x) {
       const int slot = e / NP, pp = p0 + (e - (e / NP) * NP);
-      const float sc = s_sc[slot];
-      const float2 *src = a.vals + (int64_t)s_pid[slot] * a.ips + (int64_t)(a.ch0 + 2 * pp) * a.ics;
+      const float sc = s.sc[slot];
+      const float2 *src = a.vals + (int64_t)s.pid[slot] * a.ips + (int64_t)(a.ch0 + 2 * pp) * a.ics;
       const float2 v0 = 2 * pp < a.nch ? __ldg(src) : make_float2(0.f, 0.f);
       const float2 v1 = 2 * pp + 1 < a.nch ? __ldg(src + a.ics) : make_float2(0.f, 0.f);
       s_val[e] = make_float4(v0.x * sc, v0.y * sc, v1.x * sc, v1.y * sc);
     }
-    if (tid == 0) *s_task = 0;
+    if (tid == 0) *s.task = 0;
     __syncthreads();
 
-    // 2. row tasks (RP: row-pair tasks)
-    constexpr int ntasks = RP ? T * TP : T * T;
     for (;;) {
       int task = 0;
-      if (lane == 0) task = atomicAdd(s_task, 1);
+      if (lane == 0) task = atomicAdd(s.task, 1);
       task = __shfl_sync(0xffffffffu, task, 0);
-      if (task >= ntasks) break;
-      const int pa = RP ? task / TP : task / T;
-      const int rb = RP ? (task - pa * TP) * 2 : task - pa * T;  // first row of the task
-      const int r1 = RP ? rb + g : rb;                            // this lane's row
-      const bool row_live = lane_live && r1 < T;
+      if (task >= T * T) break;
+      const int pa = task / T;
+      const int rb = task - pa * T;  // the task's row
       const int b0lo = max(pa - W + 1 - kLMin, 0), b0hi = min(pa - kLMin, 15);
       // cell sums of channel pairs (0, 1) and (2, 3) of each pair group, and their TwoSum errors
       float2 hi01[CPL], hi23[CPL], lo01[CPL], lo23[CPL];
@@ -272,11 +305,8 @@ __global__ void __launch_bounds__(kSpreadWarps * 32, RP ? 1 : 2) spread_kernel(c
         hi01[u] = hi23[u] = lo01[u] = lo23[u] = make_float2(0.f, 0.f);
       }
       bool any = false;
-      const int lhi = RP ? rb + 1 : rb;
-      const float2 *w2c = s_rec + Rec::W2 + c;  // this lane's column weight, record 0
-      // points with window corner l1 cover row l1 + o1; the ranges of kFoldRanges consecutive
-      // l1 are summed in FP32 before one compensated fold
-      for (int l1g = lhi; l1g > rb - W; l1g -= kFoldRanges) {
+      const float2 *w2c = s.rec + Rec::W2 + c;  // this lane's column weight, record 0
+      for (int l1g = rb; l1g > rb - W; l1g -= kFoldRanges) {
         float2 part01[CPL], part23[CPL];  // packed FP32 (FFMA2), same rounding as fmaf
 #pragma unroll
         for (int u = 0; u < CPL; ++u) {
@@ -289,16 +319,14 @@ __global__ void __launch_bounds__(kSpreadWarps * 32, RP ? 1 : 2) spread_kernel(c
           const int l1 = l1g - sr;
           const int b1 = l1 - kLMin;
           if (l1 <= rb - W || b1 < 0 || b1 > 15 || b0lo > b0hi) continue;
-          const int ibeg = s_off[(b1 << 4) | b0lo], iend = s_off[((b1 << 4) | b0hi) + 1];
-          const int o1 = r1 - l1;
-          const bool in1 = row_live && o1 >= 0 && o1 < W;
-          in |= in1 && ibeg < iend;
-          const int k1 = Rec::W1 + (in1 ? o1 : W);  // the zero slot for rows the range misses
-          // two points per iteration; a lane whose column or row is outside a point's window
+          const int ibeg = s.off[(b1 << 4) | b0lo], iend = s.off[((b1 << 4) | b0hi) + 1];
+          in |= lane_live && ibeg < iend;
+          const int k1 = Rec::W1 + (lane_live ? rb - l1 : W);  // a zero slot for idle lanes
+          // two points per iteration; a lane whose column is outside a point's window
           // multiplies by a zero weight
           int i = ibeg;
           for (; i + 1 < iend; i += 2) {
-            const float2 *ra = s_rec + i * F2, *rb2 = ra + F2;
+            const float2 *ra = s.rec + i * F2, *rb2 = ra + F2;
             const float2 wa = __fmul2_rn(__fmul2_rn(ra[pa], ra[k1]), w2c[i * F2]);
             const float2 wb = __fmul2_rn(__fmul2_rn(rb2[pa], rb2[k1]), w2c[(i + 1) * F2]);
 #pragma unroll
@@ -312,7 +340,7 @@ __global__ void __launch_bounds__(kSpreadWarps * 32, RP ? 1 : 2) spread_kernel(c
             }
           }
           if (i < iend) {
-            const float2 *ra = s_rec + i * F2;
+            const float2 *ra = s.rec + i * F2;
             const float2 wa = __fmul2_rn(__fmul2_rn(ra[pa], ra[k1]), w2c[i * F2]);
 #pragma unroll
             for (int u = 0; u < CPL; ++u) {
@@ -335,10 +363,10 @@ __global__ void __launch_bounds__(kSpreadWarps * 32, RP ? 1 : 2) spread_kernel(c
           }
         }
       }
-      // 3. the finished cell goes to the global grid
-      if (!any || !row_live) continue;
-      const long long ro = s_rowoff[pa * T + r1];
-      const int co = s_coloff[c];
+      // the finished cell goes to the global grid
+      if (!any) continue;
+      const long long ro = s.rowoff[pa * T + rb];
+      const int co = s.coloff[c];
       if (ro < 0 || co < 0) continue;
 #pragma unroll
       for (int u = 0; u < CPL; ++u) {
@@ -353,39 +381,176 @@ __global__ void __launch_bounds__(kSpreadWarps * 32, RP ? 1 : 2) spread_kernel(c
   }
 }
 
-template <int KT, int W, int CPL, bool COMP, bool RP>
-int launch_one(const SpreadParams &a, int64_t max_blocks, cudaStream_t st) {
-  constexpr int T = SpreadLanes<W>::T;
-  constexpr int NP = (RP ? 1 : SpreadLanes<W>::G) * CPL;
-  const size_t smem = (size_t)a.max_sub * (NP * sizeof(float4) + PointRec<W>::F2 * sizeof(float2) + 3 * sizeof(int)) +
-                      (size_t)T * T * sizeof(long long) + (2 * kKeys + 2 + T) * sizeof(int);
+// Row-group tasks with the channels split over two lane halves, for many channels (the
+// covariance gradient's r eigenvolumes).  Stage 1 as in spread_kernel; the channel values of a
+// group of 2 * CH channels are staged per point as two 16-byte-aligned halves of CH.  A task is
+// ROWS consecutive tile rows of one plane: lane (h, c) owns tile column c of those rows for the
+// channels of half h (26 of 32 lanes at W = 6), so every point of the task's ranges costs a lane
+// CH values, ROWS + 2 weight loads and ROWS * CH packed multiply-adds, and a point is visited by
+// the tasks of its W planes and the row groups its W rows meet (W = 6, ROWS = 3: 16 on
+// average).  Shared memory returns per point and lane 40 bytes of values where lanes owning all
+// channels of one cell would take 80: the loads, not the multiply-adds, bound this kernel.  The
+// task's ranges are those of the corners l1 in [b - W + 1, b + ROWS - 1]; the summation (FP32
+// groups of kFoldRanges ranges, TwoSum folds with COMP) and the atomics are those of
+// spread_kernel.
+template <int KT, int W, int CH, int ROWS, bool COMP>
+__global__ void __launch_bounds__(kSpreadWarps * 32, 1) spread_rows_kernel(const SpreadParams a) {
+  constexpr int T = kBin + W - 1;
+  static_assert(2 * T <= 32, "two lane halves of T columns per warp");
+  constexpr int HS = (CH + 1) / 2 * 2;       // float2 per half of a point's values (even)
+  constexpr int PS = 2 * HS;                 // float2 of values per point
+  constexpr int RG = (T + ROWS - 1) / ROWS;  // row groups per plane
+  using Rec = PointRec<W, ROWS>;
+  constexpr int F2 = Rec::F2;
+  extern __shared__ float4 smem4[];
+  float2 *s_val = reinterpret_cast<float2 *>(smem4);  // max_sub * PS
+  const StageSmem s = carve(s_val + a.max_sub * PS, a.max_sub, T, F2);
+  const int sub = blockIdx.x;
+  if (sub >= *a.nsub) return;
+  const SubTile st = sub_tile(a, sub);
+  stage_subproblem<KT, W, ROWS>(a, s, st);
+
+  const int tid = threadIdx.x, lane = tid & 31;
+  const int h = lane / T;
+  const bool lane_live = h < 2;
+  const int hv = lane_live ? h : 0;             // idle lanes read half 0 ...
+  const int c = lane_live ? lane - h * T : T;   // ... and the zero column weight
+  const float2 *w2c = s.rec + Rec::W2 + c;      // this lane's column weight, record 0
+  for (int p0 = 0; p0 < a.nch; p0 += 2 * CH) {  // channel groups of 2 * CH
+    __syncthreads();
+    // this group's scaled channel values, in sorted order: half hh holds p0 + hh * CH + ch
+    for (int e = tid; e < st.cnt * 2 * CH; e += blockDim.x) {
+      const int slot = e / (2 * CH), r = e - slot * (2 * CH);
+      const int hh = r / CH, ch = r - hh * CH;
+      const float sc = s.sc[slot];
+      float2 v = make_float2(0.f, 0.f);
+      if (p0 + r < a.nch) {
+        const float2 x = __ldg(a.vals + (int64_t)s.pid[slot] * a.ips + (int64_t)(a.ch0 + p0 + r) * a.ics);
+        v = make_float2(x.x * sc, x.y * sc);
+      }
+      s_val[slot * PS + hh * HS + ch] = v;
+    }
+    if (tid == 0) *s.task = 0;
+    __syncthreads();
+
+    for (;;) {
+      int task = 0;
+      if (lane == 0) task = atomicAdd(s.task, 1);
+      task = __shfl_sync(0xffffffffu, task, 0);
+      if (task >= T * RG) break;
+      const int pa = task / RG;
+      const int rb = (task - pa * RG) * ROWS;  // first row of the task
+      const int b0lo = max(pa - W + 1 - kLMin, 0), b0hi = min(pa - kLMin, 15);
+      float2 hi[ROWS][CH], lo[ROWS][CH];  // cell sums and their TwoSum errors
+#pragma unroll
+      for (int q = 0; q < ROWS; ++q)
+#pragma unroll
+        for (int ch = 0; ch < CH; ++ch) hi[q][ch] = lo[q][ch] = make_float2(0.f, 0.f);
+      bool any = false;
+      for (int l1g = rb + ROWS - 1; l1g > rb - W; l1g -= kFoldRanges) {
+        float2 part[ROWS][CH];  // packed FP32 (FFMA2), same rounding as fmaf
+#pragma unroll
+        for (int q = 0; q < ROWS; ++q)
+#pragma unroll
+          for (int ch = 0; ch < CH; ++ch) part[q][ch] = make_float2(0.f, 0.f);
+        bool got = false;
+#pragma unroll
+        for (int sr = 0; sr < kFoldRanges; ++sr) {
+          const int l1 = l1g - sr;
+          const int b1 = l1 - kLMin;
+          if (l1 <= rb - W || b1 < 0 || b1 > 15 || b0lo > b0hi) continue;
+          const int ibeg = s.off[(b1 << 4) | b0lo], iend = s.off[((b1 << 4) | b0hi) + 1];
+          got |= ibeg < iend;
+          const int k1 = Rec::W1 + rb - l1;  // row rb + q reads the axis-1 weight k1 + q
+          for (int i = ibeg; i < iend; ++i) {
+            const float2 *rec = s.rec + i * F2;
+            const float2 w02 = __fmul2_rn(rec[pa], w2c[i * F2]);
+            float2 w[ROWS];
+#pragma unroll
+            for (int q = 0; q < ROWS; ++q) w[q] = __fmul2_rn(w02, rec[k1 + q]);
+            const float2 *vp = s_val + i * PS + hv * HS;
+            float2 v[CH];
+#pragma unroll
+            for (int ch = 0; ch + 1 < CH; ch += 2) {
+              const float4 x = *reinterpret_cast<const float4 *>(vp + ch);
+              v[ch] = make_float2(x.x, x.y);
+              v[ch + 1] = make_float2(x.z, x.w);
+            }
+            if (CH & 1) v[CH - 1] = vp[CH - 1];
+#pragma unroll
+            for (int q = 0; q < ROWS; ++q)
+#pragma unroll
+              for (int ch = 0; ch < CH; ++ch) part[q][ch] = __ffma2_rn(w[q], v[ch], part[q][ch]);
+          }
+        }
+        if (!got) continue;
+        any = true;
+#pragma unroll
+        for (int q = 0; q < ROWS; ++q)
+#pragma unroll
+          for (int ch = 0; ch < CH; ++ch) {
+            if (!COMP) hi[q][ch] = __fadd2_rn(hi[q][ch], part[q][ch]);
+            else two_sum2(hi[q][ch], lo[q][ch], part[q][ch]);
+          }
+      }
+      // the finished cells go to the global grid
+      if (!any || !lane_live) continue;
+      const int co = s.coloff[c];
+      if (co < 0) continue;
+#pragma unroll
+      for (int q = 0; q < ROWS; ++q) {
+        if (rb + q >= T) break;
+        const long long ro = s.rowoff[pa * T + rb + q];
+        if (ro < 0) continue;
+        float2 *dst = a.grid + (ro + co) * a.cs + (int64_t)(a.ch0 + p0 + hv * CH) * a.chs;
+#pragma unroll
+        for (int ch = 0; ch < CH; ++ch) {
+          const float2 x = COMP ? __fadd2_rn(hi[q][ch], lo[q][ch]) : hi[q][ch];
+          if (p0 + hv * CH + ch < a.nch && (x.x != 0.0f || x.y != 0.0f)) atomicAdd(dst + ch * a.chs, x);
+        }
+      }
+    }
+  }
+}
+
+constexpr int kRowGroupCH = 5;  // channels per lane half (row-group tasks)
+constexpr int kRows = 3;        // tile rows per lane (row-group tasks; 2 measured 12 % slower)
+
+template <typename Kernel>
+int launch_spread_kernel(Kernel kernel, const char *name, size_t smem, const SpreadParams &a, int64_t max_blocks,
+                         cudaStream_t st) {
   if (smem > 227 * 1024) {
     set_error("spreading stage of %zu bytes exceeds shared memory", smem);
     return COV3D_EINVAL;
   }
-  if (smem > 32 * 1024) {  // static shared arrays come on top of the dynamic size
-    cudaError_t e = cudaFuncSetAttribute(spread_kernel<KT, W, CPL, COMP, RP>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return check_cuda(e, "cudaFuncSetAttribute(spread_kernel)");
+  if (smem > 32 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return check_cuda(e, "cudaFuncSetAttribute(spread)");
   }
-  spread_kernel<KT, W, CPL, COMP, RP><<<(unsigned)max_blocks, kSpreadWarps * 32, smem, st>>>(a);
-  return launched("spread_kernel");
+  kernel<<<(unsigned)max_blocks, kSpreadWarps * 32, smem, st>>>(a);
+  return launched(name);
 }
 
 // One launch for all channels: the block sorts and stages its points once.  With three or more
-// channel pairs, row-pair tasks with every lane holding kRowPairCPL pairs (groups of that many);
-// otherwise row tasks with the pairs spread over lane groups.
+// channel pairs, row-group tasks over two lane halves of kRowGroupCH channels (groups of
+// 2 * kRowGroupCH channels); otherwise row tasks with the (at most two, G >= 2) pairs spread
+// over the lane groups.
 template <int KT, int W, bool COMP>
 int launch_wc(SpreadParams a, int nchan, int64_t max_blocks, cudaStream_t st) {
+  constexpr int T = kBin + W - 1;
   constexpr int G = SpreadLanes<W>::G;
   a.ch0 = 0;
   a.nch = nchan;
   const int npairs = (nchan + 1) / 2;
-  if (npairs >= 3 && 2 * SpreadLanes<W>::T <= 32) return launch_one<KT, W, kRowPairCPL, COMP, true>(a, max_blocks, st);
-  const int cpl = (npairs + G - 1) / G;
-  if (cpl <= 1) return launch_one<KT, W, 1, COMP, false>(a, max_blocks, st);
-  if (cpl == 2) return launch_one<KT, W, 2, COMP, false>(a, max_blocks, st);
-  return launch_one<KT, W, kMaxCPL, COMP, false>(a, max_blocks, st);
+  if (npairs >= 3) {
+    constexpr int PS = 2 * ((kRowGroupCH + 1) / 2 * 2);
+    const size_t smem = (size_t)a.max_sub * PS * sizeof(float2) + stage_bytes(a.max_sub, T, PointRec<W, kRows>::F2);
+    return launch_spread_kernel(spread_rows_kernel<KT, W, kRowGroupCH, kRows, COMP>, "spread_rows_kernel", smem, a,
+                                max_blocks, st);
+  }
+  static_assert(2 * G >= 2, "at most two channel pairs spread over the lane groups");
+  const size_t smem = (size_t)a.max_sub * G * sizeof(float4) + stage_bytes(a.max_sub, T, PointRec<W, 1>::F2);
+  return launch_spread_kernel(spread_kernel<KT, W, 1, COMP>, "spread_kernel", smem, a, max_blocks, st);
 }
 
 template <int KT, int W>

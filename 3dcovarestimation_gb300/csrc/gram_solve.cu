@@ -260,35 +260,40 @@ __device__ __forceinline__ cd csub(cd a, cd b) { return {a.x - b.x, a.y - b.y}; 
 
 // In-place Cholesky m = L L^H of a Hermitian positive definite r x r matrix (lower triangle
 // written into m).  Returns log det m, or NaN if m is not numerically positive definite.
+// In-place Cholesky m = L L^H (lower triangle); returns log det m, NaN if m is not positive
+// definite.  The diagonal entry (k, k) holds {L_kk, 1 / L_kk}, so the triangular solves
+// multiply instead of dividing.
 __device__ double chol_logdet(cd *m, int r) {
   double logdet = 0.0;
   for (int k = 0; k < r; ++k) {
     double d = m[k * r + k].x;
     for (int j = 0; j < k; ++j) d -= m[k * r + j].x * m[k * r + j].x + m[k * r + j].y * m[k * r + j].y;
     if (!(d > 0.0)) return __longlong_as_double(0x7ff8000000000000ULL);
-    const double lkk = sqrt(d);
-    m[k * r + k] = {lkk, 0.0};
+    const double lkk = sqrt(d), inv = 1.0 / lkk;
+    m[k * r + k] = {lkk, inv};
     logdet += 2.0 * log(lkk);
     for (int i = k + 1; i < r; ++i) {
       cd s = m[i * r + k];
       for (int j = 0; j < k; ++j) s = csub(s, cmul(m[i * r + j], cconj(m[k * r + j])));
-      m[i * r + k] = {s.x / lkk, s.y / lkk};
+      m[i * r + k] = {s.x * inv, s.y * inv};
     }
   }
   return logdet;
 }
 
-// Solve (L L^H) x = rhs in place.
+// Solve (L L^H) x = rhs in place, L from chol_logdet.
 __device__ void chol_solve(const cd *Lm, int r, cd *x) {
   for (int i = 0; i < r; ++i) {
     cd s = x[i];
     for (int j = 0; j < i; ++j) s = csub(s, cmul(Lm[i * r + j], x[j]));
-    x[i] = {s.x / Lm[i * r + i].x, s.y / Lm[i * r + i].x};
+    const double inv = Lm[i * r + i].y;
+    x[i] = {s.x * inv, s.y * inv};
   }
   for (int i = r - 1; i >= 0; --i) {
     cd s = x[i];
     for (int j = i + 1; j < r; ++j) s = csub(s, cmul(cconj(Lm[j * r + i]), x[j]));
-    x[i] = {s.x / Lm[i * r + i].x, s.y / Lm[i * r + i].x};
+    const double inv = Lm[i * r + i].y;
+    x[i] = {s.x * inv, s.y * inv};
   }
 }
 
@@ -310,10 +315,12 @@ struct SolveArgs {
   int *bad;            // set to 1 if a factorisation failed
 };
 
-// RMAX sizes the per-thread working arrays (local memory): the smallest class that holds r keeps
-// them small enough to stay in L1
+// Thread kc of image b.  Every one of the image's r threads factors m (the same arithmetic,
+// so the same bits) and solves for z; thread kc then writes column kc of C from column kc of
+// m^-1, and thread 0 the per-image outputs (cost, z, m, u).  RMAX sizes the per-thread
+// working arrays (local memory): the smallest class that holds r keeps them in L1.
 template <int RMAX>
-__device__ double solve_one(const SolveArgs &a, const int b) {
+__device__ double solve_one(const SolveArgs &a, const int b, const int kc) {
   const int r = a.r;
   cd m[RMAX * RMAX];
   cd z[RMAX];
@@ -330,7 +337,7 @@ __device__ double solve_one(const SolveArgs &a, const int b) {
       }
       bb[i] = {hb[i].x / a.s2, hb[i].y / a.s2};
     }
-    if (a.m_out) {
+    if (a.m_out && kc == 0) {
       for (int i = 0; i < r * r; ++i) a.m_out[(int64_t)b * r * r + i] = make_float2((float)m[i].x, (float)m[i].y);
     }
     const double logdet = chol_logdet(m, r);
@@ -343,25 +350,26 @@ __device__ double solve_one(const SolveArgs &a, const int b) {
     double bz = 0.0;
     for (int i = 0; i < r; ++i) bz += bb[i].x * z[i].x + bb[i].y * z[i].y;
     cost = 0.5 * (-bz + logdet);
-    if (a.z_out) {
+    if (a.z_out && kc == 0) {
       for (int i = 0; i < r; ++i) a.z_out[(int64_t)b * r + i] = make_float2((float)z[i].x, (float)z[i].y);
     }
     if (a.C) {
-      // columns of m^-1: solve m x = e_k; C_ij = (conj(minv_ij) + conj(z_i) z_j) / (2 s2)
+      // column kc of m^-1: solve m x = e_kc; C_ij = (conj(minv_ij) + conj(z_i) z_j) / (2 s2)
       const double f = a.wscale / (2.0 * a.s2);
-      cd col[kMaxRank];
-      for (int k = 0; k < r; ++k) {
-        for (int i = 0; i < r; ++i) col[i] = {i == k ? 1.0 : 0.0, 0.0};
-        chol_solve(m, r, col);  // col = minv[:, k]
-        for (int i = 0; i < r; ++i) {
-          const cd zz = cmul(cconj(z[i]), z[k]);
-          a.C[((int64_t)b * r + i) * r + k] = make_float2((float)((col[i].x + zz.x) * f), (float)((-col[i].y + zz.y) * f));
-        }
+      cd col[RMAX];
+      for (int i = 0; i < r; ++i) col[i] = {i == kc ? 1.0 : 0.0, 0.0};
+      chol_solve(m, r, col);
+      for (int i = 0; i < r; ++i) {
+        const cd zz = cmul(cconj(z[i]), z[kc]);
+        a.C[((int64_t)b * r + i) * r + kc] = make_float2((float)((col[i].x + zz.x) * f), (float)((-col[i].y + zz.y) * f));
       }
-      for (int i = 0; i < r; ++i) a.u[(int64_t)b * r + i] = make_float2((float)(-z[i].x * f), (float)(z[i].y * f));
+      if (kc == 0) {
+        for (int i = 0; i < r; ++i) a.u[(int64_t)b * r + i] = make_float2((float)(-z[i].x * f), (float)(z[i].y * f));
+      }
     }
   } else {
-    // least squares
+    // least squares (thread 0 of the image)
+    if (kc != 0) return 0.0;
     double t2 = 0.0, fro = 0.0, tr = 0.0;
     for (int i = 0; i < r; ++i) {
       t2 += (double)hb[i].x * hb[i].x + (double)hb[i].y * hb[i].y;
@@ -382,25 +390,30 @@ __device__ double solve_one(const SolveArgs &a, const int b) {
       }
     }
   }
+  if (kc != 0) return 0.0;
   cost *= a.cscale;
   if (a.cost_b) a.cost_b[b] = cost;
   return cost;
 }
 
-// one thread per image; the images' costs are summed per block (one FP64 atomic per block
-// instead of one per image on the same address)
+constexpr int kSolveThreads = 128;
+
+// r threads per image, kSolveThreads / r images per block; the images' costs are summed per
+// block (one FP64 atomic per block instead of one per image on the same address)
 template <int RMAX>
-__global__ void solve_kernel(const SolveArgs a) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  double cost = b < a.B ? solve_one<RMAX>(a, b) : 0.0;
+__global__ void __launch_bounds__(kSolveThreads) solve_kernel(const SolveArgs a) {
+  const int ipb = kSolveThreads / a.r;
+  const int b = blockIdx.x * ipb + threadIdx.x / a.r;
+  const int kc = threadIdx.x - (threadIdx.x / a.r) * a.r;
+  double cost = (threadIdx.x < ipb * a.r && b < a.B) ? solve_one<RMAX>(a, b, kc) : 0.0;
   if (!a.cost_sum) return;
   for (int o = 16; o > 0; o >>= 1) cost += __shfl_xor_sync(0xffffffffu, cost, o);
-  __shared__ double wsum[32];
+  __shared__ double wsum[kSolveThreads / 32];
   if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = cost;
   __syncthreads();
   if (threadIdx.x == 0) {
     double t = 0.0;
-    for (int i = 0; i < (int)((blockDim.x + 31) >> 5); ++i) t += wsum[i];
+    for (int i = 0; i < kSolveThreads / 32; ++i) t += wsum[i];
     atomicAdd(a.cost_sum, t);
   }
 }
@@ -554,13 +567,15 @@ int launch_solve(cudaStream_t st, int B, int r, int objective, const void *gram,
   sa.z_out = static_cast<float2 *>(z);
   sa.m_out = static_cast<float2 *>(m);
   sa.bad = bad;
-  const unsigned blocks = (unsigned)((B + 31) / 32);
+  static_assert(kMaxRank <= kSolveThreads, "one thread per column of every image");
+  const int ipb = kSolveThreads / r;
+  const unsigned blocks = (unsigned)((B + ipb - 1) / ipb);
   if (r <= 10) {
-    solve_kernel<10><<<blocks, 32, 0, st>>>(sa);
+    solve_kernel<10><<<blocks, kSolveThreads, 0, st>>>(sa);
   } else if (r <= 16) {
-    solve_kernel<16><<<blocks, 32, 0, st>>>(sa);
+    solve_kernel<16><<<blocks, kSolveThreads, 0, st>>>(sa);
   } else {
-    solve_kernel<kMaxRank><<<blocks, 32, 0, st>>>(sa);
+    solve_kernel<kMaxRank><<<blocks, kSolveThreads, 0, st>>>(sa);
   }
   return launched("solve_kernel");
 }

@@ -43,7 +43,7 @@ __device__ __forceinline__ float prologue(const PointGeom &g, int64_t id, const 
 
 constexpr int kLMin = -8;   // window corners relative to the bin lie in [kLMin, kLMin + 16)
 constexpr int kKeys = 256;  // sort key (l1 - kLMin) * 16 + (l0 - kLMin)
-constexpr int kFoldRanges = 2;  // window-corner rows l1 summed in FP32 between compensated folds
+constexpr int kFoldRanges = 3;  // window-corner rows l1 summed in FP32 between compensated folds
 
 // Per-point record staged once per block, in float2 units (each weight twice, the operand of a
 // packed multiply): the axis-0 weights by tile plane and the axis-2 weights by tile column, zero

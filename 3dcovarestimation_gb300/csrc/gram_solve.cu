@@ -139,7 +139,6 @@ __host__ __device__ constexpr int tri_j(int k) {
 
 constexpr int kGramSubsets = 8;   // product subsets per image (2 warps each)
 constexpr int kGramLanes = 64;    // threads per subset, striding over the pixels
-constexpr int kGramRun = 32;      // pixels summed in plain FP32 before the Kahan update
 
 // part[KK] += conj(v[i]) * v[j] for product k = S + kGramSubsets * KK, indices fixed at
 // compile time so the pixel stays in registers
@@ -157,29 +156,35 @@ struct GramAcc {
   }
 };
 
-// One run of pixels for the products k = S, S + kGramSubsets, ... of this subset:
-// part[kk] += conj(v[i]) * v[j] with v the pixel's r projections and y (registers)
+// One staged chunk of pixels for the products k = S, S + kGramSubsets, ... of this subset:
+// part[kk] += conj(v[i]) * v[j] with v a pixel's r projections and y (row of R + 1 in shared
+// memory, read into registers)
 template <int R, int S, int PER>
-__device__ __forceinline__ void gram_run(const float2 *__restrict__ Qb, const float2 *__restrict__ Yb, int64_t q_ps,
-                                         int p0, int pend, int lane, float2 (&part)[PER]) {
+__device__ __forceinline__ void gram_chunk(const float2 *rows, int np, int lane, float2 (&part)[PER]) {
   constexpr int R1 = R + 1;
-  for (int p = p0 + lane; p < pend; p += kGramLanes) {
+  for (int p = lane; p < np; p += kGramLanes) {
     float2 v[R1];
 #pragma unroll
-    for (int i = 0; i < R; ++i) v[i] = Qb[(int64_t)p * q_ps + i];
-    v[R] = Yb[p];
+    for (int i = 0; i < R1; ++i) v[i] = rows[p * R1 + i];
     GramAcc<R1, S, 0, PER>::run(v, part);
   }
 }
 
-// Per-image Gram for the fused step's layout (point-major Q, channel stride 1): one block per
-// image, eight product subsets of two warps; each thread holds one pixel's r projections and y
-// in registers at a time.
+constexpr int kGramChunkPx = kGramSubsets * kGramLanes;  // pixels staged per chunk
+
+// Per-image Gram for the fused step's layout (point-major Q with r contiguous projections per
+// pixel): one block per image, eight product subsets of two warps.  Chunks of kGramChunkPx
+// pixels are staged in shared memory by coalesced 8-byte asynchronous copies (double-buffered)
+// as rows of r projections and y, 88 bytes apart at r = 10 so the subsets' 8-byte reads are
+// free of bank conflicts; every subset reads every pixel of the chunk from there, and each
+// thread adds its chunk sums to Kahan-compensated totals.
 template <int R>
 __global__ void __launch_bounds__(kGramSubsets * kGramLanes, 1) gram_pixel_kernel(
-    const float2 *__restrict__ Q, int64_t q_is, int64_t q_ps, const float2 *__restrict__ Y, int P,
-    float2 *__restrict__ gram, float2 *__restrict__ h, float *__restrict__ yy) {
+    const float2 *__restrict__ Q, int64_t q_is, const float2 *__restrict__ Y, int P, float2 *__restrict__ gram,
+    float2 *__restrict__ h, float *__restrict__ yy) {
   constexpr int R1 = R + 1, NPR = R1 * (R1 + 1) / 2, PER = (NPR + kGramSubsets - 1) / kGramSubsets;
+  constexpr int NT = kGramSubsets * kGramLanes;
+  extern __shared__ float2 srows[];  // 2 * kGramChunkPx * R1
   const int b = blockIdx.x;
   const int sub = threadIdx.x / kGramLanes, lane = threadIdx.x % kGramLanes;
   float2 sum[PER], comp[PER];
@@ -190,20 +195,44 @@ __global__ void __launch_bounds__(kGramSubsets * kGramLanes, 1) gram_pixel_kerne
   }
   const float2 *Qb = Q + (int64_t)b * q_is;
   const float2 *Yb = Y + (int64_t)b * P;
-  for (int p0 = 0; p0 < P; p0 += kGramLanes * kGramRun) {
+  auto stage = [&](int c, float2 *dst) {
+    const int p0 = c * kGramChunkPx, np = min(kGramChunkPx, P - p0);
+    const float2 *src = Qb + (int64_t)p0 * R;
+    for (int e = threadIdx.x; e < np * R; e += NT) {
+      const int p = e / R, i = e - p * R;
+      const unsigned d = (unsigned)__cvta_generic_to_shared(dst + p * R1 + i);
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src + e) : "memory");
+    }
+    for (int p = threadIdx.x; p < np; p += NT) {
+      const unsigned d = (unsigned)__cvta_generic_to_shared(dst + p * R1 + R);
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(Yb + p0 + p) : "memory");
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+  };
+  const int nchunks = (P + kGramChunkPx - 1) / kGramChunkPx;
+  stage(0, srows);
+  for (int c = 0; c < nchunks; ++c) {
+    const float2 *cur = srows + (c & 1) * kGramChunkPx * R1;
+    if (c + 1 < nchunks) {
+      stage(c + 1, srows + ((c + 1) & 1) * kGramChunkPx * R1);
+      asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+    } else {
+      asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    }
+    __syncthreads();
+    const int np = min(kGramChunkPx, P - c * kGramChunkPx);
     float2 part[PER];
 #pragma unroll
     for (int kk = 0; kk < PER; ++kk) part[kk] = make_float2(0.f, 0.f);
-    const int pend = min(P, p0 + kGramLanes * kGramRun);
     switch (sub) {
-      case 0: gram_run<R, 0, PER>(Qb, Yb, q_ps, p0, pend, lane, part); break;
-      case 1: gram_run<R, 1, PER>(Qb, Yb, q_ps, p0, pend, lane, part); break;
-      case 2: gram_run<R, 2, PER>(Qb, Yb, q_ps, p0, pend, lane, part); break;
-      case 3: gram_run<R, 3, PER>(Qb, Yb, q_ps, p0, pend, lane, part); break;
-      case 4: gram_run<R, 4, PER>(Qb, Yb, q_ps, p0, pend, lane, part); break;
-      case 5: gram_run<R, 5, PER>(Qb, Yb, q_ps, p0, pend, lane, part); break;
-      case 6: gram_run<R, 6, PER>(Qb, Yb, q_ps, p0, pend, lane, part); break;
-      default: gram_run<R, 7, PER>(Qb, Yb, q_ps, p0, pend, lane, part); break;
+      case 0: gram_chunk<R, 0, PER>(cur, np, lane, part); break;
+      case 1: gram_chunk<R, 1, PER>(cur, np, lane, part); break;
+      case 2: gram_chunk<R, 2, PER>(cur, np, lane, part); break;
+      case 3: gram_chunk<R, 3, PER>(cur, np, lane, part); break;
+      case 4: gram_chunk<R, 4, PER>(cur, np, lane, part); break;
+      case 5: gram_chunk<R, 5, PER>(cur, np, lane, part); break;
+      case 6: gram_chunk<R, 6, PER>(cur, np, lane, part); break;
+      default: gram_chunk<R, 7, PER>(cur, np, lane, part); break;
     }
 #pragma unroll
     for (int kk = 0; kk < PER; ++kk) {  // Kahan update of the running totals
@@ -214,6 +243,7 @@ __global__ void __launch_bounds__(kGramSubsets * kGramLanes, 1) gram_pixel_kerne
       comp[kk].y = (ty - sum[kk].y) - yv;
       sum[kk].y = ty;
     }
+    __syncthreads();  // the buffer is refilled next
   }
   // reduce over the 64 lanes of the subset: shuffles within each warp, then the two warps
   __shared__ float2 red[kGramSubsets][2][PER];
@@ -258,8 +288,6 @@ __device__ __forceinline__ cd cmul(cd a, cd b) { return {a.x * b.x - a.y * b.y, 
 __device__ __forceinline__ cd cconj(cd a) { return {a.x, -a.y}; }
 __device__ __forceinline__ cd csub(cd a, cd b) { return {a.x - b.x, a.y - b.y}; }
 
-// In-place Cholesky m = L L^H of a Hermitian positive definite r x r matrix (lower triangle
-// written into m).  Returns log det m, or NaN if m is not numerically positive definite.
 // In-place Cholesky m = L L^H (lower triangle); returns log det m, NaN if m is not positive
 // definite.  The diagonal entry (k, k) holds {L_kk, 1 / L_kk}, so the triangular solves
 // multiply instead of dividing.
@@ -507,8 +535,11 @@ int launch_gram(cudaStream_t st, int B, int P, int r, const void *q, int64_t is,
     return COV3D_EINVAL;
   }
   if (cs == 1 && ps == r && r == 10) {
-    gram_pixel_kernel<10><<<B, kGramSubsets * kGramLanes, 0, st>>>(
-        static_cast<const float2 *>(q), is, ps, static_cast<const float2 *>(images), P, static_cast<float2 *>(gram),
+    const size_t smem = 2 * (size_t)kGramChunkPx * (10 + 1) * sizeof(float2);
+    cudaError_t e = cudaFuncSetAttribute(gram_pixel_kernel<10>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return check_cuda(e, "cudaFuncSetAttribute(gram_pixel_kernel)");
+    gram_pixel_kernel<10><<<B, kGramSubsets * kGramLanes, smem, st>>>(
+        static_cast<const float2 *>(q), is, static_cast<const float2 *>(images), P, static_cast<float2 *>(gram),
         static_cast<float2 *>(h), yy);
     return launched("gram_pixel_kernel");
   }

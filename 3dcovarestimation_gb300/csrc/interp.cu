@@ -31,7 +31,7 @@ struct InterpParams {
 };
 
 constexpr int kBin = 8;
-constexpr int kInterpWarps = 16;
+constexpr int kInterpWarps = 24;  // 56 registers: 24 warps next to the one 190 KB tile per SM
 
 // Channel pairs per pass: lanes are (window cell, channel pair) pairs, so W * CP <= 32, and the
 // tile (bin + halo) of 2*CP complex channels must fit in shared memory.

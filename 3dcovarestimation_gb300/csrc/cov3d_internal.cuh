@@ -114,7 +114,7 @@ struct cov3d_plan {
   cov3d::DevBuf bin_count;     // int (nbins + 1), last = dead points
   cov3d::DevBuf bin_off;       // int (nbins + 2)
   cov3d::DevBuf sub_off;       // int (nbins + 1)
-  cov3d::DevBuf pt_bin, pt_rank, perm;        // int (M)
+  cov3d::DevBuf pt_bin, pt_rank;              // int (M)
   cov3d::DevBuf sorted;        // SortedPoint (M), bin-sorted order
   cov3d::DevBuf sub_bin, sub_first, sub_count;  // int (max subproblems)
   cov3d::DevBuf nsub;          // int scalar

@@ -114,12 +114,51 @@ __global__ void ml_reg_kernel(const float2 *__restrict__ grid, float2 *__restric
   const int64_t n3 = (int64_t)n * n * n;
   const int half = n / 2;
   const float cfs = (float)coef;
+  // 16-byte accesses need an even row length and 16-byte aligned grids
+  const bool vec = (n & 1) == 0 && ((reinterpret_cast<uintptr_t>(grid) | reinterpret_cast<uintptr_t>(gg)) & 15) == 0;
   double part = 0.0;
   for (int64_t row = blockIdx.x; row < (int64_t)n * n; row += gridDim.x) {
     int s0 = (int)(row / n), s1 = (int)(row - (int64_t)s0 * n);
     s0 = s0 + half >= n ? s0 + half - n : s0 + half;
     s1 = s1 + half >= n ? s1 + half - n : s1 + half;
     const float *frow = fr + ((int64_t)s0 * n + s1) * n;
+    if (vec) {  // two cells per thread, 16-byte loads, four channels' loads in flight
+      for (int s2 = 2 * threadIdx.x; s2 < n; s2 += 2 * blockDim.x) {
+        const int c2a = s2 + half >= n ? s2 + half - n : s2 + half;
+        const int c2b = s2 + 1 + half >= n ? s2 + 1 + half - n : s2 + 1 + half;
+        const float wa = __ldg(frow + c2a), wb = __ldg(frow + c2b);
+        const float cfa = cfs * wa, cfb = cfs * wb;
+        const int64_t cell = row * n + s2;
+        const float4 *src = reinterpret_cast<const float4 *>(grid + cell);
+        float4 *dst = reinterpret_cast<float4 *>(gg + cell);
+        const int64_t cstep = n3 / 2;  // one channel, in float4
+        float pa = 0.0f, pb = 0.0f;
+        int c = 0;
+        for (; c + 4 <= nchan; c += 4) {
+          float4 x[4], y[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) x[u] = __ldg(src + (c + u) * cstep);
+#pragma unroll
+          for (int u = 0; u < 4; ++u) y[u] = init ? make_float4(0.f, 0.f, 0.f, 0.f) : dst[(c + u) * cstep];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            dst[(c + u) * cstep] = make_float4(fmaf(cfa, x[u].x, y[u].x), fmaf(cfa, x[u].y, y[u].y),
+                                               fmaf(cfb, x[u].z, y[u].z), fmaf(cfb, x[u].w, y[u].w));
+            pa = fmaf(x[u].x, x[u].x, fmaf(x[u].y, x[u].y, pa));
+            pb = fmaf(x[u].z, x[u].z, fmaf(x[u].w, x[u].w, pb));
+          }
+        }
+        for (; c < nchan; ++c) {
+          const float4 x = __ldg(src + c * cstep);
+          const float4 y = init ? make_float4(0.f, 0.f, 0.f, 0.f) : dst[c * cstep];
+          dst[c * cstep] = make_float4(fmaf(cfa, x.x, y.x), fmaf(cfa, x.y, y.y), fmaf(cfb, x.z, y.z), fmaf(cfb, x.w, y.w));
+          pa = fmaf(x.x, x.x, fmaf(x.y, x.y, pa));
+          pb = fmaf(x.z, x.z, fmaf(x.w, x.w, pb));
+        }
+        part += (double)(wa * pa) + (double)(wb * pb);
+      }
+      continue;
+    }
     for (int s2 = threadIdx.x; s2 < n; s2 += blockDim.x) {
       const int c2 = s2 + half >= n ? s2 + half - n : s2 + half;
       const float w = __ldg(frow + c2);
@@ -183,7 +222,8 @@ int launch_unpack_grad(cov3d_plan *p, const void *fine, const float *vectors, co
   const int64_t L3 = (int64_t)p->L * p->L * p->L;
   const int64_t rows = (int64_t)p->L * p->L;
   (void)L3;
-  unpack_grad_kernel<<<(unsigned)(rows < 1216 ? rows : 1216), 256, 0, p->stream>>>(static_cast<const float2 *>(fine), vectors, log_scale,
+  const int threads = p->L >= 256 ? 256 : (p->L + 31) / 32 * 32;  // one voxel row per pass
+  unpack_grad_kernel<<<(unsigned)(rows < 2432 ? rows : 2432), threads, 0, p->stream>>>(static_cast<const float2 *>(fine), vectors, log_scale,
                                                          use_gc ? p->gc1d.as<float>() : nullptr, nchan, p->L, p->n,
                                                          grad_vec, grad_log_acc);
   return launched("unpack_grad_kernel");
@@ -193,9 +233,9 @@ int launch_ml_reg(cov3d_plan *p, const void *grid, void *ggrid, const float *fr,
                   double *cost_acc, int init) {
   const int64_t n3 = (int64_t)p->n * p->n * p->n;
   const int64_t rows = (int64_t)p->n * p->n;
-  const unsigned blocks = (unsigned)(rows < 1216 ? rows : 1216);
+  const unsigned blocks = (unsigned)(rows < 2432 ? rows : 2432);  // 16 blocks of 4 warps per SM
   (void)n3;
-  ml_reg_kernel<<<blocks, 256, 0, p->stream>>>(static_cast<const float2 *>(grid), static_cast<float2 *>(ggrid), fr,
+  ml_reg_kernel<<<blocks, 128, 0, p->stream>>>(static_cast<const float2 *>(grid), static_cast<float2 *>(ggrid), fr,
                                                nchan, p->n, coef, cost_acc, init);
   return launched("ml_reg_kernel");
 }

@@ -11,33 +11,46 @@ namespace cov3d {
 
 namespace {
 
+// Bin of every point (dead points, whose window misses the grid, go to bin nbins) and its
+// rank in the bin.  The lanes of a warp that share a bin (neighbouring pixels mostly do) take
+// their ranks from one atomic on the bin's counter, in lane order.
 template <int KT, int W>
 __global__ void bin_count_kernel(PointGeom g, KernelSpec k, Bins bins, int64_t M, int *__restrict__ count,
                                  int *__restrict__ pt_bin, int *__restrict__ pt_rank) {
   const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (id >= M) return;
-  float t[3];
-  point_index(g, id, t);
-  int b[3];
-  bool dead = false;
+  const bool valid = id < M;
+  int bin = -1;
+  if (valid) {
+    float t[3];
+    point_index(g, id, t);
+    int b[3];
+    bool dead = false;
 #pragma unroll
-  for (int d = 0; d < 3; ++d) {
-    int c0 = first_cell<KT, W>(t[d]);
-    if (!(t[d] == t[d])) {  // NaN coordinate: no contribution
-      dead = true;
-      c0 = 0;
+    for (int d = 0; d < 3; ++d) {
+      int c0 = first_cell<KT, W>(t[d]);
+      if (!(t[d] == t[d])) {  // NaN coordinate: no contribution
+        dead = true;
+        c0 = 0;
+      }
+      if (k.periodic) {
+        c0 = pmod(c0, g.n);
+      } else {
+        if (c0 + W - 1 < 0 || c0 > g.n - 1) dead = true;
+        c0 = min(max(c0, 0), g.n - 1);
+      }
+      b[d] = c0 / bins.bs[d];
     }
-    if (k.periodic) {
-      c0 = pmod(c0, g.n);
-    } else {
-      if (c0 + W - 1 < 0 || c0 > g.n - 1) dead = true;
-      c0 = min(max(c0, 0), g.n - 1);
-    }
-    b[d] = c0 / bins.bs[d];
+    bin = dead ? (int)bins.nbins : (b[0] * bins.nb[1] + b[1]) * bins.nb[2] + b[2];
   }
-  const int bin = dead ? (int)bins.nbins : (b[0] * bins.nb[1] + b[1]) * bins.nb[2] + b[2];
+  const unsigned grp = __match_any_sync(0xffffffffu, bin);
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(grp) - 1;
+  int base = 0;
+  if (valid && lane == leader) base = atomicAdd(count + bin, __popc(grp));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  if (!valid) return;
   pt_bin[id] = bin;
-  pt_rank[id] = atomicAdd(count + bin, 1);
+  pt_rank[id] = base + __popc(grp & ((1u << lane) - 1u));
 }
 
 // Single-block exclusive scans over the bin counts: point offsets, and subproblem offsets
@@ -84,11 +97,10 @@ __global__ void bin_scan_kernel(const int *__restrict__ count, int64_t nbins, in
 }
 
 __global__ void scatter_kernel(PointGeom g, int64_t M, const int *__restrict__ pt_bin, const int *__restrict__ pt_rank,
-                               const int *__restrict__ off, int *__restrict__ perm, SortedPoint *__restrict__ sorted) {
+                               const int *__restrict__ off, SortedPoint *__restrict__ sorted) {
   const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (id >= M) return;
   const int pos = off[pt_bin[id]] + pt_rank[id];
-  perm[pos] = (int)id;
   float t[3];
   point_index(g, id, t);
   SortedPoint sp;
@@ -135,7 +147,6 @@ int sort_points(cov3d_plan *p) {
   COV3D_TRY(grow(p->sub_off, (nb + 2) * 4));
   COV3D_TRY(grow(p->pt_bin, M * 4));
   COV3D_TRY(grow(p->pt_rank, M * 4));
-  COV3D_TRY(grow(p->perm, M * 4));
   COV3D_TRY(grow(p->sorted, M * (int64_t)sizeof(SortedPoint)));
   COV3D_TRY(grow(p->sub_bin, max_subs * 4));
   COV3D_TRY(grow(p->sub_first, max_subs * 4));
@@ -165,7 +176,7 @@ int sort_points(cov3d_plan *p) {
   bin_scan_kernel<<<1, 1024, 0, p->stream>>>(p->bin_count.as<int>(), nb, p->max_sub, p->bin_off.as<int>(), p->sub_off.as<int>(), p->nsub.as<int>());
   COV3D_LAUNCHED("bin_scan_kernel");
   scatter_kernel<<<blocks, 256, 0, p->stream>>>(g, M, p->pt_bin.as<int>(), p->pt_rank.as<int>(), p->bin_off.as<int>(),
-                                                p->perm.as<int>(), p->sorted.as<SortedPoint>());
+                                                p->sorted.as<SortedPoint>());
   COV3D_LAUNCHED("scatter_kernel");
   subproblem_kernel<<<(int)((nb + 255) / 256), 256, 0, p->stream>>>(nb, p->max_sub, p->bin_count.as<int>(), p->bin_off.as<int>(),
                                                                     p->sub_off.as<int>(), p->sub_bin.as<int>(), p->sub_first.as<int>(),

@@ -65,8 +65,10 @@ def cpu_baseline(args):
     from oracle import cpu_step
 
     threads = os.cpu_count()
-    # size the sample so the per-image part takes about cpu_seconds
-    _, probe = cpu_step.time_baseline(args.L, args.rank, args.batch, 2, args.width, real="float", threads=threads)
+    # a discarded warm-up call (thread pools, FFT plans), then a probe that sizes the sample so
+    # the per-image part takes about cpu_seconds
+    cpu_step.time_baseline(args.L, args.rank, args.batch, 2, args.width, real="float", threads=threads)
+    _, probe = cpu_step.time_baseline(args.L, args.rank, args.batch, 4, args.width, real="float", threads=threads)
     sample = int(max(2, min(256, args.cpu_seconds / max(probe["t_image_s"], 1e-6))))
     ips, det = cpu_step.time_baseline(args.L, args.rank, args.batch, sample, args.width, real="float",
                                       seed=args.seed, threads=threads)

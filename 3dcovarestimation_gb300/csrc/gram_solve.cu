@@ -605,6 +605,8 @@ int launch_solve(cudaStream_t st, int B, int r, int objective, const void *gram,
     solve_kernel<10><<<blocks, kSolveThreads, 0, st>>>(sa);
   } else if (r <= 16) {
     solve_kernel<16><<<blocks, kSolveThreads, 0, st>>>(sa);
+  } else if (r <= 20) {
+    solve_kernel<20><<<blocks, kSolveThreads, 0, st>>>(sa);
   } else {
     solve_kernel<kMaxRank><<<blocks, kSolveThreads, 0, st>>>(sa);
   }

@@ -126,6 +126,8 @@ struct cov3d_plan {
   cov3d::DevBuf acc;           // double accumulators
   cov3d::DevBuf cgw;           // mean / CG workspace (state, vectors, shell sums)
   cov3d::DevBuf xbf, gsum;     // BF16 Gram operands and real Gram sums
+  cov3d::DevBuf fftw;          // twiddles exp(-2 pi i j / fftw_n) of the fused axis-0 CG transform
+  int fftw_n = 0;
   double *h_acc = nullptr;     // pinned host mirror of acc (64 doubles)
   std::map<int, cufftHandle> *ffts = nullptr;  // cuFFT plans by channel count
 

@@ -14,6 +14,9 @@
 //      fine grid, the operator the reference uses for its starting point, mean.py:238-239)
 //   2: M r = ifft3_L(fft3_L(r) / s)                      (a Fourier diagonal on the L^3 grid:
 //      the optimal circulant approximation of A from cov3d_circulant_symbol, or a learned s)
+#include <cmath>
+#include <vector>
+
 #include "cov3d_device.cuh"
 
 namespace cov3d {
@@ -164,6 +167,176 @@ __global__ void fine_diag_kernel(float2 *__restrict__ g, const float *__restrict
       grow[s2] = make_float2(v.x * f, v.y * f);
     }
   }
+}
+
+// DFT of N values held in registers (natural order in, natural order out), recursive
+// decimation in time, radix 4 (radix 2 for the last factor when N is not a power of 4);
+// w[j] = exp(-2 pi i j / n) is the n-point twiddle table and STRIDE = n / N picks the N-point
+// twiddles from it; INV uses exp(+2 pi i j / n) (unnormalised, as cuFFT).
+__device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+template <int STRIDE, bool INV>
+__device__ __forceinline__ float2 twiddle(const float2 *w, int j) {
+  float2 t = w[j * STRIDE];
+  if (INV) t.y = -t.y;
+  return t;
+}
+
+template <int N, int STRIDE, bool INV>
+__device__ __forceinline__ void reg_dft(float2 *a, const float2 *w) {
+  if constexpr (N == 2) {
+    const float2 x = a[0], y = a[1];
+    a[0] = make_float2(x.x + y.x, x.y + y.y);
+    a[1] = make_float2(x.x - y.x, x.y - y.y);
+  } else if constexpr (N >= 4) {
+    constexpr int Q = N / 4;
+    float2 s0[Q], s1[Q], s2[Q], s3[Q];
+#pragma unroll
+    for (int i = 0; i < Q; ++i) {
+      s0[i] = a[4 * i];
+      s1[i] = a[4 * i + 1];
+      s2[i] = a[4 * i + 2];
+      s3[i] = a[4 * i + 3];
+    }
+    if constexpr (Q > 1) {
+      reg_dft<Q, 4 * STRIDE, INV>(s0, w);
+      reg_dft<Q, 4 * STRIDE, INV>(s1, w);
+      reg_dft<Q, 4 * STRIDE, INV>(s2, w);
+      reg_dft<Q, 4 * STRIDE, INV>(s3, w);
+    }
+#pragma unroll
+    for (int k = 0; k < Q; ++k) {
+      const float2 t0 = s0[k];
+      const float2 t1 = k == 0 ? s1[k] : cmulf(s1[k], twiddle<STRIDE, INV>(w, k));
+      const float2 t2 = k == 0 ? s2[k] : cmulf(s2[k], twiddle<STRIDE, INV>(w, 2 * k));
+      const float2 t3 = k == 0 ? s3[k] : cmulf(s3[k], twiddle<STRIDE, INV>(w, 3 * k));
+      const float2 a0 = make_float2(t0.x + t2.x, t0.y + t2.y), a1 = make_float2(t0.x - t2.x, t0.y - t2.y);
+      const float2 b0 = make_float2(t1.x + t3.x, t1.y + t3.y), b1 = make_float2(t1.x - t3.x, t1.y - t3.y);
+      // forward: X[k + Q] = a1 - i b1, X[k + 3Q] = a1 + i b1; the inverse swaps them
+      const float2 mib = INV ? make_float2(-b1.y, b1.x) : make_float2(b1.y, -b1.x);
+      a[k] = make_float2(a0.x + b0.x, a0.y + b0.y);
+      a[k + Q] = make_float2(a1.x + mib.x, a1.y + mib.y);
+      a[k + 2 * Q] = make_float2(a0.x - b0.x, a0.y - b0.y);
+      a[k + 3 * Q] = make_float2(a1.x - mib.x, a1.y - mib.y);
+    }
+  }
+}
+
+// The axis-0 part of the CG operator, fused: for every line (s1, s2) of an n^3 FFT-native grid
+// whose nonzero axis-0 entries are the support planes [0, L/2) and [n - L/2, n), the forward DFT
+// along axis 0, the multiply by diag (its reciprocal with `divide`; diag centred like
+// fine_diag_kernel's), the inverse DFT and the store of the support entries only, in place.
+// It replaces a cuFFT axis-0 transform, fine_diag_kernel and the inverse transform (three
+// passes over n^3 values) by one pass over the support half and the diagonal.
+// n = N1 * N2 by the four-step decomposition: index i0 = n1 + N1 n2, frequency k = k2 + N2 k1;
+// N2-point DFTs over n2 (thread n1), twiddle exp(-2 pi i n1 k2 / n), an exchange through shared
+// memory, N1-point DFTs over n1 (thread k2); the inverse mirrors it.  A block takes 256 / TPL
+// consecutive lines s2 of one s1, so every row of loads and stores is contiguous.
+template <int N1, int N2>
+__global__ void __launch_bounds__(256) axis0_diag_kernel(float2 *__restrict__ g, const float *__restrict__ diag,
+                                                         const float2 *__restrict__ tw, int L, int divide,
+                                                         const CgState *st) {
+  constexpr int n = N1 * N2;
+  constexpr int TPL = N1 > N2 ? N1 : N2;  // threads per line
+  constexpr int LPB = 256 / TPL;          // lines per block
+  constexpr int RA = N1 + 1;              // exchange row of the forward transform (padded)
+  constexpr int RB = N2 + 1;              // exchange row of the inverse transform (padded)
+  // per-line exchange stride: a half warp (16 lanes of 8-byte accesses) spans H = min(LPB, 16)
+  // lines and 16 / H roles, so lines must fall 16 / H banks-pairs apart: EX = 16 / H (mod 16)
+  constexpr int EX0 = N2 * RA > N1 * RB ? N2 * RA : N1 * RB;
+  constexpr int STEP = 16 / (LPB < 16 ? LPB : 16);
+  constexpr int EX = EX0 + ((STEP - EX0 % 16) % 16 + 16) % 16;
+  __shared__ float2 s_tw[n];
+  __shared__ float2 s_ex[LPB * EX];
+  if (stopped(st)) return;
+  for (int j = threadIdx.x; j < n; j += blockDim.x) s_tw[j] = tw[j];
+  const int l = threadIdx.x % LPB, role = threadIdx.x / LPB;
+  const int64_t line = (int64_t)blockIdx.x * LPB + l;  // s1 * n + s2
+  const int s1 = (int)(line / n), s2 = (int)(line - (int64_t)s1 * n);
+  const int64_t nn = (int64_t)n * n;
+  float2 *col = g + line;  // entry i0 of the line at col[i0 * nn]
+  const int h = L / 2;
+  float2 *ex = s_ex + l * EX;
+  __syncthreads();
+  if (role < N1) {  // forward, thread n1: N2-point DFT over n2 of x[n1 + N1 n2], twiddle, exchange
+    float2 v[N2];
+#pragma unroll
+    for (int n2 = 0; n2 < N2; ++n2) {
+      const int i0 = role + N1 * n2;
+      v[n2] = (i0 < h || i0 >= n - h) ? col[i0 * nn] : make_float2(0.f, 0.f);
+    }
+    reg_dft<N2, n / N2, false>(v, s_tw);
+#pragma unroll
+    for (int k2 = 0; k2 < N2; ++k2) ex[k2 * RA + role] = k2 == 0 ? v[0] : cmulf(v[k2], s_tw[role * k2]);
+  }
+  __syncthreads();
+  float2 u[N1];
+  if (role < N2) {
+#pragma unroll
+    for (int n1 = 0; n1 < N1; ++n1) u[n1] = ex[role * RA + n1];
+  }
+  __syncthreads();
+  if (role < N2) {  // thread k2: N1-point DFT over n1 gives X[k2 + N2 k1]; diagonal; inverse over k1
+    const float *dcol = diag + (int64_t)native_to_centered(s1, n) * n + native_to_centered(s2, n);
+    float d[N1];  // loaded before the transform, so their latency hides behind it
+#pragma unroll
+    for (int k1 = 0; k1 < N1; ++k1) d[k1] = __ldg(dcol + (int64_t)native_to_centered(role + N2 * k1, n) * nn);
+    reg_dft<N1, n / N1, false>(u, s_tw);
+#pragma unroll
+    for (int k1 = 0; k1 < N1; ++k1) {
+      const float f = divide ? 1.0f / d[k1] : d[k1];
+      u[k1] = make_float2(u[k1].x * f, u[k1].y * f);
+    }
+    reg_dft<N1, n / N1, true>(u, s_tw);  // u[m1] = sum_k1 X[k2 + N2 k1] exp(+2 pi i k1 m1 / N1)
+#pragma unroll
+    for (int m1 = 0; m1 < N1; ++m1) {
+      float2 t = s_tw[role * m1];
+      t.y = -t.y;
+      ex[m1 * RB + role] = m1 == 0 ? u[0] : cmulf(u[m1], t);
+    }
+  }
+  __syncthreads();
+  if (role < N1) {  // thread m1: inverse N2-point DFT over k2 gives x[m1 + N1 m2]; support rows only
+    float2 v[N2];
+#pragma unroll
+    for (int k2 = 0; k2 < N2; ++k2) v[k2] = ex[role * RB + k2];
+    reg_dft<N2, n / N2, true>(v, s_tw);
+#pragma unroll
+    for (int m2 = 0; m2 < N2; ++m2) {
+      const int i0 = role + N1 * m2;
+      if (i0 < h || i0 >= n - h) col[i0 * nn] = v[m2];
+    }
+  }
+}
+
+// The fused axis-0 transform for the grid sizes it is built for (n = 64 .. 512); returns false
+// (nothing launched) for others, which take cuFFT and fine_diag_kernel.
+bool axis0_fused_size(int n) { return n == 64 || n == 128 || n == 256 || n == 512; }
+
+int launch_axis0_diag(cov3d_plan *p, float2 *g, const float *diag, int L, int n, int divide, const CgState *gate) {
+  if (p->fftw_n != n) {
+    std::vector<float2> h(n);
+    for (int j = 0; j < n; ++j) {
+      const double a = 2.0 * 3.14159265358979323846 * (double)j / (double)n;
+      h[j] = make_float2((float)std::cos(a), (float)-std::sin(a));
+    }
+    COV3D_TRY(grow(p->fftw, (int64_t)n * sizeof(float2)));
+    COV3D_CUDA(cudaMemcpyAsync(p->fftw.ptr, h.data(), n * sizeof(float2), cudaMemcpyHostToDevice, p->stream));
+    COV3D_CUDA(cudaStreamSynchronize(p->stream));  // h goes out of scope
+    p->fftw_n = n;
+  }
+  const float2 *tw = p->fftw.as<float2>();
+  const int64_t lines = (int64_t)n * n;
+  switch (n) {
+    case 64: axis0_diag_kernel<8, 8><<<(unsigned)(lines / 32), 256, 0, p->stream>>>(g, diag, tw, L, divide, gate); break;
+    case 128: axis0_diag_kernel<16, 8><<<(unsigned)(lines / 16), 256, 0, p->stream>>>(g, diag, tw, L, divide, gate); break;
+    case 256: axis0_diag_kernel<16, 16><<<(unsigned)(lines / 16), 256, 0, p->stream>>>(g, diag, tw, L, divide, gate); break;
+    case 512: axis0_diag_kernel<32, 16><<<(unsigned)(lines / 8), 256, 0, p->stream>>>(g, diag, tw, L, divide, gate); break;
+    default: set_error("no fused axis-0 transform for n = %d", n); return COV3D_EINVAL;
+  }
+  return launched("axis0_diag_kernel");
 }
 
 // out = crop(fine) / n^3; optionally keep only the real part; optionally accumulate <p, out>
@@ -492,7 +665,7 @@ int regularize_lhs(cov3d_plan *p, const void *d_lhs, float *d_out) {
 
 int mean_init(cov3d_plan *p, const void *d_rhs, const float *d_reg, void *d_b, void *d_x0) {
   const int L = p->L, n = p->n;
-  const int64_t n3 = (int64_t)n * n * n, L3 = (int64_t)L * L * L;
+  const int64_t n3 = (int64_t)n * n * n;
   COV3D_TRY(grow(p->fine, n3 * 8));
   float2 *fine = p->fine.as<float2>();
   cufftHandle h;
@@ -555,12 +728,17 @@ int cg_solve(cov3d_plan *p, const float *d_lhs, const void *d_b, void *d_x, doub
   // kept): 2D FFTs over the support planes and an out-of-place 1D FFT along axis 0 into `full`,
   // whose other planes the 2D inverse never needs; `fine` keeps zeros off its support planes
   const bool pruned = (L % 2 == 0) && n >= L + 2;
+  // with pruning and a grid size the fused axis-0 kernel covers, the axis-0 transforms and the
+  // diagonal are one in-place pass over the support planes of `fine`
+  const bool fused = pruned && axis0_fused_size(n);
   float2 *full = fine;
   if (pruned) {
-    COV3D_TRY(grow(p->fine2, n3 * 8));
-    full = p->fine2.as<float2>();
+    if (!fused) {
+      COV3D_TRY(grow(p->fine2, n3 * 8));
+      full = p->fine2.as<float2>();
+      COV3D_TRY(get_fft_axis0(p, &h0));
+    }
     COV3D_TRY(get_fft_planes(p, &hp));
-    COV3D_TRY(get_fft_axis0(p, &h0));
     COV3D_CUDA(cudaMemsetAsync(fine, 0, (size_t)n3 * 8, s));
   }
   const int64_t half_off = (int64_t)(n - L / 2) * n * n;  // second block of support planes
@@ -568,6 +746,18 @@ int cg_solve(cov3d_plan *p, const float *d_lhs, const void *d_b, void *d_x, doub
 
   // out = crop(ifft3(diag^(+-1) * fft3(pad(in)))), with <p, out> into st->pap when dotp is given
   auto apply_op = [&](const float2 *in, float2 *out, int divide, const float2 *dotp, const CgState *gate) -> int {
+    if (fused) {
+      pad_support_kernel<<<capped((int64_t)L * n), 256, 0, s>>>(in, L, n, fine, gate);
+      COV3D_LAUNCHED("pad_support_kernel");
+      COV3D_TRY(fft2(hp, fine, fine, CUFFT_FORWARD));
+      COV3D_TRY(fft2(hp, fine + half_off, fine + half_off, CUFFT_FORWARD));
+      COV3D_TRY(launch_axis0_diag(p, fine, d_lhs, L, n, divide, gate));
+      COV3D_TRY(fft2(hp, fine, fine, CUFFT_INVERSE));
+      COV3D_TRY(fft2(hp, fine + half_off, fine + half_off, CUFFT_INVERSE));
+      crop_kernel<<<capped((int64_t)L * L), 256, 0, s>>>(fine, L, n, out, 0, dotp,
+                                                          dotp ? st : const_cast<CgState *>(gate));
+      return launched("crop_kernel");
+    }
     if (pruned) {
       pad_support_kernel<<<capped((int64_t)L * n), 256, 0, s>>>(in, L, n, fine, gate);
       COV3D_LAUNCHED("pad_support_kernel");

@@ -226,8 +226,10 @@ __device__ __forceinline__ void reg_dft(float2 *a, const float2 *w) {
 
 // The axis-0 part of the CG operator, fused: for every line (s1, s2) of an n^3 FFT-native grid
 // whose nonzero axis-0 entries are the support planes [0, L/2) and [n - L/2, n), the forward DFT
-// along axis 0, the multiply by diag (its reciprocal with `divide`; diag centred like
+// along axis 0, the multiply by scale * diag (scale / diag with `divide`; diag centred like
 // fine_diag_kernel's), the inverse DFT and the store of the support entries only, in place.
+// L >= 2n makes every plane a support plane (a full transform, for the L^3 preconditioner).
+// The twiddles are every tw_step-th entry of a larger table.
 // It replaces a cuFFT axis-0 transform, fine_diag_kernel and the inverse transform (three
 // passes over n^3 values) by one pass over the support half and the diagonal.
 // n = N1 * N2 by the four-step decomposition: index i0 = n1 + N1 n2, frequency k = k2 + N2 k1;
@@ -236,8 +238,8 @@ __device__ __forceinline__ void reg_dft(float2 *a, const float2 *w) {
 // consecutive lines s2 of one s1, so every row of loads and stores is contiguous.
 template <int N1, int N2>
 __global__ void __launch_bounds__(256) axis0_diag_kernel(float2 *__restrict__ g, const float *__restrict__ diag,
-                                                         const float2 *__restrict__ tw, int L, int divide,
-                                                         const CgState *st) {
+                                                         const float2 *__restrict__ tw, int tw_step, int L,
+                                                         int divide, float scale, const CgState *st) {
   constexpr int n = N1 * N2;
   constexpr int TPL = N1 > N2 ? N1 : N2;  // threads per line
   constexpr int LPB = 256 / TPL;          // lines per block
@@ -251,7 +253,7 @@ __global__ void __launch_bounds__(256) axis0_diag_kernel(float2 *__restrict__ g,
   __shared__ float2 s_tw[n];
   __shared__ float2 s_ex[LPB * EX];
   if (stopped(st)) return;
-  for (int j = threadIdx.x; j < n; j += blockDim.x) s_tw[j] = tw[j];
+  for (int j = threadIdx.x; j < n; j += blockDim.x) s_tw[j] = tw[j * tw_step];
   const int l = threadIdx.x % LPB, role = threadIdx.x / LPB;
   const int64_t line = (int64_t)blockIdx.x * LPB + l;  // s1 * n + s2
   const int s1 = (int)(line / n), s2 = (int)(line - (int64_t)s1 * n);
@@ -286,7 +288,7 @@ __global__ void __launch_bounds__(256) axis0_diag_kernel(float2 *__restrict__ g,
     reg_dft<N1, n / N1, false>(u, s_tw);
 #pragma unroll
     for (int k1 = 0; k1 < N1; ++k1) {
-      const float f = divide ? 1.0f / d[k1] : d[k1];
+      const float f = divide ? scale / d[k1] : scale * d[k1];
       u[k1] = make_float2(u[k1].x * f, u[k1].y * f);
     }
     reg_dft<N1, n / N1, true>(u, s_tw);  // u[m1] = sum_k1 X[k2 + N2 k1] exp(+2 pi i k1 m1 / N1)
@@ -315,25 +317,30 @@ __global__ void __launch_bounds__(256) axis0_diag_kernel(float2 *__restrict__ g,
 // (nothing launched) for others, which take cuFFT and fine_diag_kernel.
 bool axis0_fused_size(int n) { return n == 64 || n == 128 || n == 256 || n == 512; }
 
-int launch_axis0_diag(cov3d_plan *p, float2 *g, const float *diag, int L, int n, int divide, const CgState *gate) {
-  if (p->fftw_n != n) {
-    std::vector<float2> h(n);
-    for (int j = 0; j < n; ++j) {
-      const double a = 2.0 * 3.14159265358979323846 * (double)j / (double)n;
+int launch_axis0_diag(cov3d_plan *p, float2 *g, const float *diag, int L, int n, int divide, float scale,
+                      const CgState *gate) {
+  // one twiddle table of the plan's fine size serves the fine operator and the L^3
+  // preconditioner (every (fine n / n)-th entry)
+  const int tn = p->n % n == 0 ? p->n : n;
+  if (p->fftw_n != tn) {
+    std::vector<float2> h(tn);
+    for (int j = 0; j < tn; ++j) {
+      const double a = 2.0 * 3.14159265358979323846 * (double)j / (double)tn;
       h[j] = make_float2((float)std::cos(a), (float)-std::sin(a));
     }
-    COV3D_TRY(grow(p->fftw, (int64_t)n * sizeof(float2)));
-    COV3D_CUDA(cudaMemcpyAsync(p->fftw.ptr, h.data(), n * sizeof(float2), cudaMemcpyHostToDevice, p->stream));
+    COV3D_TRY(grow(p->fftw, (int64_t)tn * sizeof(float2)));
+    COV3D_CUDA(cudaMemcpyAsync(p->fftw.ptr, h.data(), tn * sizeof(float2), cudaMemcpyHostToDevice, p->stream));
     COV3D_CUDA(cudaStreamSynchronize(p->stream));  // h goes out of scope
-    p->fftw_n = n;
+    p->fftw_n = tn;
   }
   const float2 *tw = p->fftw.as<float2>();
+  const int ts = tn / n;
   const int64_t lines = (int64_t)n * n;
   switch (n) {
-    case 64: axis0_diag_kernel<8, 8><<<(unsigned)(lines / 32), 256, 0, p->stream>>>(g, diag, tw, L, divide, gate); break;
-    case 128: axis0_diag_kernel<16, 8><<<(unsigned)(lines / 16), 256, 0, p->stream>>>(g, diag, tw, L, divide, gate); break;
-    case 256: axis0_diag_kernel<16, 16><<<(unsigned)(lines / 16), 256, 0, p->stream>>>(g, diag, tw, L, divide, gate); break;
-    case 512: axis0_diag_kernel<32, 16><<<(unsigned)(lines / 8), 256, 0, p->stream>>>(g, diag, tw, L, divide, gate); break;
+    case 64: axis0_diag_kernel<8, 8><<<(unsigned)(lines / 32), 256, 0, p->stream>>>(g, diag, tw, ts, L, divide, scale, gate); break;
+    case 128: axis0_diag_kernel<16, 8><<<(unsigned)(lines / 16), 256, 0, p->stream>>>(g, diag, tw, ts, L, divide, scale, gate); break;
+    case 256: axis0_diag_kernel<16, 16><<<(unsigned)(lines / 16), 256, 0, p->stream>>>(g, diag, tw, ts, L, divide, scale, gate); break;
+    case 512: axis0_diag_kernel<32, 16><<<(unsigned)(lines / 8), 256, 0, p->stream>>>(g, diag, tw, ts, L, divide, scale, gate); break;
     default: set_error("no fused axis-0 transform for n = %d", n); return COV3D_EINVAL;
   }
   return launched("axis0_diag_kernel");
@@ -617,6 +624,20 @@ static int get_fft_coarse(cov3d_plan *p, cufftHandle *out) {
   return check_cufft(cufftSetStream(it->second, p->stream), "cufftSetStream");
 }
 
+// 2D transforms of the L planes (axes 1, 2) of an L^3 volume
+static int get_fft_coarse_planes(cov3d_plan *p, cufftHandle *out) {
+  auto it = p->ffts->find(-4);
+  if (it == p->ffts->end()) {
+    cufftHandle h;
+    int dims[2] = {p->L, p->L};
+    COV3D_TRY(check_cufft(cufftPlanMany(&h, 2, dims, nullptr, 1, p->L * p->L, nullptr, 1, p->L * p->L, CUFFT_C2C, p->L),
+                          "cufftPlanMany(coarse planes)"));
+    it = p->ffts->emplace(-4, h).first;
+  }
+  *out = it->second;
+  return check_cufft(cufftSetStream(it->second, p->stream), "cufftSetStream");
+}
+
 static int fft(cufftHandle h, float2 *g, int dir) {
   return check_cufft(cufftExecC2C(h, reinterpret_cast<cufftComplex *>(g), reinterpret_cast<cufftComplex *>(g), dir),
                      "cufftExecC2C");
@@ -723,7 +744,12 @@ int cg_solve(cov3d_plan *p, const float *d_lhs, const void *d_b, void *d_x, doub
   cudaStream_t s = p->stream;
   cufftHandle h, hc = 0, hp = 0, h0 = 0;
   COV3D_TRY(get_fft(p, 1, &h));
-  if (precond == 2) COV3D_TRY(get_fft_coarse(p, &hc));
+  // the L^3 preconditioner: 2D transforms of the L planes around the fused axis-0 kernel where
+  // it covers L, else a cuFFT 3D transform and fine_diag_kernel
+  const bool coarse_fused = precond == 2 && axis0_fused_size(L);
+  cufftHandle hcp = 0;
+  if (coarse_fused) COV3D_TRY(get_fft_coarse_planes(p, &hcp));
+  else if (precond == 2) COV3D_TRY(get_fft_coarse(p, &hc));
   // even L: pruned transforms (the input has L nonzero planes, only L planes of the output are
   // kept): 2D FFTs over the support planes and an out-of-place 1D FFT along axis 0 into `full`,
   // whose other planes the 2D inverse never needs; `fine` keeps zeros off its support planes
@@ -751,7 +777,7 @@ int cg_solve(cov3d_plan *p, const float *d_lhs, const void *d_b, void *d_x, doub
       COV3D_LAUNCHED("pad_support_kernel");
       COV3D_TRY(fft2(hp, fine, fine, CUFFT_FORWARD));
       COV3D_TRY(fft2(hp, fine + half_off, fine + half_off, CUFFT_FORWARD));
-      COV3D_TRY(launch_axis0_diag(p, fine, d_lhs, L, n, divide, gate));
+      COV3D_TRY(launch_axis0_diag(p, fine, d_lhs, L, n, divide, 1.0f, gate));
       COV3D_TRY(fft2(hp, fine, fine, CUFFT_INVERSE));
       COV3D_TRY(fft2(hp, fine + half_off, fine + half_off, CUFFT_INVERSE));
       crop_kernel<<<capped((int64_t)L * L), 256, 0, s>>>(fine, L, n, out, 0, dotp,
@@ -788,6 +814,11 @@ int cg_solve(cov3d_plan *p, const float *d_lhs, const void *d_b, void *d_x, doub
   // z = M(r)
   auto apply_M = [&](const float2 *in, float2 *out, const CgState *gate) -> int {
     if (precond == 1) return apply_op(in, out, 1, nullptr, gate);
+    if (coarse_fused) {
+      COV3D_TRY(fft2(hcp, in, out, CUFFT_FORWARD));
+      COV3D_TRY(launch_axis0_diag(p, out, d_sym, 2 * L, L, 1, 1.0f / (float)L3, gate));
+      return fft2(hcp, out, out, CUFFT_INVERSE);
+    }
     copy_kernel<<<nb(L3), 256, 0, s>>>(in, out, L3);
     COV3D_LAUNCHED("copy_kernel");
     COV3D_TRY(fft(hc, out, CUFFT_FORWARD));

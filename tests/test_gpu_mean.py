@@ -147,19 +147,26 @@ def test_cg_reports_maxiter(pkg, dev):
     assert np.isfinite(info.relres) and info.relres > 1e-12
 
 
-@pytest.mark.parametrize("L,precond", [(32, None), (32, "diagonal"), (64, None), (64, "diagonal"), (128, None)])
+@pytest.mark.parametrize("L,precond", [(32, None), (32, "diagonal"), (64, None), (64, "diagonal"), (64, "symbol"),
+                                       (128, None), (128, "symbol")])
 def test_cg_iterates_match_oracle_on_fused_grids(pkg, dev, L, precond):
     """Grids of n = 64, 128, 256 take the fused axis-0 transform (four-step FFT, diagonal,
-    inverse in one kernel): three CG iterations from zero against the float64 oracle's."""
+    inverse in one kernel), and so do the L^3 preconditioner's transforms at L = 64, 128: three
+    CG iterations from zero against the float64 oracle's."""
     rng = np.random.default_rng(L)
     n = 2 * L
     reg = rng.uniform(0.5, 3.0, (n, n, n))
     b = (rng.standard_normal((L, L, L)) + 1j * rng.standard_normal((L, L, L))).reshape(-1)
     A = O.padding_operator(reg, L)
-    M = O.fine_diagonal_preconditioner(reg, L) if precond == "diagonal" else None
+    M, pc = None, precond
+    if precond == "diagonal":
+        M = O.fine_diagonal_preconditioner(reg, L)
+    elif precond == "symbol":
+        sym = rng.uniform(0.5, 3.0, (L, L, L))
+        M, pc = O.circulant_preconditioner(sym), T(sym, dev, torch.float32)
     ref, _, _ = O.conjugate_gradient(A, b, x0=np.zeros_like(b), rtol=1e-12, maxiter=3, precond=M)
     x, info = pkg.cg_solve(T(reg, dev, torch.float32), T(b, dev, torch.complex64),
                            torch.zeros(L**3, dtype=torch.complex64, device=dev), L, rtol=1e-12, maxiter=3,
-                           precond=precond)
+                           precond=pc)
     assert not info.converged and info.iters == 2
     assert rel(x.reshape(-1), ref) < TOL_CG

@@ -313,28 +313,145 @@ __global__ void __launch_bounds__(256) axis0_diag_kernel(float2 *__restrict__ g,
   }
 }
 
+// One n-point DFT per line by the same four-step decomposition as axis0_diag_kernel: element
+// i = n1 + N1 n2 comes from load(i) (thread n1), the result X[k], k = k2 + N2 k1, goes to
+// store(k, X) (thread k2).  ex is the line's exchange area (N2 (N1 + 1) values); every thread
+// of the block calls it (it synchronises the block).
+template <int N1, int N2, bool INV, typename Load, typename Store>
+__device__ __forceinline__ void line_dft(float2 *ex, const float2 *s_tw, int role, Load load, Store store) {
+  constexpr int n = N1 * N2;
+  constexpr int RA = N1 + 1;
+  if (role < N1) {
+    float2 v[N2];
+#pragma unroll
+    for (int n2 = 0; n2 < N2; ++n2) v[n2] = load(role + N1 * n2);
+    reg_dft<N2, n / N2, INV>(v, s_tw);
+#pragma unroll
+    for (int k2 = 0; k2 < N2; ++k2) ex[k2 * RA + role] = k2 == 0 ? v[0] : cmulf(v[k2], twiddle<1, INV>(s_tw, role * k2));
+  }
+  __syncthreads();
+  if (role < N2) {
+    float2 u[N1];
+#pragma unroll
+    for (int n1 = 0; n1 < N1; ++n1) u[n1] = ex[role * RA + n1];
+    reg_dft<N1, n / N1, INV>(u, s_tw);
+#pragma unroll
+    for (int k1 = 0; k1 < N1; ++k1) store(role + N2 * k1, u[k1]);
+  }
+}
+
+// support plane / row t in [0, L) of an axis of the fine grid (FFT-native storage)
+__device__ __forceinline__ int support_index(int t, int L, int n) { return t < L / 2 ? t : n - L + t; }
+__device__ __forceinline__ bool in_support(int s, int L, int n) { return s < L / 2 || s >= n - L / 2; }
+
+// The pruned transforms of the CG operator around axis0_diag_kernel, as line DFTs of the fine
+// grid (n = N1 N2, FFT-native storage, a voxel j of the L^3 volume at index voxel_store(j)):
+//   kRowFwd: rows (s0, s1) of support planes and rows: the volume row zero-padded, DFT along
+//            axis 2, the whole row written (pad fused);
+//   kColFwd: columns (s0, s2) of support planes: the support entries, DFT along axis 1, the whole
+//            column written;
+//   kColInv: the inverse along axis 1, support entries written;
+//   kRowInv: the inverse along axis 2, the L support entries / n^3 written to the volume (crop
+//            fused), with <p, out> into st->pap when p is given.
+// Every kernel writes exactly what the next reads, so the grid needs no zeroing.  Rows are
+// contiguous (a line's threads are adjacent lanes); columns are n apart (a block takes
+// consecutive columns, adjacent lanes on adjacent columns).
+enum { kRowFwd = 0, kColFwd = 1, kColInv = 2, kRowInv = 3 };
+
+template <int N1, int N2, int KIND>
+__global__ void __launch_bounds__(256) cg_line_kernel(const float2 *__restrict__ vol, float2 *__restrict__ g,
+                                                      float2 *__restrict__ out, const float2 *__restrict__ p,
+                                                      const float2 *__restrict__ tw, int L, CgState *st) {
+  constexpr int n = N1 * N2;
+  constexpr int TPL = N1 > N2 ? N1 : N2;
+  constexpr int LPB = 256 / TPL;
+  constexpr bool ROWS = KIND == kRowFwd || KIND == kRowInv;
+  constexpr int RA = N1 + 1;
+  // exchange stride per line: with columns a half warp spans min(LPB, 16) lines (see
+  // axis0_diag_kernel); with rows (TPL >= 16) it stays within one line
+  constexpr int EX0 = N2 * RA;
+  constexpr int STEP = 16 / (LPB < 16 ? LPB : 16);
+  constexpr int EX = ROWS ? EX0 : EX0 + ((STEP - EX0 % 16) % 16 + 16) % 16;
+  static_assert(!ROWS || TPL >= 16, "row lines need at least 16 threads per line");
+  __shared__ float2 s_tw[n];
+  __shared__ float2 s_ex[LPB * EX];
+  if (stopped(st)) return;
+  for (int j = threadIdx.x; j < n; j += blockDim.x) s_tw[j] = tw[j];
+  const int l = ROWS ? threadIdx.x / TPL : threadIdx.x % LPB;
+  const int role = ROWS ? threadIdx.x % TPL : threadIdx.x / LPB;
+  const int64_t line = (int64_t)blockIdx.x * LPB + l;
+  float2 *ex = s_ex + l * EX;
+  const float2 zero = make_float2(0.f, 0.f);
+  __syncthreads();
+  if (KIND == kRowFwd) {
+    const int j0 = (int)(line / L), j1 = (int)(line - (int64_t)(line / L) * L);
+    const float2 *src = vol + ((int64_t)j0 * L + j1) * L;
+    float2 *dst = g + ((int64_t)voxel_store(j0, L, n) * n + voxel_store(j1, L, n)) * n;
+    line_dft<N1, N2, false>(
+        ex, s_tw, role, [&](int i) { const int j = pad_voxel(i, L, n); return j < 0 ? zero : src[j]; },
+        [&](int k, float2 v) { dst[k] = v; });
+  } else if (KIND == kColFwd || KIND == kColInv) {
+    const int t0 = (int)(line / n), s2 = (int)(line - (int64_t)(line / n) * n);
+    float2 *c = g + (int64_t)support_index(t0, L, n) * n * n + s2;  // entry s1 at c[s1 * n]
+    if (KIND == kColFwd) {
+      line_dft<N1, N2, false>(
+          ex, s_tw, role, [&](int i) { return in_support(i, L, n) ? c[(int64_t)i * n] : zero; },
+          [&](int k, float2 v) { c[(int64_t)k * n] = v; });
+    } else {
+      line_dft<N1, N2, true>(
+          ex, s_tw, role, [&](int i) { return c[(int64_t)i * n]; },
+          [&](int k, float2 v) { if (in_support(k, L, n)) c[(int64_t)k * n] = v; });
+    }
+  } else {  // kRowInv
+    const int j0 = (int)(line / L), j1 = (int)(line - (int64_t)(line / L) * L);
+    const float2 *src = g + ((int64_t)voxel_store(j0, L, n) * n + voxel_store(j1, L, n)) * n;
+    float2 *dst = out + ((int64_t)j0 * L + j1) * L;
+    const float2 *pr = p ? p + ((int64_t)j0 * L + j1) * L : nullptr;
+    const float inv = 1.0f / ((float)n * (float)n * (float)n);
+    double re = 0.0, im = 0.0;
+    line_dft<N1, N2, true>(
+        ex, s_tw, role, [&](int i) { return src[i]; },
+        [&](int k, float2 v) {
+          const int j = pad_voxel(k, L, n);
+          if (j < 0) return;
+          const float2 y = make_float2(v.x * inv, v.y * inv);
+          dst[j] = y;
+          if (pr) {  // conj(p) * y
+            const float2 q = pr[j];
+            re += (double)q.x * y.x + (double)q.y * y.y;
+            im += (double)q.x * y.y - (double)q.y * y.x;
+          }
+        });
+    if (p) block_add2(re, im, &st->pap[0], &st->pap[1]);
+  }
+}
+
 // The fused axis-0 transform for the grid sizes it is built for (n = 64 .. 512); returns false
 // (nothing launched) for others, which take cuFFT and fine_diag_kernel.
 bool axis0_fused_size(int n) { return n == 64 || n == 128 || n == 256 || n == 512; }
 
+// One twiddle table exp(-2 pi i j / tn) of the plan's fine size tn serves the fine operator and
+// the L^3 preconditioner (every (tn / n)-th entry); built on the host in double precision.
+int ensure_twiddles(cov3d_plan *p, int n) {
+  const int tn = p->n % n == 0 ? p->n : n;
+  if (p->fftw_n == tn) return COV3D_OK;
+  std::vector<float2> h(tn);
+  for (int j = 0; j < tn; ++j) {
+    const double a = 2.0 * 3.14159265358979323846 * (double)j / (double)tn;
+    h[j] = make_float2((float)std::cos(a), (float)-std::sin(a));
+  }
+  COV3D_TRY(grow(p->fftw, (int64_t)tn * sizeof(float2)));
+  COV3D_CUDA(cudaMemcpyAsync(p->fftw.ptr, h.data(), tn * sizeof(float2), cudaMemcpyHostToDevice, p->stream));
+  COV3D_CUDA(cudaStreamSynchronize(p->stream));  // h goes out of scope
+  p->fftw_n = tn;
+  return COV3D_OK;
+}
+
 int launch_axis0_diag(cov3d_plan *p, float2 *g, const float *diag, int L, int n, int divide, float scale,
                       const CgState *gate) {
-  // one twiddle table of the plan's fine size serves the fine operator and the L^3
-  // preconditioner (every (fine n / n)-th entry)
-  const int tn = p->n % n == 0 ? p->n : n;
-  if (p->fftw_n != tn) {
-    std::vector<float2> h(tn);
-    for (int j = 0; j < tn; ++j) {
-      const double a = 2.0 * 3.14159265358979323846 * (double)j / (double)tn;
-      h[j] = make_float2((float)std::cos(a), (float)-std::sin(a));
-    }
-    COV3D_TRY(grow(p->fftw, (int64_t)tn * sizeof(float2)));
-    COV3D_CUDA(cudaMemcpyAsync(p->fftw.ptr, h.data(), tn * sizeof(float2), cudaMemcpyHostToDevice, p->stream));
-    COV3D_CUDA(cudaStreamSynchronize(p->stream));  // h goes out of scope
-    p->fftw_n = tn;
-  }
+  COV3D_TRY(ensure_twiddles(p, n));
   const float2 *tw = p->fftw.as<float2>();
-  const int ts = tn / n;
+  const int ts = p->fftw_n / n;
   const int64_t lines = (int64_t)n * n;
   switch (n) {
     case 64: axis0_diag_kernel<8, 8><<<(unsigned)(lines / 32), 256, 0, p->stream>>>(g, diag, tw, ts, L, divide, scale, gate); break;
@@ -344,6 +461,45 @@ int launch_axis0_diag(cov3d_plan *p, float2 *g, const float *diag, int L, int n,
     default: set_error("no fused axis-0 transform for n = %d", n); return COV3D_EINVAL;
   }
   return launched("axis0_diag_kernel");
+}
+
+// The whole CG operator on hand-written line DFTs (n = 128, 256, 512): pad + rows, columns,
+// axis 0 with the diagonal, inverse columns, inverse rows + crop (+ <p, out> into acc).
+bool pruned3_size(int n) { return n == 128 || n == 256 || n == 512; }
+
+template <int N1, int N2>
+int pruned3_launch(cov3d_plan *p, const float2 *in, float2 *fine, float2 *out, const float2 *dotp, const float *diag,
+                   int divide, int L, const CgState *gate, CgState *acc) {
+  constexpr int TPL = N1 > N2 ? N1 : N2, LPB = 256 / TPL;
+  constexpr int n = N1 * N2;
+  cudaStream_t s = p->stream;
+  const float2 *tw = p->fftw.as<float2>();
+  CgState *g = const_cast<CgState *>(gate);
+  const unsigned rows = (unsigned)((int64_t)L * L / LPB), cols = (unsigned)((int64_t)L * n / LPB);
+  cg_line_kernel<N1, N2, kRowFwd><<<rows, 256, 0, s>>>(in, fine, nullptr, nullptr, tw, L, g);
+  COV3D_LAUNCHED("cg_line_kernel");
+  cg_line_kernel<N1, N2, kColFwd><<<cols, 256, 0, s>>>(nullptr, fine, nullptr, nullptr, tw, L, g);
+  COV3D_LAUNCHED("cg_line_kernel");
+  COV3D_TRY(launch_axis0_diag(p, fine, diag, L, n, divide, 1.0f, gate));
+  cg_line_kernel<N1, N2, kColInv><<<cols, 256, 0, s>>>(nullptr, fine, nullptr, nullptr, tw, L, g);
+  COV3D_LAUNCHED("cg_line_kernel");
+  cg_line_kernel<N1, N2, kRowInv><<<rows, 256, 0, s>>>(nullptr, fine, out, dotp, tw, L, dotp ? acc : g);
+  return launched("cg_line_kernel");
+}
+
+int pruned3(cov3d_plan *p, const float2 *in, float2 *fine, float2 *out, const float2 *dotp, const float *diag,
+            int divide, int L, int n, const CgState *gate, CgState *acc) {
+  COV3D_TRY(ensure_twiddles(p, n));
+  if (p->fftw_n != n) {
+    set_error("pruned line transform: twiddle table of %d for n = %d", p->fftw_n, n);
+    return COV3D_EINVAL;
+  }
+  switch (n) {
+    case 128: return pruned3_launch<16, 8>(p, in, fine, out, dotp, diag, divide, L, gate, acc);
+    case 256: return pruned3_launch<16, 16>(p, in, fine, out, dotp, diag, divide, L, gate, acc);
+    case 512: return pruned3_launch<32, 16>(p, in, fine, out, dotp, diag, divide, L, gate, acc);
+    default: set_error("no pruned line transform for n = %d", n); return COV3D_EINVAL;
+  }
 }
 
 // out = crop(fine) / n^3; optionally keep only the real part; optionally accumulate <p, out>
@@ -757,6 +913,8 @@ int cg_solve(cov3d_plan *p, const float *d_lhs, const void *d_b, void *d_x, doub
   // with pruning and a grid size the fused axis-0 kernel covers, the axis-0 transforms and the
   // diagonal are one in-place pass over the support planes of `fine`
   const bool fused = pruned && axis0_fused_size(n);
+  // for n = 128 .. 512 the whole operator runs on hand-written line DFTs (no cuFFT)
+  const bool lines3 = fused && pruned3_size(n) && p->n == n;
   float2 *full = fine;
   if (pruned) {
     if (!fused) {
@@ -764,14 +922,17 @@ int cg_solve(cov3d_plan *p, const float *d_lhs, const void *d_b, void *d_x, doub
       full = p->fine2.as<float2>();
       COV3D_TRY(get_fft_axis0(p, &h0));
     }
-    COV3D_TRY(get_fft_planes(p, &hp));
-    COV3D_CUDA(cudaMemsetAsync(fine, 0, (size_t)n3 * 8, s));
+    if (!lines3) {
+      COV3D_TRY(get_fft_planes(p, &hp));
+      COV3D_CUDA(cudaMemsetAsync(fine, 0, (size_t)n3 * 8, s));
+    }
   }
   const int64_t half_off = (int64_t)(n - L / 2) * n * n;  // second block of support planes
   COV3D_CUDA(cudaMemsetAsync(st, 0, sizeof(CgState), s));
 
   // out = crop(ifft3(diag^(+-1) * fft3(pad(in)))), with <p, out> into st->pap when dotp is given
   auto apply_op = [&](const float2 *in, float2 *out, int divide, const float2 *dotp, const CgState *gate) -> int {
+    if (lines3) return pruned3(p, in, fine, out, dotp, d_lhs, divide, L, n, gate, st);
     if (fused) {
       pad_support_kernel<<<capped((int64_t)L * n), 256, 0, s>>>(in, L, n, fine, gate);
       COV3D_LAUNCHED("pad_support_kernel");

@@ -141,4 +141,21 @@ __device__ __forceinline__ float tap_weight(float t, int q, float beta) {
   return es_weight<W>(t - (float)(c0 + q), beta);
 }
 
+// Index maps of the fine grid (FFT-native storage: frequency / voxel offset k at k mod n).
+// centered index of storage index s on a grid of size m (fftshift)
+__device__ __forceinline__ int native_to_centered(int s, int m) {
+  const int c = s + m / 2;
+  return c >= m ? c - m : c;
+}
+// voxel index (0 .. L-1) of storage index s on a zero-padded axis, or -1 for padding
+__device__ __forceinline__ int pad_voxel(int s, int L, int n) {
+  const int h = L / 2;
+  return s < L - h ? s + h : (s >= n - h ? s - n + h : -1);
+}
+// storage index of voxel j
+__device__ __forceinline__ int voxel_store(int j, int L, int n) {
+  const int k = j - L / 2;
+  return k < 0 ? k + n : k;
+}
+
 }  // namespace cov3d

@@ -164,6 +164,20 @@ int get_fft(cov3d_plan *p, int nchan, cufftHandle *out);
 int get_fft_planes(cov3d_plan *p, cufftHandle *out);
 int get_fft_axis0(cov3d_plan *p, cufftHandle *out);
 int fft2(cufftHandle h, const float2 *in, float2 *out, int dir);
+
+// line_fft.cu: hand-written line DFTs of the fine grid.  `stop` points at a done flag (kernels
+// return once it is nonzero) or is null.
+bool axis0_fused_size(int n);
+bool line_transforms_apply(const cov3d_plan *p);
+int ensure_twiddles(cov3d_plan *p, int n);
+int launch_axis0_diag(cov3d_plan *p, float2 *g, const float *diag, int L, int n, int divide, float scale,
+                      const int *stop);
+int cg_operator_lines(cov3d_plan *p, const float2 *in, float2 *fine, float2 *out, const float2 *dotp,
+                      const float *diag, int divide, const int *stop, const int *stop_last, double *dot);
+int step_forward_lines(cov3d_plan *p, const float *vec, const float *logs, const float *gc, int r, float2 *stage,
+                       float2 *grid, const float *fr, double coef, double *cost);
+int step_inverse_lines(cov3d_plan *p, float2 *grad_grid, const float *vec, const float *logs, const float *gc, int r,
+                       float *gvec, double *glog);
 inline bool prunable(const cov3d_plan *p) { return p->L % 2 == 0 && p->n >= p->L + 2; }
 
 // points_sort.cu

@@ -68,11 +68,6 @@ __device__ void block_add2(double a, double b, double *ga, double *gb) {
 
 __device__ __forceinline__ bool stopped(const CgState *st) { return st != nullptr && st->done != 0; }
 
-// centered index of FFT-native storage index s on a grid of size m (fftshift)
-__device__ __forceinline__ int native_to_centered(int s, int m) {
-  const int c = s + m / 2;
-  return c >= m ? c - m : c;
-}
 
 // fine[s] = src[centered(s)] (/ div[centered(s)]); src complex or real
 __global__ void load_centered_kernel(const float2 *__restrict__ src, const float *__restrict__ src_real,
@@ -100,16 +95,6 @@ inline unsigned capped(int64_t n_items_per_block_unit) {
                                                         : kRowBlocks);
 }
 
-// voxel index of FFT-native storage index s on the padded axis, or -1 for padding
-__device__ __forceinline__ int pad_voxel(int s, int L, int n) {
-  const int h = L / 2;
-  return s < L - h ? s + h : (s >= n - h ? s - n + h : -1);
-}
-// FFT-native storage index of voxel j
-__device__ __forceinline__ int voxel_store(int j, int L, int n) {
-  const int k = j - L / 2;
-  return k < 0 ? k + n : k;
-}
 
 // zero-pad x (L^3, voxel offset k = j - L/2) into FFT-native storage k mod n
 __global__ void pad_kernel(const float2 *__restrict__ x, int L, int n, float2 *__restrict__ fine, const CgState *st) {
@@ -166,339 +151,6 @@ __global__ void fine_diag_kernel(float2 *__restrict__ g, const float *__restrict
       const float2 v = grow[s2];
       grow[s2] = make_float2(v.x * f, v.y * f);
     }
-  }
-}
-
-// DFT of N values held in registers (natural order in, natural order out), recursive
-// decimation in time, radix 4 (radix 2 for the last factor when N is not a power of 4);
-// w[j] = exp(-2 pi i j / n) is the n-point twiddle table and STRIDE = n / N picks the N-point
-// twiddles from it; INV uses exp(+2 pi i j / n) (unnormalised, as cuFFT).
-__device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
-  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
-}
-
-template <int STRIDE, bool INV>
-__device__ __forceinline__ float2 twiddle(const float2 *w, int j) {
-  float2 t = w[j * STRIDE];
-  if (INV) t.y = -t.y;
-  return t;
-}
-
-template <int N, int STRIDE, bool INV>
-__device__ __forceinline__ void reg_dft(float2 *a, const float2 *w) {
-  if constexpr (N == 2) {
-    const float2 x = a[0], y = a[1];
-    a[0] = make_float2(x.x + y.x, x.y + y.y);
-    a[1] = make_float2(x.x - y.x, x.y - y.y);
-  } else if constexpr (N >= 4) {
-    constexpr int Q = N / 4;
-    float2 s0[Q], s1[Q], s2[Q], s3[Q];
-#pragma unroll
-    for (int i = 0; i < Q; ++i) {
-      s0[i] = a[4 * i];
-      s1[i] = a[4 * i + 1];
-      s2[i] = a[4 * i + 2];
-      s3[i] = a[4 * i + 3];
-    }
-    if constexpr (Q > 1) {
-      reg_dft<Q, 4 * STRIDE, INV>(s0, w);
-      reg_dft<Q, 4 * STRIDE, INV>(s1, w);
-      reg_dft<Q, 4 * STRIDE, INV>(s2, w);
-      reg_dft<Q, 4 * STRIDE, INV>(s3, w);
-    }
-#pragma unroll
-    for (int k = 0; k < Q; ++k) {
-      const float2 t0 = s0[k];
-      const float2 t1 = k == 0 ? s1[k] : cmulf(s1[k], twiddle<STRIDE, INV>(w, k));
-      const float2 t2 = k == 0 ? s2[k] : cmulf(s2[k], twiddle<STRIDE, INV>(w, 2 * k));
-      const float2 t3 = k == 0 ? s3[k] : cmulf(s3[k], twiddle<STRIDE, INV>(w, 3 * k));
-      const float2 a0 = make_float2(t0.x + t2.x, t0.y + t2.y), a1 = make_float2(t0.x - t2.x, t0.y - t2.y);
-      const float2 b0 = make_float2(t1.x + t3.x, t1.y + t3.y), b1 = make_float2(t1.x - t3.x, t1.y - t3.y);
-      // forward: X[k + Q] = a1 - i b1, X[k + 3Q] = a1 + i b1; the inverse swaps them
-      const float2 mib = INV ? make_float2(-b1.y, b1.x) : make_float2(b1.y, -b1.x);
-      a[k] = make_float2(a0.x + b0.x, a0.y + b0.y);
-      a[k + Q] = make_float2(a1.x + mib.x, a1.y + mib.y);
-      a[k + 2 * Q] = make_float2(a0.x - b0.x, a0.y - b0.y);
-      a[k + 3 * Q] = make_float2(a1.x - mib.x, a1.y - mib.y);
-    }
-  }
-}
-
-// The axis-0 part of the CG operator, fused: for every line (s1, s2) of an n^3 FFT-native grid
-// whose nonzero axis-0 entries are the support planes [0, L/2) and [n - L/2, n), the forward DFT
-// along axis 0, the multiply by scale * diag (scale / diag with `divide`; diag centred like
-// fine_diag_kernel's), the inverse DFT and the store of the support entries only, in place.
-// L >= 2n makes every plane a support plane (a full transform, for the L^3 preconditioner).
-// The twiddles are every tw_step-th entry of a larger table.
-// It replaces a cuFFT axis-0 transform, fine_diag_kernel and the inverse transform (three
-// passes over n^3 values) by one pass over the support half and the diagonal.
-// n = N1 * N2 by the four-step decomposition: index i0 = n1 + N1 n2, frequency k = k2 + N2 k1;
-// N2-point DFTs over n2 (thread n1), twiddle exp(-2 pi i n1 k2 / n), an exchange through shared
-// memory, N1-point DFTs over n1 (thread k2); the inverse mirrors it.  A block takes 256 / TPL
-// consecutive lines s2 of one s1, so every row of loads and stores is contiguous.
-template <int N1, int N2>
-__global__ void __launch_bounds__(256) axis0_diag_kernel(float2 *__restrict__ g, const float *__restrict__ diag,
-                                                         const float2 *__restrict__ tw, int tw_step, int L,
-                                                         int divide, float scale, const CgState *st) {
-  constexpr int n = N1 * N2;
-  constexpr int TPL = N1 > N2 ? N1 : N2;  // threads per line
-  constexpr int LPB = 256 / TPL;          // lines per block
-  constexpr int RA = N1 + 1;              // exchange row of the forward transform (padded)
-  constexpr int RB = N2 + 1;              // exchange row of the inverse transform (padded)
-  // per-line exchange stride: a half warp (16 lanes of 8-byte accesses) spans H = min(LPB, 16)
-  // lines and 16 / H roles, so lines must fall 16 / H banks-pairs apart: EX = 16 / H (mod 16)
-  constexpr int EX0 = N2 * RA > N1 * RB ? N2 * RA : N1 * RB;
-  constexpr int STEP = 16 / (LPB < 16 ? LPB : 16);
-  constexpr int EX = EX0 + ((STEP - EX0 % 16) % 16 + 16) % 16;
-  __shared__ float2 s_tw[n];
-  __shared__ float2 s_ex[LPB * EX];
-  if (stopped(st)) return;
-  for (int j = threadIdx.x; j < n; j += blockDim.x) s_tw[j] = tw[j * tw_step];
-  const int l = threadIdx.x % LPB, role = threadIdx.x / LPB;
-  const int64_t line = (int64_t)blockIdx.x * LPB + l;  // s1 * n + s2
-  const int s1 = (int)(line / n), s2 = (int)(line - (int64_t)s1 * n);
-  const int64_t nn = (int64_t)n * n;
-  float2 *col = g + line;  // entry i0 of the line at col[i0 * nn]
-  const int h = L / 2;
-  float2 *ex = s_ex + l * EX;
-  __syncthreads();
-  if (role < N1) {  // forward, thread n1: N2-point DFT over n2 of x[n1 + N1 n2], twiddle, exchange
-    float2 v[N2];
-#pragma unroll
-    for (int n2 = 0; n2 < N2; ++n2) {
-      const int i0 = role + N1 * n2;
-      v[n2] = (i0 < h || i0 >= n - h) ? col[i0 * nn] : make_float2(0.f, 0.f);
-    }
-    reg_dft<N2, n / N2, false>(v, s_tw);
-#pragma unroll
-    for (int k2 = 0; k2 < N2; ++k2) ex[k2 * RA + role] = k2 == 0 ? v[0] : cmulf(v[k2], s_tw[role * k2]);
-  }
-  __syncthreads();
-  float2 u[N1];
-  if (role < N2) {
-#pragma unroll
-    for (int n1 = 0; n1 < N1; ++n1) u[n1] = ex[role * RA + n1];
-  }
-  __syncthreads();
-  if (role < N2) {  // thread k2: N1-point DFT over n1 gives X[k2 + N2 k1]; diagonal; inverse over k1
-    const float *dcol = diag + (int64_t)native_to_centered(s1, n) * n + native_to_centered(s2, n);
-    float d[N1];  // loaded before the transform, so their latency hides behind it
-#pragma unroll
-    for (int k1 = 0; k1 < N1; ++k1) d[k1] = __ldg(dcol + (int64_t)native_to_centered(role + N2 * k1, n) * nn);
-    reg_dft<N1, n / N1, false>(u, s_tw);
-#pragma unroll
-    for (int k1 = 0; k1 < N1; ++k1) {
-      const float f = divide ? scale / d[k1] : scale * d[k1];
-      u[k1] = make_float2(u[k1].x * f, u[k1].y * f);
-    }
-    reg_dft<N1, n / N1, true>(u, s_tw);  // u[m1] = sum_k1 X[k2 + N2 k1] exp(+2 pi i k1 m1 / N1)
-#pragma unroll
-    for (int m1 = 0; m1 < N1; ++m1) {
-      float2 t = s_tw[role * m1];
-      t.y = -t.y;
-      ex[m1 * RB + role] = m1 == 0 ? u[0] : cmulf(u[m1], t);
-    }
-  }
-  __syncthreads();
-  if (role < N1) {  // thread m1: inverse N2-point DFT over k2 gives x[m1 + N1 m2]; support rows only
-    float2 v[N2];
-#pragma unroll
-    for (int k2 = 0; k2 < N2; ++k2) v[k2] = ex[role * RB + k2];
-    reg_dft<N2, n / N2, true>(v, s_tw);
-#pragma unroll
-    for (int m2 = 0; m2 < N2; ++m2) {
-      const int i0 = role + N1 * m2;
-      if (i0 < h || i0 >= n - h) col[i0 * nn] = v[m2];
-    }
-  }
-}
-
-// One n-point DFT per line by the same four-step decomposition as axis0_diag_kernel: element
-// i = n1 + N1 n2 comes from load(i) (thread n1), the result X[k], k = k2 + N2 k1, goes to
-// store(k, X) (thread k2).  ex is the line's exchange area (N2 (N1 + 1) values); every thread
-// of the block calls it (it synchronises the block).
-template <int N1, int N2, bool INV, typename Load, typename Store>
-__device__ __forceinline__ void line_dft(float2 *ex, const float2 *s_tw, int role, Load load, Store store) {
-  constexpr int n = N1 * N2;
-  constexpr int RA = N1 + 1;
-  if (role < N1) {
-    float2 v[N2];
-#pragma unroll
-    for (int n2 = 0; n2 < N2; ++n2) v[n2] = load(role + N1 * n2);
-    reg_dft<N2, n / N2, INV>(v, s_tw);
-#pragma unroll
-    for (int k2 = 0; k2 < N2; ++k2) ex[k2 * RA + role] = k2 == 0 ? v[0] : cmulf(v[k2], twiddle<1, INV>(s_tw, role * k2));
-  }
-  __syncthreads();
-  if (role < N2) {
-    float2 u[N1];
-#pragma unroll
-    for (int n1 = 0; n1 < N1; ++n1) u[n1] = ex[role * RA + n1];
-    reg_dft<N1, n / N1, INV>(u, s_tw);
-#pragma unroll
-    for (int k1 = 0; k1 < N1; ++k1) store(role + N2 * k1, u[k1]);
-  }
-}
-
-// support plane / row t in [0, L) of an axis of the fine grid (FFT-native storage)
-__device__ __forceinline__ int support_index(int t, int L, int n) { return t < L / 2 ? t : n - L + t; }
-__device__ __forceinline__ bool in_support(int s, int L, int n) { return s < L / 2 || s >= n - L / 2; }
-
-// The pruned transforms of the CG operator around axis0_diag_kernel, as line DFTs of the fine
-// grid (n = N1 N2, FFT-native storage, a voxel j of the L^3 volume at index voxel_store(j)):
-//   kRowFwd: rows (s0, s1) of support planes and rows: the volume row zero-padded, DFT along
-//            axis 2, the whole row written (pad fused);
-//   kColFwd: columns (s0, s2) of support planes: the support entries, DFT along axis 1, the whole
-//            column written;
-//   kColInv: the inverse along axis 1, support entries written;
-//   kRowInv: the inverse along axis 2, the L support entries / n^3 written to the volume (crop
-//            fused), with <p, out> into st->pap when p is given.
-// Every kernel writes exactly what the next reads, so the grid needs no zeroing.  Rows are
-// contiguous (a line's threads are adjacent lanes); columns are n apart (a block takes
-// consecutive columns, adjacent lanes on adjacent columns).
-enum { kRowFwd = 0, kColFwd = 1, kColInv = 2, kRowInv = 3 };
-
-template <int N1, int N2, int KIND>
-__global__ void __launch_bounds__(256) cg_line_kernel(const float2 *__restrict__ vol, float2 *__restrict__ g,
-                                                      float2 *__restrict__ out, const float2 *__restrict__ p,
-                                                      const float2 *__restrict__ tw, int L, CgState *st) {
-  constexpr int n = N1 * N2;
-  constexpr int TPL = N1 > N2 ? N1 : N2;
-  constexpr int LPB = 256 / TPL;
-  constexpr bool ROWS = KIND == kRowFwd || KIND == kRowInv;
-  constexpr int RA = N1 + 1;
-  // exchange stride per line: with columns a half warp spans min(LPB, 16) lines (see
-  // axis0_diag_kernel); with rows (TPL >= 16) it stays within one line
-  constexpr int EX0 = N2 * RA;
-  constexpr int STEP = 16 / (LPB < 16 ? LPB : 16);
-  constexpr int EX = ROWS ? EX0 : EX0 + ((STEP - EX0 % 16) % 16 + 16) % 16;
-  static_assert(!ROWS || TPL >= 16, "row lines need at least 16 threads per line");
-  __shared__ float2 s_tw[n];
-  __shared__ float2 s_ex[LPB * EX];
-  if (stopped(st)) return;
-  for (int j = threadIdx.x; j < n; j += blockDim.x) s_tw[j] = tw[j];
-  const int l = ROWS ? threadIdx.x / TPL : threadIdx.x % LPB;
-  const int role = ROWS ? threadIdx.x % TPL : threadIdx.x / LPB;
-  const int64_t line = (int64_t)blockIdx.x * LPB + l;
-  float2 *ex = s_ex + l * EX;
-  const float2 zero = make_float2(0.f, 0.f);
-  __syncthreads();
-  if (KIND == kRowFwd) {
-    const int j0 = (int)(line / L), j1 = (int)(line - (int64_t)(line / L) * L);
-    const float2 *src = vol + ((int64_t)j0 * L + j1) * L;
-    float2 *dst = g + ((int64_t)voxel_store(j0, L, n) * n + voxel_store(j1, L, n)) * n;
-    line_dft<N1, N2, false>(
-        ex, s_tw, role, [&](int i) { const int j = pad_voxel(i, L, n); return j < 0 ? zero : src[j]; },
-        [&](int k, float2 v) { dst[k] = v; });
-  } else if (KIND == kColFwd || KIND == kColInv) {
-    const int t0 = (int)(line / n), s2 = (int)(line - (int64_t)(line / n) * n);
-    float2 *c = g + (int64_t)support_index(t0, L, n) * n * n + s2;  // entry s1 at c[s1 * n]
-    if (KIND == kColFwd) {
-      line_dft<N1, N2, false>(
-          ex, s_tw, role, [&](int i) { return in_support(i, L, n) ? c[(int64_t)i * n] : zero; },
-          [&](int k, float2 v) { c[(int64_t)k * n] = v; });
-    } else {
-      line_dft<N1, N2, true>(
-          ex, s_tw, role, [&](int i) { return c[(int64_t)i * n]; },
-          [&](int k, float2 v) { if (in_support(k, L, n)) c[(int64_t)k * n] = v; });
-    }
-  } else {  // kRowInv
-    const int j0 = (int)(line / L), j1 = (int)(line - (int64_t)(line / L) * L);
-    const float2 *src = g + ((int64_t)voxel_store(j0, L, n) * n + voxel_store(j1, L, n)) * n;
-    float2 *dst = out + ((int64_t)j0 * L + j1) * L;
-    const float2 *pr = p ? p + ((int64_t)j0 * L + j1) * L : nullptr;
-    const float inv = 1.0f / ((float)n * (float)n * (float)n);
-    double re = 0.0, im = 0.0;
-    line_dft<N1, N2, true>(
-        ex, s_tw, role, [&](int i) { return src[i]; },
-        [&](int k, float2 v) {
-          const int j = pad_voxel(k, L, n);
-          if (j < 0) return;
-          const float2 y = make_float2(v.x * inv, v.y * inv);
-          dst[j] = y;
-          if (pr) {  // conj(p) * y
-            const float2 q = pr[j];
-            re += (double)q.x * y.x + (double)q.y * y.y;
-            im += (double)q.x * y.y - (double)q.y * y.x;
-          }
-        });
-    if (p) block_add2(re, im, &st->pap[0], &st->pap[1]);
-  }
-}
-
-// The fused axis-0 transform for the grid sizes it is built for (n = 64 .. 512); returns false
-// (nothing launched) for others, which take cuFFT and fine_diag_kernel.
-bool axis0_fused_size(int n) { return n == 64 || n == 128 || n == 256 || n == 512; }
-
-// One twiddle table exp(-2 pi i j / tn) of the plan's fine size tn serves the fine operator and
-// the L^3 preconditioner (every (tn / n)-th entry); built on the host in double precision.
-int ensure_twiddles(cov3d_plan *p, int n) {
-  const int tn = p->n % n == 0 ? p->n : n;
-  if (p->fftw_n == tn) return COV3D_OK;
-  std::vector<float2> h(tn);
-  for (int j = 0; j < tn; ++j) {
-    const double a = 2.0 * 3.14159265358979323846 * (double)j / (double)tn;
-    h[j] = make_float2((float)std::cos(a), (float)-std::sin(a));
-  }
-  COV3D_TRY(grow(p->fftw, (int64_t)tn * sizeof(float2)));
-  COV3D_CUDA(cudaMemcpyAsync(p->fftw.ptr, h.data(), tn * sizeof(float2), cudaMemcpyHostToDevice, p->stream));
-  COV3D_CUDA(cudaStreamSynchronize(p->stream));  // h goes out of scope
-  p->fftw_n = tn;
-  return COV3D_OK;
-}
-
-int launch_axis0_diag(cov3d_plan *p, float2 *g, const float *diag, int L, int n, int divide, float scale,
-                      const CgState *gate) {
-  COV3D_TRY(ensure_twiddles(p, n));
-  const float2 *tw = p->fftw.as<float2>();
-  const int ts = p->fftw_n / n;
-  const int64_t lines = (int64_t)n * n;
-  switch (n) {
-    case 64: axis0_diag_kernel<8, 8><<<(unsigned)(lines / 32), 256, 0, p->stream>>>(g, diag, tw, ts, L, divide, scale, gate); break;
-    case 128: axis0_diag_kernel<16, 8><<<(unsigned)(lines / 16), 256, 0, p->stream>>>(g, diag, tw, ts, L, divide, scale, gate); break;
-    case 256: axis0_diag_kernel<16, 16><<<(unsigned)(lines / 16), 256, 0, p->stream>>>(g, diag, tw, ts, L, divide, scale, gate); break;
-    case 512: axis0_diag_kernel<32, 16><<<(unsigned)(lines / 8), 256, 0, p->stream>>>(g, diag, tw, ts, L, divide, scale, gate); break;
-    default: set_error("no fused axis-0 transform for n = %d", n); return COV3D_EINVAL;
-  }
-  return launched("axis0_diag_kernel");
-}
-
-// The whole CG operator on hand-written line DFTs (n = 128, 256, 512): pad + rows, columns,
-// axis 0 with the diagonal, inverse columns, inverse rows + crop (+ <p, out> into acc).
-bool pruned3_size(int n) { return n == 128 || n == 256 || n == 512; }
-
-template <int N1, int N2>
-int pruned3_launch(cov3d_plan *p, const float2 *in, float2 *fine, float2 *out, const float2 *dotp, const float *diag,
-                   int divide, int L, const CgState *gate, CgState *acc) {
-  constexpr int TPL = N1 > N2 ? N1 : N2, LPB = 256 / TPL;
-  constexpr int n = N1 * N2;
-  cudaStream_t s = p->stream;
-  const float2 *tw = p->fftw.as<float2>();
-  CgState *g = const_cast<CgState *>(gate);
-  const unsigned rows = (unsigned)((int64_t)L * L / LPB), cols = (unsigned)((int64_t)L * n / LPB);
-  cg_line_kernel<N1, N2, kRowFwd><<<rows, 256, 0, s>>>(in, fine, nullptr, nullptr, tw, L, g);
-  COV3D_LAUNCHED("cg_line_kernel");
-  cg_line_kernel<N1, N2, kColFwd><<<cols, 256, 0, s>>>(nullptr, fine, nullptr, nullptr, tw, L, g);
-  COV3D_LAUNCHED("cg_line_kernel");
-  COV3D_TRY(launch_axis0_diag(p, fine, diag, L, n, divide, 1.0f, gate));
-  cg_line_kernel<N1, N2, kColInv><<<cols, 256, 0, s>>>(nullptr, fine, nullptr, nullptr, tw, L, g);
-  COV3D_LAUNCHED("cg_line_kernel");
-  cg_line_kernel<N1, N2, kRowInv><<<rows, 256, 0, s>>>(nullptr, fine, out, dotp, tw, L, dotp ? acc : g);
-  return launched("cg_line_kernel");
-}
-
-int pruned3(cov3d_plan *p, const float2 *in, float2 *fine, float2 *out, const float2 *dotp, const float *diag,
-            int divide, int L, int n, const CgState *gate, CgState *acc) {
-  COV3D_TRY(ensure_twiddles(p, n));
-  if (p->fftw_n != n) {
-    set_error("pruned line transform: twiddle table of %d for n = %d", p->fftw_n, n);
-    return COV3D_EINVAL;
-  }
-  switch (n) {
-    case 128: return pruned3_launch<16, 8>(p, in, fine, out, dotp, diag, divide, L, gate, acc);
-    case 256: return pruned3_launch<16, 16>(p, in, fine, out, dotp, diag, divide, L, gate, acc);
-    case 512: return pruned3_launch<32, 16>(p, in, fine, out, dotp, diag, divide, L, gate, acc);
-    default: set_error("no pruned line transform for n = %d", n); return COV3D_EINVAL;
   }
 }
 
@@ -914,7 +566,7 @@ int cg_solve(cov3d_plan *p, const float *d_lhs, const void *d_b, void *d_x, doub
   // diagonal are one in-place pass over the support planes of `fine`
   const bool fused = pruned && axis0_fused_size(n);
   // for n = 128 .. 512 the whole operator runs on hand-written line DFTs (no cuFFT)
-  const bool lines3 = fused && pruned3_size(n) && p->n == n;
+  const bool lines3 = fused && line_transforms_apply(p) && p->n == n;
   float2 *full = fine;
   if (pruned) {
     if (!fused) {
@@ -932,13 +584,14 @@ int cg_solve(cov3d_plan *p, const float *d_lhs, const void *d_b, void *d_x, doub
 
   // out = crop(ifft3(diag^(+-1) * fft3(pad(in)))), with <p, out> into st->pap when dotp is given
   auto apply_op = [&](const float2 *in, float2 *out, int divide, const float2 *dotp, const CgState *gate) -> int {
-    if (lines3) return pruned3(p, in, fine, out, dotp, d_lhs, divide, L, n, gate, st);
+    const int *stop = gate ? &gate->done : nullptr;
+    if (lines3) return cg_operator_lines(p, in, fine, out, dotp, d_lhs, divide, stop, dotp ? &st->done : stop, st->pap);
     if (fused) {
       pad_support_kernel<<<capped((int64_t)L * n), 256, 0, s>>>(in, L, n, fine, gate);
       COV3D_LAUNCHED("pad_support_kernel");
       COV3D_TRY(fft2(hp, fine, fine, CUFFT_FORWARD));
       COV3D_TRY(fft2(hp, fine + half_off, fine + half_off, CUFFT_FORWARD));
-      COV3D_TRY(launch_axis0_diag(p, fine, d_lhs, L, n, divide, 1.0f, gate));
+      COV3D_TRY(launch_axis0_diag(p, fine, d_lhs, L, n, divide, 1.0f, stop));
       COV3D_TRY(fft2(hp, fine, fine, CUFFT_INVERSE));
       COV3D_TRY(fft2(hp, fine + half_off, fine + half_off, CUFFT_INVERSE));
       crop_kernel<<<capped((int64_t)L * L), 256, 0, s>>>(fine, L, n, out, 0, dotp,
@@ -977,7 +630,7 @@ int cg_solve(cov3d_plan *p, const float *d_lhs, const void *d_b, void *d_x, doub
     if (precond == 1) return apply_op(in, out, 1, nullptr, gate);
     if (coarse_fused) {
       COV3D_TRY(fft2(hcp, in, out, CUFFT_FORWARD));
-      COV3D_TRY(launch_axis0_diag(p, out, d_sym, 2 * L, L, 1, 1.0f / (float)L3, gate));
+      COV3D_TRY(launch_axis0_diag(p, out, d_sym, 2 * L, L, 1, 1.0f / (float)L3, gate ? &gate->done : nullptr));
       return fft2(hcp, out, out, CUFFT_INVERSE);
     }
     copy_kernel<<<nb(L3), 256, 0, s>>>(in, out, L3);

@@ -69,8 +69,9 @@ def test_fused_step_matches_reference(pkg, dev, objective, with_reg):
 
 
 # r = 10 takes the staged Gram and per-pixel W-pass kernels, r = 20 two channel groups of the
-# spreading, two interpolation passes and the rank-20 solve
-@pytest.mark.parametrize("L,r,B", [(16, 3, 8), (24, 5, 12), (16, 10, 6), (16, 20, 4)])
+# spreading, two interpolation passes and the rank-20 solve; L = 64 and 128 (fine grids of 128,
+# 256) the hand-written line transforms with the pack, regulariser and unpack fused in
+@pytest.mark.parametrize("L,r,B", [(16, 3, 8), (24, 5, 12), (16, 10, 6), (16, 20, 4), (64, 3, 2), (128, 2, 1)])
 def test_fused_es_step_matches_fp64_oracle(pkg, dev, L, r, B):
     rng = np.random.default_rng(L * r)
     vec = rng.standard_normal((r, L, L, L))

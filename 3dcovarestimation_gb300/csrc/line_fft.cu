@@ -328,7 +328,7 @@ __global__ void __launch_bounds__(256) line_kernel(const LineArgs a) {
       const float g01 = a.gc ? 1.0f / (__ldg(a.gc + j0) * __ldg(a.gc + j1)) : 1.0f;
       const float *vsrc = a.vec + c * L3 + vrow;
       float *gdst = a.gvec + c * L3 + vrow;
-      double part = 0.0;
+      float part = 0.0f;  // this thread's terms in FP32, then one FP64 block sum
       line_dft<N1, N2, true>(
           ex, s_tw, role, [&](int i) { return row[i]; },
           [&](int k, float2 v) {
@@ -337,9 +337,9 @@ __global__ void __launch_bounds__(256) line_kernel(const LineArgs a) {
             const float gj = a.gc ? g01 / __ldg(a.gc + j) : 1.0f;
             const float dV = 2.0f * v.x * gj;
             gdst[j] = dV * es;
-            part += (double)(dV * (__ldg(vsrc + j) * es));
+            part = fmaf(dV, __ldg(vsrc + j) * es, part);
           });
-      block_add_pair(part, 0.0, a.glog + c, nullptr);
+      block_add_pair((double)part, 0.0, a.glog + c, nullptr);
     }
   } else if (KIND == kColFwd || KIND == kColInv) {
     const int t0 = (int)(line / n), s2 = (int)(line - (int64_t)(line / n) * n);
@@ -359,7 +359,7 @@ __global__ void __launch_bounds__(256) line_kernel(const LineArgs a) {
       const int s1 = (int)(line / n), s2 = (int)(line - (int64_t)(line / n) * n);
       float2 *gx = a.gout + c * a.cs + line;
       const float *frl = a.fr ? a.fr + (int64_t)native_to_centered(s1, n) * n + native_to_centered(s2, n) : nullptr;
-      double part = 0.0;
+      float part = 0.0f;  // this thread's N1 terms in FP32, then one FP64 block sum (FP64 is slow)
       line_dft<N1, N2, false>(
           ex, s_tw, role, [&](int i) { return in_support(i, L, n) ? ax[(int64_t)i * nn] : zero; },
           [&](int k, float2 v) {
@@ -369,11 +369,11 @@ __global__ void __launch_bounds__(256) line_kernel(const LineArgs a) {
               const float w = __ldg(frl + (int64_t)native_to_centered(k, n) * nn);
               const float cf = (float)a.coef * w;
               y = make_float2(cf * v.x, cf * v.y);
-              part += (double)(w * fmaf(v.x, v.x, v.y * v.y));
+              part = fmaf(w, fmaf(v.x, v.x, v.y * v.y), part);
             }
             ax[(int64_t)k * nn] = y;
           });
-      if (a.fr) block_add_pair(part * a.coef, 0.0, a.cost, nullptr);
+      if (a.fr) block_add_pair((double)part * a.coef, 0.0, a.cost, nullptr);
     } else {  // kAxisInv
       line_dft<N1, N2, true>(
           ex, s_tw, role, [&](int i) { return ax[(int64_t)i * nn]; },

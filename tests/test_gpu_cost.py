@@ -94,10 +94,11 @@ def test_fused_es_step_matches_fp64_oracle(pkg, dev, L, r, B):
     assert rel(gl, ref[2]) < TOL_GRAD
 
 
-def test_fused_step_equals_dropin_autograd_full_size(pkg, dev):
-    """Two independent code paths at L=64: the single-call fused step and the drop-in cost
-    (vol_forward + ProjectedCost autograd) on the same discretized plan."""
-    L, r, B = 64, 4, 16
+@pytest.mark.parametrize("L,r,B", [(64, 4, 16), (256, 2, 2)])
+def test_fused_step_equals_dropin_autograd_full_size(pkg, dev, L, r, B):
+    """Two independent code paths: the single-call fused step (line-DFT transforms with the
+    pack and unpack fused; n = 128 and 512) and the drop-in cost (torch's FFT of the volumes,
+    vol_forward + ProjectedCost autograd) on the same discretized plan."""
     g = torch.Generator(device=dev).manual_seed(1)
     covar = pkg.Covar(L, r, upsampling_factor=2).to(dev)
     covar.init_grid_correction("bilinear")

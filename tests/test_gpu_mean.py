@@ -170,3 +170,46 @@ def test_cg_iterates_match_oracle_on_fused_grids(pkg, dev, L, precond):
                            precond=pc)
     assert not info.converged and info.iters == 2
     assert rel(x.reshape(-1), ref) < TOL_CG
+
+
+@pytest.mark.parametrize("precond", [None, "diagonal", "symbol"])
+def test_cg_iterates_at_n512_match_torch_fft_cg(pkg, dev, precond):
+    """L = 256 (the fine grid of 512 takes the 32 x 16 line DFTs, the L^3 preconditioner the
+    16 x 16 axis-0 kernel on every other twiddle): three CG iterations against the same
+    iterations written with torch's float64 FFTs."""
+    L, n = 256, 512
+    g = torch.Generator(device=dev).manual_seed(3)
+    reg = torch.rand((n,) * 3, generator=g, device=dev, dtype=torch.float64) * 2.5 + 0.5
+    b = torch.randn((L,) * 3, generator=g, device=dev, dtype=torch.complex128).reshape(-1)
+    sym = torch.rand((L,) * 3, generator=g, device=dev, dtype=torch.float64) * 2.5 + 0.5
+
+    def A(x, d=reg):
+        X = pkg.centered_fft3(x.reshape((L,) * 3), padding_size=(n,) * 3)
+        return pkg.centered_ifft3(d * X, cropping_size=(L,) * 3).reshape(-1)
+
+    if precond == "diagonal":
+        M = lambda v: A(v, 1.0 / reg)  # noqa: E731
+    elif precond == "symbol":
+        M = lambda v: pkg.centered_ifft3(pkg.centered_fft3(v.reshape((L,) * 3)) / sym).reshape(-1)  # noqa: E731
+    else:
+        M = lambda v: v  # noqa: E731
+    x = torch.zeros_like(b)
+    r = b - A(x)
+    z = M(r)
+    p = z.clone()
+    rz = torch.vdot(r, z).real
+    for _ in range(3):
+        Ap = A(p)
+        alpha = rz / torch.vdot(p, Ap)
+        x = x + alpha * p
+        r = r - alpha * Ap
+        z = M(r)
+        rz_new = torch.vdot(r, z).real
+        p = z + (rz_new / rz) * p
+        rz = rz_new
+    pc = sym.to(torch.float32) if precond == "symbol" else precond
+    xd, info = pkg.cg_solve(reg.to(torch.float32), b.to(torch.complex64),
+                            torch.zeros(L**3, dtype=torch.complex64, device=dev), L, rtol=1e-12, maxiter=3,
+                            precond=pc)
+    assert not info.converged and info.iters == 2
+    assert rel(xd.reshape(-1).to(torch.complex128), x) < TOL_CG

@@ -663,14 +663,18 @@ int covar_cost_grad(cov3d_plan *p, const cov3d_cost_args *a, double *h_cost, dou
   // channel's L support planes, then the axis-0 FFT out of place into fine.
   const bool pruned = prunable(p);
   // fine grids of n = 128 .. 512: hand-written line transforms with the pack, the regulariser
-  // (value, and the gradient grid's initial coef * fr * G or zero) and the unpack fused in
-  const bool lines = pruned && line_transforms_apply(p);
+  // (value, and the gradient grid's initial coef * fr * G or zero) and the unpack fused in.  The
+  // forward one up to n = 256: at 512 its 32 x 16 split idles half the threads in one stage and
+  // measured slower than pack + cuFFT + regulariser (19.0 against 15.4 ms at L = 256, r = 10);
+  // the inverse is faster at every size (8.8 against 11.1 ms there).
+  const bool lines_inv = pruned && line_transforms_apply(p);
+  const bool lines_fwd = lines_inv && p->n <= 256;
   const bool with_reg = a->d_fourier_reg && a->reg_scale != 0.0;
   const float *gcp = a->use_grid_correction ? p->gc1d.as<float>() : nullptr;
   cufftHandle fft = 0, fplanes = 0, faxis0 = 0;
   if (pruned) {
     COV3D_TRY(grow(p->fine2, n3 * r * 8));
-    if (!lines) {
+    if (!lines_fwd) {  // the forward transform on cuFFT
       COV3D_TRY(get_fft_planes(p, &fplanes));
       COV3D_TRY(get_fft_axis0(p, &faxis0));
     }
@@ -678,7 +682,7 @@ int covar_cost_grad(cov3d_plan *p, const cov3d_cost_args *a, double *h_cost, dou
     COV3D_TRY(get_fft(p, r, &fft));
   }
   const int64_t half_off = (int64_t)(p->n - L / 2) * p->n * p->n;
-  if (lines) {
+  if (lines_fwd) {
     PhaseScope ps(p, kPhaseFftFwd);
     COV3D_TRY(step_forward_lines(p, a->d_vectors, a->d_log_sqrt, gcp, r, p->fine2.as<float2>(), p->fine.as<float2>(),
                                  with_reg ? a->d_fourier_reg : nullptr, a->reg_scale / (2.0 * a->noise_var), acc + 1));
@@ -687,7 +691,7 @@ int covar_cost_grad(cov3d_plan *p, const cov3d_cost_args *a, double *h_cost, dou
     COV3D_TRY(launch_pack(p, a->d_vectors, nullptr, a->d_log_sqrt, a->use_grid_correction, r,
                           pruned ? p->fine2.ptr : p->fine.ptr));
   }
-  if (!lines) {
+  if (!lines_fwd) {
     PhaseScope ps(p, kPhaseFftFwd);
     if (pruned) {
       for (int c = 0; c < r; ++c) {
@@ -733,18 +737,18 @@ int covar_cost_grad(cov3d_plan *p, const cov3d_cost_args *a, double *h_cost, dou
   }
   // 7'. the regulariser (value and gradient coef * fr * G) initialises the gradient grid, so the
   // spread adds onto it and no zeroing pass is needed; without one, the grid is zeroed
-  if (with_reg && !lines) {
+  if (with_reg && !lines_fwd) {
     PhaseScope ps(p, kPhaseReg);
     COV3D_TRY(launch_ml_reg(p, p->fine.ptr, p->fine2.ptr, a->d_fourier_reg, r, a->reg_scale / (2.0 * a->noise_var),
                             acc + 1, 1));
   }
   {
     PhaseScope ps(p, kPhaseSpread);
-    if (!with_reg && !lines) COV3D_TRY(launch_zero(p, p->fine2.ptr, n3 * r * 8));
+    if (!with_reg && !lines_fwd) COV3D_TRY(launch_zero(p, p->fine2.ptr, n3 * r * 8));
     COV3D_TRY(launch_spread(p, p->q.ptr, r, 1, r, ep, p->fine2.ptr, 1, n3, shift));
   }
   // 9. adjoint FFT, 10. crop + deapodise + chain rule to the Covar parameters
-  if (lines) {
+  if (lines_inv) {
     PhaseScope ps(p, kPhaseFftInv);
     COV3D_TRY(step_inverse_lines(p, p->fine2.as<float2>(), a->d_vectors, a->d_log_sqrt, gcp, r, d_grad_vectors,
                                  acc + 8));
@@ -762,7 +766,7 @@ int covar_cost_grad(cov3d_plan *p, const cov3d_cost_args *a, double *h_cost, dou
                             "cufftExecC2C(inverse)"));
     }
   }
-  if (!lines) {
+  if (!lines_inv) {
     PhaseScope ps(p, kPhaseUnpack);
     COV3D_TRY(launch_unpack_grad(p, p->fine2.ptr, a->d_vectors, a->d_log_sqrt, a->use_grid_correction, r,
                                  d_grad_vectors, acc + 8));

@@ -6,7 +6,10 @@
 //
 //   A(x) = crop_L( ifft3( lhs * fft3( pad_n(x) ) ) )      (centered transforms, ifft / n^3)
 //
-// The operator is pad + cuFFT + diagonal multiply + inverse cuFFT + crop.  The vector updates
+// For even L and fine grids of n = 128 .. 512 the operator runs on the hand-written pruned line
+// DFTs of line_fft.cu (pad, crop and the diagonal fused in); at n = 64 the axis-0 transform
+// and the diagonal are fused between cuFFT 2D transforms of the support planes; otherwise it is
+// pad + cuFFT + diagonal multiply + inverse cuFFT + crop.  The vector updates
 // are fused with their inner products, which accumulate in FP64.  The iteration scalars stay
 // in device memory and a convergence flag turns every kernel of later iterations into a
 // no-op, so the host polls the flag only every few iterations.  Preconditioners:

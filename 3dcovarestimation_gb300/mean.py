@@ -4,7 +4,8 @@
 with the nearest-neighbour plan (``cov3d_mean_accumulate``), floors the kernel
 (``cov3d_regularize_lhs``), takes the Fourier-diagonal solve as the starting point and corrects
 it for the zero padding with conjugate gradients run entirely on the device
-(``cov3d_cg_solve``: FP64 inner products and residual norms, FP32 vectors and cuFFT).
+(``cov3d_cg_solve``: FP64 inner products and residual norms, FP32 vectors, hand-written
+pruned line DFTs for the operator on fine grids of 128 .. 512, cuFFT otherwise).
 
 Preconditioners of the CG (``precond``): ``None`` is the reference's plain CG;
 ``"diagonal"`` divides by the kernel on the fine grid (the operator the reference uses for its
@@ -76,7 +77,7 @@ def complex_conjugate_gradient(A_mv, b, x0=None, rtol=1e-6, maxiter=None):
 
 
 class _MeanSolver:
-    """A plan used for the mean's grids, CG operator and cuFFT plans."""
+    """A plan used for the mean's grids, CG operator and transform workspaces."""
 
     _cache = {}
 

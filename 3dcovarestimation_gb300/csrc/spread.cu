@@ -65,7 +65,7 @@ struct PointRec {
 // point ids, prologue factors, key counters and offsets, column offsets, the task counter.
 struct StageSmem {
   long long *rowoff;  // T * T
-  float2 *rec;        // max_sub * F2
+  void *rec;          // max_sub * F2 record elements (float2, or float for scalar weights)
   int *key, *pid;     // max_sub each
   float *sc;          // max_sub
   int *cnt, *off;     // kKeys, kKeys + 1
@@ -73,16 +73,16 @@ struct StageSmem {
   int *task;          // 1
 };
 
-__host__ __device__ constexpr size_t stage_bytes(int max_sub, int T, int F2) {
-  return (size_t)T * T * sizeof(long long) + (size_t)max_sub * (F2 * sizeof(float2) + 3 * sizeof(int)) +
+__host__ __device__ constexpr size_t stage_bytes(int max_sub, int T, int F2, size_t esize) {
+  return (size_t)T * T * sizeof(long long) + (size_t)max_sub * (F2 * esize + 3 * sizeof(int)) +
          (size_t)(2 * kKeys + 2 + T) * sizeof(int);
 }
 
-__device__ __forceinline__ StageSmem carve(void *base, int max_sub, int T, int F2) {
+__device__ __forceinline__ StageSmem carve(void *base, int max_sub, int T, int F2, int esize) {
   StageSmem s;
   s.rowoff = static_cast<long long *>(base);
-  s.rec = reinterpret_cast<float2 *>(s.rowoff + T * T);
-  s.key = reinterpret_cast<int *>(s.rec + max_sub * F2);
+  s.rec = s.rowoff + T * T;
+  s.key = reinterpret_cast<int *>(static_cast<char *>(s.rec) + (size_t)max_sub * F2 * esize);
   s.pid = s.key + max_sub;
   s.sc = reinterpret_cast<float *>(s.pid + max_sub);
   s.cnt = reinterpret_cast<int *>(s.sc + max_sub);
@@ -113,7 +113,11 @@ __device__ __forceinline__ SubTile sub_tile(const SpreadParams &a, int sub) {
 // axis-0) corner (l1, l0) of their window and stages, in that order, each point's record, id
 // and prologue factor (im_backward's Nyquist zeroing, CTF and scale), then the global offsets
 // of the tile's rows and columns.  The caller synchronises before reading them.
-template <int KT, int W, int ROWS>
+// a weight as a record element: twice (a packed-multiply operand) or once
+__device__ __forceinline__ void put_weight(float2 *e, float x) { *e = make_float2(x, x); }
+__device__ __forceinline__ void put_weight(float *e, float x) { *e = x; }
+
+template <int KT, int W, int ROWS, typename E>
 __device__ __forceinline__ void stage_subproblem(const SpreadParams &a, const StageSmem &s, const SubTile &st) {
   using Rec = PointRec<W, ROWS>;
   constexpr int T = Rec::T;
@@ -169,24 +173,24 @@ __device__ __forceinline__ void stage_subproblem(const SpreadParams &a, const St
       c0 = wrap1(c0, n);
       c2 = wrap1(c2, n);
     }
-    float2 *rec = s.rec + slot * F2;
+    E *rec = static_cast<E *>(s.rec) + slot * F2;
     const int l0 = c0 - st.ts0, l2 = c2 - st.ts2;  // bin-local corners, >= 1 - W (zero padding below)
-    const float2 z = make_float2(0.f, 0.f);
+    const float z = 0.0f;
 #pragma unroll
     for (int e = 0; e < T; ++e) {
-      rec[e] = z;
-      rec[Rec::W2 + e] = z;
+      put_weight(rec + e, z);
+      put_weight(rec + Rec::W2 + e, z);
     }
-    rec[Rec::W2 + T] = z;
+    put_weight(rec + Rec::W2 + T, z);
 #pragma unroll
-    for (int e = T; e < Rec::W1; ++e) rec[e] = z;
+    for (int e = T; e < Rec::W1; ++e) put_weight(rec + e, z);
 #pragma unroll
-    for (int e = Rec::W1 + W; e < Rec::W2; ++e) rec[e] = z;
+    for (int e = Rec::W1 + W; e < Rec::W2; ++e) put_weight(rec + e, z);
 #pragma unroll
     for (int r = 0; r < W; ++r) {
-      if (l0 + r >= 0 && l0 + r < T) rec[l0 + r] = make_float2(w0[r], w0[r]);
-      if (l2 + r >= 0 && l2 + r < T) rec[Rec::W2 + l2 + r] = make_float2(w2[r], w2[r]);
-      rec[Rec::W1 + r] = make_float2(w1[r], w1[r]);
+      if (l0 + r >= 0 && l0 + r < T) put_weight(rec + l0 + r, w0[r]);
+      if (l2 + r >= 0 && l2 + r < T) put_weight(rec + Rec::W2 + l2 + r, w2[r]);
+      put_weight(rec + Rec::W1 + r, w1[r]);
     }
     const int id = sp_id(sp.idf);
     float sc = (a.nyquist && sp_nyquist(sp.idf)) ? 0.0f : a.scale;
@@ -265,11 +269,12 @@ __global__ void __launch_bounds__(kSpreadWarps * 32, W < 8 ? 2 : 1) spread_kerne
   constexpr int F2 = Rec::F2;
   extern __shared__ float4 smem4[];
   float4 *s_val = smem4;  // max_sub * NP
-  const StageSmem s = carve(s_val + a.max_sub * NP, a.max_sub, T, F2);
+  const StageSmem s = carve(s_val + a.max_sub * NP, a.max_sub, T, F2, sizeof(float2));
+  const float2 *recs = static_cast<const float2 *>(s.rec);
   const int sub = blockIdx.x;
   if (sub >= *a.nsub) return;
   const SubTile st = sub_tile(a, sub);
-  stage_subproblem<KT, W, 1>(a, s, st);
+  stage_subproblem<KT, W, 1, float2>(a, s, st);
 
   const int tid = threadIdx.x, lane = tid & 31;
   const int g = lane / T, c = lane - (lane / T) * T;
@@ -305,7 +310,7 @@ __global__ void __launch_bounds__(kSpreadWarps * 32, W < 8 ? 2 : 1) spread_kerne
         hi01[u] = hi23[u] = lo01[u] = lo23[u] = make_float2(0.f, 0.f);
       }
       bool any = false;
-      const float2 *w2c = s.rec + Rec::W2 + c;  // this lane's column weight, record 0
+      const float2 *w2c = recs + Rec::W2 + c;  // this lane's column weight, record 0
       for (int l1g = rb; l1g > rb - W; l1g -= kFoldRanges) {
         float2 part01[CPL], part23[CPL];  // packed FP32 (FFMA2), same rounding as fmaf
 #pragma unroll
@@ -326,7 +331,7 @@ __global__ void __launch_bounds__(kSpreadWarps * 32, W < 8 ? 2 : 1) spread_kerne
           // multiplies by a zero weight
           int i = ibeg;
           for (; i + 1 < iend; i += 2) {
-            const float2 *ra = s.rec + i * F2, *rb2 = ra + F2;
+            const float2 *ra = recs + i * F2, *rb2 = ra + F2;
             const float2 wa = __fmul2_rn(__fmul2_rn(ra[pa], ra[k1]), w2c[i * F2]);
             const float2 wb = __fmul2_rn(__fmul2_rn(rb2[pa], rb2[k1]), w2c[(i + 1) * F2]);
 #pragma unroll
@@ -340,7 +345,7 @@ __global__ void __launch_bounds__(kSpreadWarps * 32, W < 8 ? 2 : 1) spread_kerne
             }
           }
           if (i < iend) {
-            const float2 *ra = s.rec + i * F2;
+            const float2 *ra = recs + i * F2;
             const float2 wa = __fmul2_rn(__fmul2_rn(ra[pa], ra[k1]), w2c[i * F2]);
 #pragma unroll
             for (int u = 0; u < CPL; ++u) {
@@ -404,18 +409,19 @@ __global__ void __launch_bounds__(kSpreadWarps * 32, 1) spread_rows_kernel(const
   constexpr int F2 = Rec::F2;
   extern __shared__ float4 smem4[];
   float2 *s_val = reinterpret_cast<float2 *>(smem4);  // max_sub * PS
-  const StageSmem s = carve(s_val + a.max_sub * PS, a.max_sub, T, F2);
+  const StageSmem s = carve(s_val + a.max_sub * PS, a.max_sub, T, F2, sizeof(float));
+  const float *recs = static_cast<const float *>(s.rec);  // weights once each (scalar records)
   const int sub = blockIdx.x;
   if (sub >= *a.nsub) return;
   const SubTile st = sub_tile(a, sub);
-  stage_subproblem<KT, W, ROWS>(a, s, st);
+  stage_subproblem<KT, W, ROWS, float>(a, s, st);
 
   const int tid = threadIdx.x, lane = tid & 31;
   const int h = lane / T;
   const bool lane_live = h < 2;
   const int hv = lane_live ? h : 0;             // idle lanes read half 0 ...
   const int c = lane_live ? lane - h * T : T;   // ... and the zero column weight
-  const float2 *w2c = s.rec + Rec::W2 + c;      // this lane's column weight, record 0
+  const float *w2c = recs + Rec::W2 + c;        // this lane's column weight, record 0
   for (int p0 = 0; p0 < a.nch; p0 += 2 * CH) {  // channel groups of 2 * CH
     __syncthreads();
     // this group's scaled channel values, in sorted order: half hh holds p0 + hh * CH + ch
@@ -463,11 +469,14 @@ __global__ void __launch_bounds__(kSpreadWarps * 32, 1) spread_rows_kernel(const
           got |= ibeg < iend;
           const int k1 = Rec::W1 + rb - l1;  // row rb + q reads the axis-1 weight k1 + q
           for (int i = ibeg; i < iend; ++i) {
-            const float2 *rec = s.rec + i * F2;
-            const float2 w02 = __fmul2_rn(rec[pa], w2c[i * F2]);
+            const float *rec = recs + i * F2;
+            const float w02 = rec[pa] * w2c[i * F2];
             float2 w[ROWS];
 #pragma unroll
-            for (int q = 0; q < ROWS; ++q) w[q] = __fmul2_rn(w02, rec[k1 + q]);
+            for (int q = 0; q < ROWS; ++q) {
+              const float wq = w02 * rec[k1 + q];
+              w[q] = make_float2(wq, wq);
+            }
             const float2 *vp = s_val + i * PS + hv * HS;
             float2 v[CH];
 #pragma unroll
@@ -544,12 +553,14 @@ int launch_wc(SpreadParams a, int nchan, int64_t max_blocks, cudaStream_t st) {
   const int npairs = (nchan + 1) / 2;
   if (npairs >= 3) {
     constexpr int PS = 2 * ((kRowGroupCH + 1) / 2 * 2);
-    const size_t smem = (size_t)a.max_sub * PS * sizeof(float2) + stage_bytes(a.max_sub, T, PointRec<W, kRows>::F2);
+    const size_t smem = (size_t)a.max_sub * PS * sizeof(float2) +
+                        stage_bytes(a.max_sub, T, PointRec<W, kRows>::F2, sizeof(float));
     return launch_spread_kernel(spread_rows_kernel<KT, W, kRowGroupCH, kRows, COMP>, "spread_rows_kernel", smem, a,
                                 max_blocks, st);
   }
   static_assert(2 * G >= 2, "at most two channel pairs spread over the lane groups");
-  const size_t smem = (size_t)a.max_sub * G * sizeof(float4) + stage_bytes(a.max_sub, T, PointRec<W, 1>::F2);
+  const size_t smem =
+      (size_t)a.max_sub * G * sizeof(float4) + stage_bytes(a.max_sub, T, PointRec<W, 1>::F2, sizeof(float2));
   return launch_spread_kernel(spread_kernel<KT, W, 1, COMP>, "spread_kernel", smem, a, max_blocks, st);
 }
 

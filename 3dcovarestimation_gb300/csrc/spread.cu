@@ -45,8 +45,10 @@ constexpr int kLMin = -8;   // window corners relative to the bin lie in [kLMin,
 constexpr int kKeys = 256;  // sort key (l1 - kLMin) * 16 + (l0 - kLMin)
 constexpr int kFoldRanges = 3;  // window-corner rows l1 summed in FP32 between compensated folds
 
-// Per-point record staged once per block, in float2 units (each weight twice, the operand of a
-// packed multiply): the axis-0 weights by tile plane and the axis-2 weights by tile column, zero
+// Per-point record staged once per block, in elements of float2 (each weight twice, the operand
+// of a packed multiply: spread_kernel) or float (each weight once, splatted in a register:
+// spread_rows_kernel, where the bytes shared memory returns per visit are the bound): the
+// axis-0 weights by tile plane and the axis-2 weights by tile column, zero
 // outside the point's window (the column slot T is always zero, for idle lanes), and the W
 // axis-1 weights with ROWS - 1 zeros before them and max(ROWS - 1, 1) after.  A lane's weight
 // for tile row b of a point with window corner l1 is then

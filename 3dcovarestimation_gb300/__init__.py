@@ -6,17 +6,20 @@ The directory name starts with a digit, so import it with
 ``importlib.import_module("3dcovarestimation_gb300")``.
 """
 
-from . import _lib, dataset, fsc_utils, learned_pc, mean, synthetic, wiener_coords
+from . import _lib, dataset, fsc_utils, learned_pc, mean, synthetic, utils, wiener_coords
 from .covar import Covar, Mean
 from .mean import (MeanBackprojector, cg_solve, circulant_symbol, complex_conjugate_gradient,
-                   correct_upsampling_padding, get_grid_correction, reconstruct_mean, regularize_lhs, solve_mean)
+                   correct_upsampling_padding, get_grid_correction, reconstruct_mean, reconstruct_mean_from_halfsets,
+                   reconstruct_mean_from_halfsets_DDP, regularize_lhs, regularize_mean_from_halfsets, solve_mean)
 from .covar_sgd import (CovarTrainer, FusedCovarStep, ProjectedCost, cost, cost_fourier_domain,
                         cost_maximum_liklihood, cost_maximum_liklihood_fourier_domain, raw_cost_fourier_domain,
-                        raw_cost_maximum_liklihood_fourier_domain)
+                        raw_cost_maximum_liklihood_fourier_domain, trainCovar, update_fourier_reg)
+from .dataset import ResidentDataset, ResidentLoader
 from .nufft_plan import (BaseNufftPlan, NufftPlan, NufftPlanDiscretized, NufftSpec, NufftType, TorchNufftAdjoint,
                          TorchNufftForward, get_half_fourier_grid, nufft_adjoint, nufft_forward)
 from .projection_funcs import (centered_fft2, centered_fft3, centered_ifft2, centered_ifft3, crop_image, crop_tensor,
-                               im_backward, make_nufft_plan, pad_tensor, vol_forward)
+                               get_mask_threshold, im_backward, make_nufft_plan, pad_tensor, preprocess_image_batch,
+                               vol_forward)
 
 LIB_PATH = _lib.LIB_PATH
 

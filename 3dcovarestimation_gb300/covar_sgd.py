@@ -269,25 +269,76 @@ def gram_bf16(Q, y, plan=None):
     return gram, h, yy
 
 
+def _loader_batch_size(train_data) -> Optional[int]:
+    """Batch size of a DataLoader (its ``batch_size`` or its sampler's, as the reference's
+    ``get_dataloader_batch_size``) or of a :class:`ResidentLoader`."""
+    bs = getattr(train_data, "batch_size", None)
+    if bs is None:
+        for attr in ("batch_sampler", "sampler"):
+            bs = getattr(getattr(train_data, attr, None), "batch_size", None)
+            if bs is not None:
+                break
+    return bs
+
+
 class CovarTrainer:
-    """Covariance SGD trainer (reference ``covar_sgd.py:48-409``) on GPU-resident data.
+    """Covariance SGD trainer (reference ``covar_sgd.py:48-545``); every batch is one call of
+    the fused cost/gradient step (:class:`FusedCovarStep`) followed by the optimizer step.
 
-    ``train_data`` is an iterable of batches ``(images, poses, filters)`` already on the GPU:
-    images in the Fourier domain, ``poses`` either rotation matrices (B, 3, 3) (points generated
-    in the kernels) or reference-style points (B, 3, L**2)."""
+    ``train_data`` is what the reference takes -- a DataLoader whose batches are ``(images,
+    pts_rot, filters, idx)`` over a dataset exposing ``noise_var``, ``mask`` and the
+    ``to_fourier_domain`` / ``to_spatial_domain`` switches -- or a
+    :class:`~.dataset.ResidentLoader` over a device-resident dataset, whose batches carry
+    rotation matrices (B, 3, 3) instead of points (generated in the kernels).  ``noise_var``
+    and ``dataset_size`` may be given for any other iterable of batches."""
 
-    def __init__(self, covar: Covar, train_data, device, noise_var: float, dataset_size: int,
-                 save_path: Optional[str] = None) -> None:
+    def __init__(self, covar: Covar, train_data, device, save_path: Optional[str] = None, gt_data=None,
+                 training_log_freq: int = 50, *, noise_var: Optional[float] = None,
+                 dataset_size: Optional[int] = None) -> None:
         self.device = torch.device(device)
         self.train_data = train_data
-        self.covar = covar.to(self.device)
-        self.noise_var = noise_var
-        self.dataset_size = dataset_size
+        self._covar = covar.to(self.device)
+        self.batch_size = _loader_batch_size(train_data)
         self.save_path = save_path
+        self.gt_data = gt_data
+        self.training_log_freq = training_log_freq
+        self._noise_var = noise_var
+        self._dataset_size = dataset_size
         self.num_reduced_lr_before_stop = 4
         self.scheduler_patiece = 0
         self.fourier_reg = None
+        self.logTraining = True
         self.training_log = {"epoch_ind": [], "lr_history": [], "cost_val": [], "epoch_run_time": []}
+        self.step_fn = None
+
+    @property
+    def dataset(self):
+        return getattr(self.train_data, "dataset", None)
+
+    @property
+    def covar(self) -> Covar:
+        return self._covar
+
+    @property
+    def noise_var(self) -> float:
+        return self._noise_var if self._noise_var is not None else self.dataset.noise_var
+
+    @property
+    def vectorsGT(self):
+        return getattr(self.gt_data, "eigenvecs", None) if self.gt_data is not None else None
+
+    @property
+    def filter_gain(self) -> torch.Tensor:
+        """Shell-pair covariance gain of the dataset (``dataset.get_total_covar_gain``)."""
+        from .dataset import get_total_covar_gain
+
+        return get_total_covar_gain(self.dataset, device=self.device)
+
+    def to(self, *args: Any, **kwargs: Any) -> "CovarTrainer":
+        self._covar = self._covar.to(*args, **kwargs)
+        if self.fourier_reg is not None:
+            self.fourier_reg = self.fourier_reg.to(*args, **kwargs)
+        return self
 
     def compute_fourier_reg_term(self, eigenvecs: torch.Tensor) -> None:
         """Fourier regulariser from an estimate of the eigenvectors: noise_var over their radial
@@ -299,30 +350,48 @@ class CovarTrainer:
         self.fourier_reg = self.noise_var / upsample_and_expand_fourier_shell(eigen_rpsd, self.covar.resolution * us, 3)
 
     def update_fourier_reg_halfsets(self, fourier_reg: torch.Tensor) -> None:
-        """Install a regulariser computed from the half-sets, resampled to the fine grid
-        (reference ``covar_sgd.py:432-447``; this trainer optimises in the Fourier domain)."""
+        """Install a regulariser computed from the half-sets, resampled to the fine grid when the
+        optimisation runs in the Fourier domain (reference ``covar_sgd.py:432-447``)."""
         from .fsc_utils import average_fourier_shell, upsample_and_expand_fourier_shell
 
         fourier_reg = fourier_reg.to(self.device)
-        us = self.covar.upsampling_factor
-        radial = average_fourier_shell(fourier_reg) / (us**3)
-        self.fourier_reg = upsample_and_expand_fourier_shell(radial, self.covar.resolution * us, 3)
+        if getattr(self, "optimize_in_fourier_domain", True):
+            us = self.covar.upsampling_factor
+            radial = average_fourier_shell(fourier_reg) / (us**3)
+            fourier_reg = upsample_and_expand_fourier_shell(radial, self.covar.resolution * us, 3)
+        self.fourier_reg = fourier_reg
 
     def setup_training(self, lr: Optional[float] = None, momentum: float = 0.9, optim_type: str = "Adam",
-                       reg: float = 1, nufft_disc: str = "nufft", orthogonal_projection: bool = False,
-                       objective_func: str = "ml", batch_size: int = 1024, width: int = 6, compensated: bool = True):
+                       reg: float = 1, nufft_disc: str = "bilinear", orthogonal_projection: bool = False,
+                       objective_func: str = "ml", width: int = 6, compensated: bool = True,
+                       gram_precision: str = "fp32") -> None:
+        """Reference ``covar_sgd.py:302-358``: lr x batch size, Adam or SGD, the plan of
+        ``nufft_disc`` ("bilinear" / "nearest": discretized plans, Fourier-domain data; "nufft":
+        the ES kernel), reg_scale = reg / len(dataset)."""
         self.use_orthogonal_projection = orthogonal_projection
         if lr is None:
             lr = 1e-1 if optim_type == "Adam" else 1e-2
-        self.batch_size = batch_size
-        self.lr = lr * batch_size
+        if self.batch_size is None:
+            raise ValueError("the batch size of train_data is unknown")
+        self.lr = lr * self.batch_size
         self.optim_type, self.momentum = optim_type, momentum
-        self.objective = OBJECTIVE_ML if objective_func == "ml" else OBJECTIVE_LS
-        self.step_fn = FusedCovarStep(self.covar.resolution, self.covar.rank, nufft_disc,
-                                      self.covar.upsampling_factor, width=width, compensated=compensated,
-                                      device=self.device)
-        self.reg_scale = reg / self.dataset_size
         self.restart_optimizer()
+        self.optimize_in_fourier_domain = nufft_disc != "nufft"
+        self.objective_func = objective_func
+        self.objective = OBJECTIVE_ML if objective_func == "ml" else OBJECTIVE_LS
+        self.nufft_disc = nufft_disc
+        ds = self.dataset
+        if ds is not None and hasattr(ds, "to_fourier_domain"):
+            ds.to_fourier_domain() if self.optimize_in_fourier_domain else ds.to_spatial_domain()
+        self.step_fn = FusedCovarStep(self.covar.resolution, self.covar.rank, nufft_disc, self.covar.upsampling_factor,
+                                      width=width, compensated=compensated, device=self.device,
+                                      gram_precision=gram_precision)
+        if nufft_disc == "nufft":
+            self.covar.grid_correction = self.step_fn.plan.grid_correction().to(self.device)
+        else:
+            self.covar.init_grid_correction(nufft_disc)
+        n = self._dataset_size if self._dataset_size is not None else len(ds)
+        self.reg_scale = reg / n
         self.epoch_index = 0
 
     def restart_optimizer(self) -> None:
@@ -335,39 +404,168 @@ class CovarTrainer:
             self.optimizer = torch.optim.Adam(groups)
         self.scheduler = torch.optim.lr_scheduler.ReduceLROnPlateau(self.optimizer, patience=self.scheduler_patiece)
 
-    def run_batch(self, images, poses, filters):
-        """One SGD step (reference ``covar_sgd.py:199-229``); returns the cost as a device tensor."""
-        if poses.ndim == 3 and poses.shape[-1] == 3 and poses.shape[-2] == 3:
-            self.step_fn.set_rotations(poses)
+    def prepare_batch(self, batch) -> Tuple[torch.Tensor, torch.Tensor, torch.Tensor]:
+        images, poses, filters = batch[0], batch[1], batch[2]
+        return images.to(self.device), poses.to(self.device), filters.to(self.device)
+
+    def run_batch(self, images: torch.Tensor, pts_rot: torch.Tensor, filters: torch.Tensor) -> torch.Tensor:
+        """One SGD step (reference ``covar_sgd.py:199-229``); returns the cost (device scalar).
+        ``pts_rot`` is (B, 3, L^2) points or (B, 3, 3) rotations.  With ``nufft_disc="nufft"`` the
+        data are spatial (as the reference's) and enter the Fourier-domain step through a
+        centered 2D FFT with noise_var * L^2, which leaves the cost unchanged (Parseval)."""
+        L = self.covar.resolution
+        B = images.shape[0]
+        if pts_rot.ndim == 3 and tuple(pts_rot.shape[-2:]) == (3, 3):
+            self.step_fn.set_rotations(pts_rot)
         else:
-            self.step_fn.set_points(poses)
+            self.step_fn.set_points(pts_rot)
+        noise_var = self.noise_var
+        if not self.optimize_in_fourier_domain and not images.is_complex():
+            images = centered_fft2(images.reshape(B, L, L))
+            noise_var = noise_var * L**2
         cv = self.covar
         if cv.vectors.grad is None:
             cv.vectors.grad = torch.empty_like(cv.vectors)
             cv.log_sqrt_eigenvals.grad = torch.empty_like(cv.log_sqrt_eigenvals)
-        c, _, _ = self.step_fn(cv.vectors.detach(), cv.log_sqrt_eigenvals.detach(), images, filters, self.noise_var,
-                               self.reg_scale, self.fourier_reg, self.objective, grad_vectors=cv.vectors.grad,
-                               grad_log_sqrt=cv.log_sqrt_eigenvals.grad)
+        c, _, _ = self.step_fn(cv.vectors.detach(), cv.log_sqrt_eigenvals.detach(), images.reshape(B, -1),
+                               filters.reshape(B, -1), noise_var, self.reg_scale, self.fourier_reg, self.objective,
+                               grad_vectors=cv.vectors.grad, grad_log_sqrt=cv.log_sqrt_eigenvals.grad)
         self.optimizer.step()
         if self.use_orthogonal_projection:
             cv.orthogonal_projection()
-        return c
+        return c.reshape(())
 
     def run_epoch(self, epoch: int) -> None:
+        """Reference ``covar_sgd.py:246-281``: the summed cost of the epoch (cost x batch size,
+        as the reference accumulates it) stays on the device."""
         self.cost_in_epoch = torch.zeros((), dtype=torch.float64, device=self.device)
-        for images, poses, filters in self.train_data:
+        for batch in self.train_data:
+            images, poses, filters = self.prepare_batch(batch)
             c = self.run_batch(images, poses, filters)
-            self.cost_in_epoch += c.reshape(()) * images.shape[0]
+            self.cost_in_epoch += c * self.batch_size
 
     def train_epochs(self, max_epochs: int, restart_optimizer: bool = False) -> None:
+        """Reference ``covar_sgd.py:375-409``: ReduceLROnPlateau on the epoch cost, stop after
+        ``num_reduced_lr_before_stop`` reductions."""
         if restart_optimizer:
             self.restart_optimizer()
         for _ in range(max_epochs):
             t0 = time.time()
             self.run_epoch(self.epoch_index)
-            self.training_log["epoch_run_time"].append(time.time() - t0)
-            self.training_log["cost_val"].append(float(self.cost_in_epoch))
-            self.scheduler.step(self.cost_in_epoch)
+            dt = time.time() - t0
+            cost = float(self.cost_in_epoch)
+            self.scheduler.step(cost)
+            ds = self.dataset
+            if ds is not None and getattr(ds, "mask", None) is not None:
+                with torch.no_grad():
+                    m = ds.mask.to(self.device) > 0.3
+                    self.covar.vectors.data.copy_(self.covar.vectors.data * m)
+            self.training_log["epoch_ind"].append(self.epoch_index)
+            self.training_log["lr_history"].append(self.scheduler.get_last_lr()[0])
+            self.training_log["cost_val"].append(cost)
+            self.training_log["epoch_run_time"].append(dt)
+            if self.save_path is not None:
+                self.save_result()
             self.epoch_index += 1
             if self.scheduler.get_last_lr()[0] <= self.lr * (self.scheduler.factor**self.num_reduced_lr_before_stop):
+                logger.debug("learning rate reduced %d times; stopping", self.num_reduced_lr_before_stop)
                 break
+
+    def train(self, max_epochs: int, **training_kwargs: Any) -> None:
+        self.setup_training(**training_kwargs)
+        self.train_epochs(max_epochs)
+        self.complete_training()
+
+    def complete_training(self) -> None:
+        ds = self.dataset
+        if getattr(self, "optimize_in_fourier_domain", False) and ds is not None and hasattr(ds, "to_spatial_domain"):
+            ds.to_spatial_domain()
+
+    def results_dict(self) -> Dict[str, Any]:
+        """The checkpoint the reference saves as ``training_results.bin`` (``covar_sgd.py:524-545``):
+        the Covar state_dict, ``vectorsGT``, ``fourier_reg`` and the training log."""
+        ckp = self.covar.state_dict()
+        ckp["vectorsGT"] = self.vectorsGT
+        ckp["fourier_reg"] = self.fourier_reg
+        ckp.update(self.training_log)
+        return ckp
+
+    def save_result(self) -> None:
+        import os
+
+        d = os.path.split(self.save_path)[0]
+        if d:
+            os.makedirs(d, exist_ok=True)
+        torch.save(self.results_dict(), self.save_path)
+
+
+def update_fourier_reg(trainer1: CovarTrainer, trainer2: CovarTrainer) -> None:
+    """Half-set regulariser update (reference ``covar_sgd.py:1121-1152``): the covariance FSC of
+    the two half-set estimates and the averaged shell-pair gain give the new regulariser of
+    both trainers."""
+    L = trainer1.covar.resolution
+    filter_gain = (trainer1.filter_gain + trainer2.filter_gain) / 2
+    e1, l1 = trainer1.covar.eigenvecs
+    e1 = e1 * (l1**0.5).reshape(-1, 1, 1, 1)
+    e2, l2 = trainer2.covar.eigenvecs
+    e2 = e2 * (l2**0.5).reshape(-1, 1, 1, 1)
+    mask = getattr(trainer1.dataset, "mask", None)
+    reg, fsc = compute_updated_fourier_reg(e1, e2, filter_gain, trainer1.fourier_reg, L,
+                                           trainer1.optimize_in_fourier_domain, mask=mask)
+    trainer1.update_fourier_reg_halfsets(reg)
+    trainer2.update_fourier_reg_halfsets(reg)
+    trainer1.training_log["covariance_fsc_halfset"] = fsc
+
+
+def trainCovar(covar_model: Covar, dataset, batch_size: int, savepath: Optional[str] = None, gt_data=None,
+               **kwargs: Any) -> CovarTrainer:
+    """Training schedule of the reference (``covar_sgd.py:1479-1612``) on a device-resident
+    dataset (:class:`~.dataset.ResidentDataset`, or anything with its ``half_split`` /
+    ``get_total_covar_gain`` / domain switches).  Without half-sets: ``num_reg_update_iters``
+    rounds of training, each followed by the regulariser from the current eigenvectors and an
+    orthogonal projection, then a final run.  With half-sets (``use_halfsets``, the default of
+    the command line): a second model initialised at random vectors trains on the other half;
+    after each round both regularisers are updated from the half-sets' covariance FSC
+    (:func:`update_fourier_reg`); then the first model trains on the whole dataset.  Returns
+    the trainer of the final run."""
+    import copy
+
+    from .dataset import ResidentLoader
+
+    use_halfsets = kwargs.pop("use_halfsets", True)
+    num_reg_update_iters = kwargs.pop("num_reg_update_iters", 1) or 1
+    num_epochs = kwargs.pop("max_epochs", 20)
+    device = covar_model.device
+
+    def loader(ds):
+        return ResidentLoader(ds, batch_size)
+
+    if not use_halfsets:
+        trainer = CovarTrainer(covar_model, loader(dataset), device, savepath, gt_data=gt_data)
+        trainer.setup_training(**kwargs)
+        for _ in range(num_reg_update_iters):
+            trainer.train_epochs(num_epochs, restart_optimizer=True)
+            e, lam = trainer.covar.eigenvecs
+            trainer.compute_fourier_reg_term(e * (lam**0.5).reshape(-1, 1, 1, 1))
+            trainer.covar.orthogonal_projection()
+        trainer.train_epochs(num_epochs, restart_optimizer=True)
+        trainer.complete_training()
+        return trainer
+
+    covar_copy = copy.deepcopy(covar_model)
+    with torch.no_grad():
+        covar_copy.set_vectors(covar_copy.init_random_vectors(covar_model.rank).to(covar_copy.device))
+    half1, half2, _ = dataset.half_split()
+    trainer1 = CovarTrainer(covar_model, loader(half1), device, savepath, gt_data=gt_data)
+    trainer2 = CovarTrainer(covar_copy, loader(half2), device, None, gt_data=gt_data)
+    trainer1.setup_training(**kwargs)
+    trainer2.setup_training(**kwargs)
+    for _ in range(num_reg_update_iters):
+        trainer1.train_epochs(num_epochs, restart_optimizer=True)
+        trainer2.train_epochs(num_epochs, restart_optimizer=True)
+        update_fourier_reg(trainer1, trainer2)
+    trainer2.complete_training()
+    del trainer2
+    trainer1.train_data = loader(dataset)
+    trainer1.train(max_epochs=num_epochs, **kwargs)
+    return trainer1

@@ -337,3 +337,24 @@ def reconstruct_mean_from_halfsets(dataset, idx: Optional[torch.Tensor] = None, 
     m2, rhs2, lhs2 = reconstruct_mean(dataset, idx=idx[len(idx) // 2:], **kw)
     return regularize_mean_from_halfsets(m1, rhs1, lhs1, m2, rhs2, lhs2, mask=mask,
                                          do_grid_correction=kw.get("do_grid_correction", True))
+
+
+def reconstruct_mean_from_halfsets_DDP(dataset, ranks=None, **reconstruction_kwargs):
+    """Half-set mean across data-parallel ranks (reference ``mean.py:294-356``): each rank
+    backprojects the images of its shard (``dataset`` is this rank's DataLoader, e.g. with a
+    DistributedSampler), the ranks of each half-set group sum their partial rhs / lhs grids,
+    every rank receives both halves, and the regularised mean is solved on every rank.  With one
+    rank this is :func:`reconstruct_mean_from_halfsets` on the sampler's indices."""
+    import torch.distributed as dist
+
+    from .distributed import reduce_halfset_backprojections, world
+
+    if world() == 1 or (ranks is not None and len(ranks) == 1):
+        return reconstruct_mean_from_halfsets(dataset.dataset, idx=torch.tensor(list(iter(dataset.sampler))),
+                                              **reconstruction_kwargs)
+    kw = dict(reconstruction_kwargs)
+    kw["return_lhs_rhs"] = True
+    mean, rhs, lhs = reconstruct_mean(dataset, **kw)
+    half1, half2 = reduce_halfset_backprojections(rhs.contiguous(), lhs.contiguous(), mean.shape[-1], ranks)
+    return regularize_mean_from_halfsets(*half1, *half2, mask=kw.get("mask", None),
+                                         do_grid_correction=kw.get("do_grid_correction", True))

@@ -119,7 +119,7 @@ def vol_forward(volume: torch.Tensor, plan: Union[BaseNufftPlan, List[BaseNufftP
         if filters is not None:
             proj = proj * filters.unsqueeze(1)
         proj = proj / L
-    if proj.shape[0] == 1:
+    if proj.shape[1] == 1:  # one volume: the reference squeezes axis 0 (a no-op unless one image)
         proj = proj.squeeze(0)
     return centered_ifft2(proj).real if not fourier_domain else proj
 
@@ -141,3 +141,58 @@ def im_backward(image: torch.Tensor, plan: BaseNufftPlan, filters: Optional[torc
     im_fft = _nyquist_zero(im_fft)
     back = nufft_adjoint(im_fft, plan)
     return back.real / L if not fourier_domain else back / L
+
+
+def _set_pose(plan: BaseNufftPlan, poses: torch.Tensor) -> None:
+    """Points (B, 3, L^2) as the reference passes them, or rotation matrices (B, 3, 3) whose
+    points the kernels generate."""
+    if poses.ndim == 3 and tuple(poses.shape[-2:]) == (3, 3):
+        plan.setrot(poses)
+    else:
+        plan.setpts(poses)
+
+
+def preprocess_image_batch(images: torch.Tensor, nufft_plan: BaseNufftPlan, filters: torch.Tensor,
+                           pose: Tuple[torch.Tensor, torch.Tensor], mean_volume: torch.Tensor,
+                           mask: Optional[torch.Tensor] = None, mask_threshold: Optional[float] = None,
+                           softening_kernel_fourier: Optional[torch.Tensor] = None,
+                           fourier_domain: bool = False) -> torch.Tensor:
+    """Shift the images by their offsets, subtract the projected mean and apply the soft
+    projected mask (reference ``projection_funcs.py:199-252``).  ``pose`` is (points or
+    rotations, phase shift (B, L, L)); ``mean_volume`` / ``mask`` are in the domain the plan
+    expects (the upsampled centered Fourier grid for :class:`NufftPlanDiscretized`, spatial for
+    :class:`NufftPlan`).  The projections are one single-channel interpolation each (with the
+    CTF in its epilogue for the mean); the rest is 2D FFTs and elementwise work."""
+    pts_rot, phase_shift = pose
+    _set_pose(nufft_plan, pts_rot)
+    if not fourier_domain:
+        images = centered_fft2(images)
+    images = images * phase_shift
+    mean_forward = vol_forward(mean_volume, nufft_plan, filters=filters, fourier_domain=True)
+    if mean_forward.ndim == 4:
+        mean_forward = mean_forward.squeeze(1)
+    images = images - mean_forward
+    if mask is not None:
+        images = centered_ifft2(images).real
+        mask_forward = vol_forward(mask, nufft_plan, filters=None, fourier_domain=False).detach()
+        if mask_forward.ndim == 4:
+            mask_forward = mask_forward.squeeze(1)
+        mask_forward = mask_forward > mask_threshold
+        soft_mask = centered_ifft2(centered_fft2(mask_forward) * softening_kernel_fourier).real
+        images = images * soft_mask
+        if fourier_domain:
+            images = centered_fft2(images)
+    elif not fourier_domain:
+        images = centered_ifft2(images).real
+    return images
+
+
+def get_mask_threshold(mask: torch.Tensor, nufft_plan: BaseNufftPlan) -> float:
+    """10th percentile of the projected mask values above 10^-1.5 (reference
+    ``projection_funcs.py:255-269``), for the plan's current points."""
+    projected = vol_forward(mask, nufft_plan)
+    vals = projected.reshape(-1).detach().cpu().double()
+    vals = vals[vals > 10 ** (-1.5)]
+    import numpy as np
+
+    return float(np.percentile(vals.numpy(), 10))

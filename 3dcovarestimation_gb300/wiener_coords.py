@@ -3,7 +3,8 @@
 ``compute_latentMAP_batch`` runs the per-image Gram contractions in FP32 on the GPU and the
 r x r Hermitian solve (Cholesky) in FP64, one thread per image (reference
 ``wiener_coords.py:168-203``).  ``latentMAP`` loops over the dataset in batches like
-``wiener_coords.py:85-165``.
+``wiener_coords.py:85-165``; ``wiener_coords`` (``wiener_coords.py:13-82``) gives the same
+posterior mean through the same two kernels (see its docstring).
 """
 
 import math
@@ -13,7 +14,7 @@ import torch
 
 from . import _lib
 from .nufft_plan import NufftPlan, NufftPlanDiscretized
-from .projection_funcs import centered_fft3, vol_forward
+from .projection_funcs import _set_pose, centered_fft3, vol_forward
 
 
 def compute_latentMAP_batch(images: torch.Tensor, eigen_forward: torch.Tensor, noise_var: float,
@@ -58,11 +59,56 @@ def compute_latentMAP_batch(images: torch.Tensor, eigen_forward: torch.Tensor, n
     return z.real.to(dt).unsqueeze(-1), m.real.to(dt), b.real.to(dt).unsqueeze(-1)
 
 
+def wiener_coords(dataset, eigenvecs: torch.Tensor, eigenvals: torch.Tensor, batch_size: int = 1024,
+                  start_ind: Optional[int] = None, end_ind: Optional[int] = None, return_eigen_forward: bool = False,
+                  **nufft_plan_kwargs: Any):
+    """Wiener-filtered latent coordinates (reference ``wiener_coords.py:13-82``).
+
+    The reference takes, per image with projections A (r, P) and A^T = QR, the coordinates
+    Lambda R^T (R Lambda R^T + noise_var I)^-1 Q^T y.  Since R^T (R Lambda R^T + s I)^-1 R^-T =
+    (G Lambda + s I)^-1 with G = A A^T, this is Lambda (G Lambda + s I)^-1 A y, and with
+    Lambda = S S (S the symmetric square root) it is S (S G S / s + I)^-1 S A y / s: the
+    latent-MAP solve of the projections of the eigenvolumes scaled by S, with an identity prior,
+    then multiplied by S.  So no per-image QR is needed and Lambda may be singular; the Gram
+    contraction runs in FP32 and the r x r Cholesky solve in FP64 (``cov3d_gram`` +
+    ``cov3d_cost_solve``).  Points come from ``dataset[i:j]`` = (images, pts_rot, filters, idx);
+    images are spatial, like the reference's."""
+    start_ind = 0 if start_ind is None else start_ind
+    end_ind = len(dataset) if end_ind is None else end_ind
+    L = eigenvecs.shape[-1]
+    rank = eigenvecs.shape[0]
+    dtype, device = eigenvecs.dtype, eigenvecs.device
+    lam = eigenvals.to(device=device, dtype=torch.float64)
+    if lam.ndim == 1:
+        lam = torch.diag(lam)
+    w, U = torch.linalg.eigh((lam + lam.T) / 2)
+    S = (U * torch.sqrt(torch.clamp(w, min=0.0))) @ U.T  # symmetric square root of Lambda
+    scaled = torch.einsum("ij,jxyz->ixyz", S.to(torch.float32), eigenvecs.to(torch.float32)).contiguous()
+    plan = NufftPlan((L,) * 3, batch_size=rank, dtype=dtype, device=device, **nufft_plan_kwargs)
+    count = end_ind - start_ind
+    coords = torch.zeros((count, rank), device=device)
+    fwd = torch.zeros((count, rank, L, L), dtype=dtype) if return_eigen_forward else None
+    for i in range(0, count, batch_size):
+        images, pts_rot, filters, _ = dataset[start_ind + i: min(start_ind + i + batch_size, end_ind)]
+        images, pts_rot, filters = images.to(device), pts_rot.to(device), filters.to(device)
+        n = images.shape[0]
+        _set_pose(plan, pts_rot)
+        q = vol_forward(scaled, plan, filters)
+        if q.ndim == 3:
+            q = q.unsqueeze(0)
+        z, _, _ = compute_latentMAP_batch(images.reshape(n, -1), q.reshape(n, rank, -1), dataset.noise_var)
+        coords[i: i + n] = (z.squeeze(-1).real.to(torch.float64) @ S.T).to(coords.dtype)
+        if return_eigen_forward:
+            fwd[i: i + n] = vol_forward(eigenvecs, plan, filters).reshape(n, rank, L, L).to("cpu", dtype)
+    return (coords, fwd) if return_eigen_forward else coords
+
+
 def latentMAP(dataset, eigenvecs: torch.Tensor, eigenvals: torch.Tensor, batch_size: int = 1024,
               start_ind: Optional[int] = None, end_ind: Optional[int] = None, return_coords_covar: bool = False,
               nufft_plan: type = NufftPlan, **nufft_plan_kwargs: Any):
     """Latent coordinates for every image of ``dataset`` (reference ``wiener_coords.py:85-165``).
-    ``dataset[i:j]`` must return (images, pts_rot, filters, idx) and expose ``noise_var``."""
+    ``dataset[i:j]`` must return (images, pts_rot or rotations (B, 3, 3), filters, idx) and expose
+    ``noise_var``."""
     start_ind = 0 if start_ind is None else start_ind
     end_ind = len(dataset) if end_ind is None else end_ind
     L = eigenvecs.shape[-1]
@@ -85,7 +131,7 @@ def latentMAP(dataset, eigenvecs: torch.Tensor, eigenvals: torch.Tensor, batch_s
     for i in range(0, count, batch_size):
         images, pts_rot, filters, _ = dataset[start_ind + i: min(start_ind + i + batch_size, end_ind)]
         images, pts_rot, filters = images.to(device), pts_rot.to(device), filters.to(device)
-        plan.setpts(pts_rot)
+        _set_pose(plan, pts_rot)
         eig_fwd = vol_forward(vols, plan, filters)
         if eig_fwd.ndim == 3:
             eig_fwd = eig_fwd.unsqueeze(0)

@@ -8,8 +8,11 @@ upsampling 2, ML objective): on-the-fly points + bin sort, deapodise/pad + FFT3,
 interpolation with the fused projection epilogue, per-image Gram + FP64 solve, hand-written
 adjoint, compensated spreading, inverse FFT3, crop, Adam update.  Prints one JSON line.
 
-``--impl reference`` times the CPU port of the same step (oracle/cpu_step.py: float32 C
-loops with OpenMP + scipy FFT) on the host cores.
+``--impl reference`` times the reference's own step on the host cores: its
+``CovarTrainer.run_batch`` on ``NufftPlanDiscretized`` bilinear (the command line's default;
+its exact ES plan needs cuFINUFFT, which is not installed), imported unmodified from the copy
+``oracle/build_ref.py`` makes, whole steps of the same batch size.  Without that copy it
+falls back to the CPU port of the ES step (oracle/cpu_step.py), labelled ``kind: "port"``.
 """
 
 import argparse
@@ -28,7 +31,19 @@ sys.path.insert(0, ROOT)
 METRIC = "cov-SGD images/s (L=128,r=10)"
 WORKLOAD = ("cov-SGD step, GPU drop-in plain FP32 config: L=128, pixel 1.5 A, r=10 Gaussian-blob eigenvolumes, "
             "batch 1024, uniform SO(3) poses, CTF 300 kV / Cs 2.7 mm / AC 0.1 / defocus U[1,3] um, SNR 0.05, "
-            "NUFFT upsampling 2, ES width 6 (tol 1e-6), ML objective + Fourier regulariser, Adam")
+            "NUFFT upsampling 2, ML objective + Fourier regulariser, Adam")
+GPU_INTERP = "ES kernel width 6 (tol 1e-6), periodic, compensated FP32 spreading"
+REF_INTERP = ("reference NufftPlanDiscretized bilinear (grid_sample), the reference command line's default; its ES "
+              "plan (cuFINUFFT) is not installed")
+
+
+def shared_config(args, world):
+    """The workload both arms measure (identical dicts in the two JSON lines)."""
+    return {"workload": WORKLOAD, "global_batch": args.batch * world, "L": args.L, "rank": args.rank, "upsample": 2,
+            "objective": "ml + Fourier regulariser", "optimizer": "Adam", "snr": 0.05, "seed": args.seed,
+            "l2": "inputs larger than L2: each GPU step reads a distinct resident 1024-image batch "
+                  "(134 MB images + 67 MB CTF) and 1.34 GB fine grids",
+            "parallelism": f"dp{world}"}
 
 
 def parse():
@@ -43,7 +58,10 @@ def parse():
     ap.add_argument("--width", type=int, default=6)
     ap.add_argument("--resident-batches", type=int, default=16)
     ap.add_argument("--e2e-steps", type=int, default=0, help="0 = same as --steps")
-    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--cpu-seconds", type=float, default=8.0, help="per-image sample of the ES CPU port")
+    ap.add_argument("--ref-batch", type=int, default=128, help="images per reference step in the GPU arm's baseline")
+    ap.add_argument("--ref-budget", type=float, default=150.0,
+                    help="seconds of timed reference steps in --impl reference (whole steps, at least one)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--seed", type=int, default=2000)
     ap.add_argument("--uncompensated", action="store_true", help="plain FP32 spreading (no TwoSum error terms)")
@@ -54,6 +72,7 @@ def parse():
     ap.add_argument("--no-mean", action="store_true", help="skip the mean-CG measurement")
     ap.add_argument("--no-bf16", action="store_true", help="skip the BF16-Gram variant of the step")
     ap.add_argument("--no-wiener", action="store_true", help="skip the Wiener-coordinate measurement")
+    ap.add_argument("--no-bilinear", action="store_true", help="skip the bilinear-interpolation step")
     return ap.parse_args()
 
 
@@ -61,22 +80,34 @@ def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
-def cpu_baseline(args):
+def cpu_baseline_port(args):
+    """The CPU port of the ES step (oracle/cpu_step.py: float32 C + OpenMP loops, scipy FFT) on a
+    bounded sample: the per-step FFT part timed once, the per-image part on a sample of images."""
     from oracle import cpu_step
 
     threads = os.cpu_count()
-    # a discarded warm-up call (thread pools, FFT plans), then a probe that sizes the sample so
-    # the per-image part takes about cpu_seconds
     cpu_step.time_baseline(args.L, args.rank, args.batch, 2, args.width, real="float", threads=threads)
     _, probe = cpu_step.time_baseline(args.L, args.rank, args.batch, 4, args.width, real="float", threads=threads)
     sample = int(max(2, min(256, args.cpu_seconds / max(probe["t_image_s"], 1e-6))))
     ips, det = cpu_step.time_baseline(args.L, args.rank, args.batch, sample, args.width, real="float",
                                       seed=args.seed, threads=threads)
     return {"value": ips, "unit": "images/s", "cores": threads, "kind": "port",
-            "sample": (f"per-step part (pad + FFT3 + iFFT3 + crop, {det['t_step_s']:.2f} s) timed once and the "
-                       f"per-image part (points, ES interp, Gram/solve, adjoint, ES spread) on {sample} images "
-                       f"({det['t_image_s'] * 1e3:.1f} ms/image); images/s = {args.batch} / (t_step + "
+            "sample": (f"CPU port of the ES step: per-step part (pad + FFT3 + iFFT3 + crop, {det['t_step_s']:.2f} s) "
+                       f"timed once and the per-image part (points, ES interp, Gram/solve, adjoint, ES spread) on "
+                       f"{sample} images ({det['t_image_s'] * 1e3:.1f} ms/image); images/s = {args.batch} / (t_step + "
                        f"{args.batch} * t_image); float32 C + OpenMP, scipy.fft workers={threads}")}
+
+
+def cpu_baseline_reference(args, batch, steps, warmup, budget_s):
+    """Whole steps of the reference's own trainer (oracle/ref_step.py) on the host cores."""
+    from oracle import ref_step
+
+    ips, det = ref_step.time_steps(args.L, args.rank, batch, steps, warmup, seed=args.seed, budget_s=budget_s)
+    return {"value": ips, "unit": "images/s", "cores": det["threads"], "kind": "reference",
+            "sample": (f"{det['steps']} whole step(s) of {batch} images after {det['warmup']} warm-up step(s): the "
+                       f"reference's CovarTrainer.run_batch (setpts + Covar Fourier view + grid_sample projection + "
+                       f"cost_maximum_liklihood_fourier_domain + backward + Adam) on NufftPlanDiscretized bilinear, "
+                       f"torch CPU threads={det['threads']}, {det['seconds']:.1f} s timed")}, det
 
 
 def run_reference(args):
@@ -84,11 +115,22 @@ def run_reference(args):
     if rank != 0:
         return
     t0 = time.perf_counter()
-    cb = cpu_baseline(args)
+    from oracle import ref_step
+
+    if ref_step.available():
+        cb, det = cpu_baseline_reference(args, args.batch, args.steps, args.warmup, args.ref_budget)
+        steps, warmup = det["steps"], det["warmup"]
+        ms_step = det["seconds"] / steps * 1e3
+        interp = REF_INTERP
+    else:
+        cb = cpu_baseline_port(args)
+        steps, warmup = 1, 0
+        ms_step = args.batch / cb["value"] * 1e3
+        interp = "CPU port of the ES step (reference package not installed under oracle/_ref)"
     line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "images/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": args.batch / cb["value"] * 1e3,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "global_batch": args.batch, "L": args.L, "rank": args.rank},
+            "steps": steps, "warmup": warmup, "steps_requested": args.steps, "warmup_requested": args.warmup,
+            "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": shared_config(args, world), "interpolation": interp,
             "cpu_baseline": cb,
             "e2e": {"value": cb["value"], "unit": "images/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "wall_s": time.perf_counter() - t0}
@@ -435,6 +477,61 @@ def run_gb300(args):
                 "note": "Gram contractions in BF16 with FP32 accumulation (tcgen05); projections, spreading, "
                         "solve and update unchanged (FP32 / FP64)"}
 
+    # the same step on the reference's default interpolation (NufftPlanDiscretized bilinear,
+    # grid_sample semantics): the like-for-like comparison with the reference's CPU arm
+    bilinear = None
+    if not args.no_bilinear:
+        step_bl = pkg.FusedCovarStep(L, r, "bilinear", 2, device=dev, compensated=not args.uncompensated)
+        covar_bl = pkg.Covar(L, r, upsampling_factor=2).to(dev)
+        covar_bl.vectors.grad = torch.zeros_like(covar_bl.vectors)
+        covar_bl.log_sqrt_eigenvals.grad = torch.zeros_like(covar_bl.log_sqrt_eigenvals)
+        opt_bl = torch.optim.Adam([{"params": covar_bl.vectors, "lr": 1e-6 * B},
+                                   {"params": covar_bl.log_sqrt_eigenvals, "lr": 1e-4 * B}])
+
+        def step_bilinear(k, imgs=None, ctfs=None, rots=None):
+            b = (k * world + rank) % nb
+            step_bl.set_rotations(rot[b] if rots is None else rots)
+            c, _, _ = step_bl(covar_bl.vectors.detach(), covar_bl.log_sqrt_eigenvals.detach(),
+                              images[b] if imgs is None else imgs, ctf[b] if ctfs is None else ctfs, noise_var,
+                              reg_scale, fourier_reg, grad_vectors=covar_bl.vectors.grad,
+                              grad_log_sqrt=covar_bl.log_sqrt_eigenvals.grad)
+            dp.allreduce_mean_([covar_bl.vectors.grad, covar_bl.log_sqrt_eigenvals.grad])
+            opt_bl.step()
+            return c.reshape(())
+
+        for k in range(args.warmup):
+            step_bilinear(k)
+        barrier()
+        step_bl.plan.timing(True)
+        g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        g0.record(stream)
+        for k in range(args.steps):
+            step_bilinear(k)
+        g1.record(stream)
+        barrier()
+        phbl = step_bl.plan.timing_read()
+        step_bl.plan.timing(False)
+        msbl = g0.elapsed_time(g1) / args.steps
+        # end to end with host buffers, copies inside the timed region (as the headline e2e)
+        barrier()
+        t0 = time.perf_counter()
+        h2d(0)
+        for k in range(e2e_steps):
+            if k + 1 < e2e_steps:
+                h2d(k + 1)
+            slot = k % 2
+            stream.wait_event(ready[slot])
+            c = step_bilinear(k, *bufs[slot])
+            free[slot].record(stream)
+            h_cost[k:k + 1].copy_(c.reshape(1), non_blocking=True)
+        barrier()
+        e2e_bl = world * B * e2e_steps / (time.perf_counter() - t0)
+        bilinear = {"images_per_s": world * B / (msbl / 1e3), "ms_per_step": msbl, "steps": args.steps,
+                    "e2e_images_per_s": e2e_bl,
+                    "phases_ms_per_step": {k: v[0] / args.steps for k, v in phbl.items() if v[1]},
+                    "note": "fused step on NufftPlanDiscretized bilinear semantics (grid_sample, 8 taps), the "
+                            "same interpolation as the reference arm"}
+
     # Wiener / latent-MAP coordinates of the resident images with the current eigenvolumes
     # (wiener_coords.latentMAP's per-batch work: projections + FP32 Gram + FP64 Cholesky solve)
     wiener = None
@@ -487,12 +584,9 @@ def run_gb300(args):
         "metric": METRIC, "value": value, "unit": "images/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "global_batch": B * world, "L": L, "rank": r, "upsample": 2,
-                   "es_width": args.width, "resident_images": nb * B,
-                   "spreading": "fp32" if args.uncompensated else "fp32 + TwoSum compensation",
-                   "l2": "inputs larger than L2: each step reads a distinct resident 1024-image batch "
-                         "(134 MB images + 67 MB CTF) and 1.34 GB fine grids",
-                   "parallelism": f"dp{world}", "seed": args.seed},
+        "config": shared_config(args, world),
+        "interpolation": GPU_INTERP, "resident_images": nb * B,
+        "spreading": "fp32" if args.uncompensated else "fp32 + TwoSum compensation",
         "roofline": {"bound": "hbm", "kernel": kernel_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind, "traffic": load_traffic(kernel_name),
                      "algorithmic_bytes_per_launch": alg[dom], "ms_per_launch": dom_ms,
@@ -510,8 +604,12 @@ def run_gb300(args):
         line["wiener_coords"] = wiener
     if not args.no_mean:
         line["mean_cg"] = run_mean_cg(pkg, args, dev)
+    if bilinear is not None:
+        line["bilinear_step"] = bilinear
     if not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(args)
+        cb, _ = cpu_baseline_reference(args, args.ref_batch, 1, 1, 1e9)
+        line["cpu_baseline"] = cb
+        line["cpu_baseline_es_port"] = cpu_baseline_port(args)
     print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist

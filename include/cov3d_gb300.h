@@ -313,7 +313,13 @@ int cov3d_resample3d(void *stream, const float *d_in, int64_t NC, int d, int D, 
  * allocate device memory: their own pool owns the GPU, or cudaMalloc's device-wide
  * synchronisation is not acceptable on their call path.  The intermediates live in a 4 MiB
  * file-scope device array that each GPU loading the library keeps until exit; the call
- * allocates nothing (no cudaMalloc / cudaFree / allocating library routine).
+ * allocates nothing (no cudaMalloc / cudaFree / allocating library routine).  Two caveats:
+ * the first launch of the solve kernel at a given rank may make the driver enlarge its
+ * per-thread local-memory reservation (the kernel's r x r working arrays), so warm up once
+ * at the largest rank you will use; and the array's device address is looked up once per
+ * device and kept, which assumes the runtime's primary context on that device for the life
+ * of the process (after cudaDeviceReset, or with another context current, the kept address
+ * is stale: do not call this entry point then).
  * Limit: n_images * (8 r^2 + 8 r + 4) bytes plus alignment must fit in 4 MiB (e.g. 4,700
  * images at r = 10); larger requests return COV3D_EINVAL with the limit in the message.
  * The first call on each device looks up the array's device address (cudaGetSymbolAddress)

@@ -156,3 +156,65 @@ def time_baseline(L, r, batch, sample_images, width=6, real="float", seed=0, thr
     ips = batch / (t_step + batch * t_image)
     return ips, {"t_step_s": t_step, "t_image_s": t_image, "sample_images": sample_images,
                  "threads": step.threads, "real": real}
+
+
+def _centered_fft3_f64(x, n, threads):
+    """centered_fft3 of x (L, L, L) zero-padded to n (``projection_funcs.py:148-165``), float64."""
+    ax = (0, 1, 2)
+    p = O.pad_center(np.asarray(x, np.complex128), n, ax)
+    return np.fft.fftshift(_fftn(np.fft.ifftshift(p, axes=ax), ax, workers=threads), axes=ax)
+
+
+def _adjoint_fft3_f64(g, L, threads):
+    """Adjoint of :func:`_centered_fft3_f64`: n^3 * centered_ifft3 then crop to L."""
+    ax = (0, 1, 2)
+    n = g.shape[0]
+    back = np.fft.fftshift(_fftn(np.fft.ifftshift(g, axes=ax), ax, inverse=True, workers=threads), axes=ax)
+    return O.crop_center(back, L, ax) * float(n) ** 3
+
+
+def covar_cost_grad_es(vectors, log_sqrt, rotmats, images, ctf, noise_var, width=6, upsample=2, reg_scale=0.0,
+                       fourier_reg=None, threads=None, cost_only=False):
+    """Float64 ES-kernel ML covariance cost and its gradient w.r.t. (vectors, log_sqrt), the
+    same mathematics as ``nufft_oracle.covar_cost_grad(kind="es", objective="ml")`` (restating
+    ``Covar.get_vectors_fourier_domain``, covar.py:440-449, and
+    ``cost_maximum_liklihood_fourier_domain``, covar_sgd.py:1350-1378), organised one channel
+    at a time so that fine grids of 256^3 and 512^3 fit: per channel a centered FFT, the C
+    interpolation, and in the backward the C spreading, the regulariser and the inverse FFT.
+    Returns (cost, g_vectors (r, L, L, L), g_logsqrt (r,)) or the cost alone."""
+    threads = threads or os.cpu_count()
+    vectors = np.asarray(vectors, np.float64)
+    r, L = vectors.shape[0], vectors.shape[-1]
+    n = upsample * L
+    B = len(rotmats)
+    P = L * L
+    beta = O.es_beta(width, upsample)
+    gc = O.grid_correction_es(L, n, width, beta)
+    scale = np.exp(np.asarray(log_sqrt, np.float64))
+    V = vectors * scale[:, None, None, None]
+    t = O.es_index(O.rotated_points(np.asarray(rotmats, np.float64), L), n)
+    fr = None if fourier_reg is None or reg_scale == 0 else np.asarray(fourier_reg, np.float64)
+    Q = np.empty((B * P, r), np.complex128)
+    reg = 0.0
+    for ch in range(r):
+        G = _centered_fft3_f64(V[ch] / gc, n, threads)
+        Q[:, ch] = c_interp(G[..., None], t, width, beta, "double", threads)[:, 0]
+        if fr is not None:
+            reg += float(np.sum(np.abs(G) ** 2 * fr))
+        del G
+    sp = (np.asarray(ctf, np.float64).reshape(B, P) * O.nyquist_mask(L).reshape(1, P)) / L
+    Qb = Q.reshape(B, P, r).transpose(0, 2, 1) * sp[:, None, :]
+    y = np.asarray(images, np.complex128).reshape(B, P)
+    per, W = O.ml_cost_and_w(Qb, y, noise_var)
+    cost = float(np.mean(per)) + reg_scale * reg / noise_var / 2.0
+    if cost_only:
+        return cost
+    vals = (W / B * sp[:, None, :]).transpose(0, 2, 1).reshape(-1, r)
+    gV = np.empty_like(V)
+    for ch in range(r):
+        gg = c_spread(np.ascontiguousarray(vals[:, ch:ch + 1]), t, n, width, beta, "double", threads)[..., 0]
+        if fr is not None:
+            gg += (reg_scale / noise_var / 2.0) * fr * _centered_fft3_f64(V[ch] / gc, n, threads)
+        gV[ch] = 2.0 * np.real(_adjoint_fft3_f64(gg, L, threads)) / gc
+        del gg
+    return cost, gV * scale[:, None, None, None], np.sum(gV * V, axis=(1, 2, 3))

@@ -1,9 +1,10 @@
 """Import shim that lets the reference COV3D package (pure Python / PyTorch) import on a
 machine without its heavy third-party dependencies.
 
-Only used by ``make_golden.py`` in the development container, where the reference
-source tree is mounted read-only.  It is never imported by the product, the GPU tests,
-``smoke()`` or ``bench.py``.
+Test infrastructure only.  Used by ``tests/golden/make_golden.py`` (fixtures from the
+reference run in float64) and by ``oracle/ref_step.py``, the timed CPU baseline of
+``bench.py`` that runs the reference's own torch step from the copy ``oracle/build_ref.py``
+makes under ``oracle/_ref/``.  The product package never imports it.
 
 What it does:
 

@@ -1,12 +1,12 @@
 """Generate the golden fixtures under ``tests/golden/`` by running the reference COV3D code
 (pure PyTorch, CPU, float64) on small seeded inputs.
 
-Run in the development container only (the reference tree is not present on GPU machines):
+Run where the reference source tree is available (it is not needed by the tests):
 
-    python tests/golden/make_golden.py [/path/to/reference]
+    python tests/golden/make_golden.py /path/to/reference [case_function]
 
-The reference is imported unmodified through ``ref_shim`` (placeholder modules for its
-unused third-party dependencies).  Every fixture stores its inputs next to the reference's
+The reference is imported unmodified through ``oracle/ref_shim.py`` (placeholder modules for
+its unused third-party dependencies).  Every fixture stores its inputs next to the reference's
 outputs, so the tests never need the reference itself.
 
 Cases (reference file:line of the function that produced each output):
@@ -42,10 +42,12 @@ import numpy as np
 import torch
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"  # optional second argument: one case
+if len(sys.argv) < 2:
+    sys.exit("usage: make_golden.py /path/to/reference [case_function]")
+REF = sys.argv[1]
 
-sys.path.insert(0, HERE)
-import ref_shim  # noqa: E402
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+from oracle import ref_shim  # noqa: E402
 
 ref_shim.install(REF)
 
@@ -335,6 +337,238 @@ def case_halfsets(L=10, r=3, seed=31):
     save(f"halfsets_L{L}.npz", **out)
 
 
+class ExactNufftPlan(nufft_plan.NufftPlan):
+    """Float64 stand-in for the reference's cuFINUFFT plan, used only to generate fixtures for
+    the reference functions that construct or expect a ``NufftPlan`` (the spatial-domain costs,
+    ``wiener_coords``, ``latentMAP`` with its default plan): the exact NUDFT
+    ``F(w) = sum_k V[k] exp(-i w.k)``, ``k = j - L//2`` per axis, which cuFINUFFT approximates
+    to ``eps`` (modes centered, point row d paired with volume axis d).  It keeps the reference
+    plan's attributes, point wrapping and output shapes (``nufft_plan.py:318-392``); being a
+    subclass, the reference's ``nufft_forward`` / ``nufft_adjoint`` wrap it in their autograd
+    functions exactly as they wrap the real plan."""
+
+    def __init__(self, sz, batch_size=1, eps=1e-6, dtype=torch.float64, device=torch.device("cpu"), **kwargs):
+        self.sz, self.batch_size, self.device = sz, batch_size, device
+        self.dtype, self.complex_dtype = torch.float64, torch.complex128
+
+    def setpts(self, points):
+        self.points_N = points.shape[0]
+        self.points_L = int(round(points.shape[-1] ** 0.5))
+        pts = points.transpose(0, 1).reshape((3, -1)).to(torch.float64)
+        self.points = (torch.remainder(pts + torch.pi, 2 * torch.pi) - torch.pi).contiguous()
+        L = self.sz[0]
+        k = torch.arange(L, dtype=torch.float64) - L // 2
+        k0, k1, k2 = torch.meshgrid(k, k, k, indexing="ij")
+        ph = (self.points[0][:, None] * k0.reshape(1, -1) + self.points[1][:, None] * k1.reshape(1, -1)
+              + self.points[2][:, None] * k2.reshape(1, -1))
+        self._E = torch.exp(-1j * ph)
+
+    def execute_forward(self, signal):
+        B = signal.shape[0]
+        out = signal.reshape(B, -1).to(torch.complex128) @ self._E.T
+        return out.reshape(B, self.points_N, self.points_L, self.points_L)
+
+    def execute_adjoint(self, signal):
+        B = signal.shape[0]
+        out = signal.reshape(B, -1).to(torch.complex128) @ self._E.conj()
+        return out.reshape((B, *self.sz))
+
+
+def case_spatial_costs(L=10, r=3, B=6, seed=41):
+    """cost / cost_maximum_liklihood (covar_sgd.py:1190-1286): spatial eigenvolumes through an
+    exact plan, spatial images, with and without the Fourier regulariser, autograd gradients."""
+    rng = np.random.default_rng(seed)
+    vectors = rng.standard_normal((r, L, L, L)).astype(np.float32) * 0.1
+    rotvecs = random_rotvecs(rng, B)
+    pts, _ = ref_points(rotvecs, np.zeros((B, 2), np.float32), L)
+    images = (rng.standard_normal((B, L, L)) * 3).astype(np.float32)
+    filters = rng.uniform(0.2, 1.5, (B, L, L)).astype(np.float32)
+    fourier_reg = rng.uniform(0.5, 2.0, (L, L, L)).astype(np.float32)
+    noise_var, reg_scale = 2.5, 0.3
+    out = dict(L=L, r=r, vectors=vectors, rotvecs=rotvecs, pts=pts.numpy(), images=images, filters=filters,
+               fourier_reg=fourier_reg, noise_var=noise_var, reg_scale=reg_scale)
+    plan = ExactNufftPlan((L,) * 3, batch_size=r)
+    plan.setpts(pts)
+    ims = torch.tensor(images, dtype=torch.float64)
+    filt = torch.tensor(filters, dtype=torch.float64)
+    freg = torch.tensor(fourier_reg, dtype=torch.float64)
+    for name, fn in (("ml", covar_sgd.cost_maximum_liklihood), ("ls", covar_sgd.cost)):
+        for with_reg in (False, True):
+            covar = Covar(L, r, dtype=torch.float64, vectors=torch.tensor(vectors, dtype=torch.float64))
+            kw = dict(reg_scale=reg_scale, fourier_reg=freg) if with_reg else {}
+            c = fn(covar.get_vectors_spatial_domain(), ims, plan, filt, noise_var, **kw)
+            c.backward()
+            tag = f"{name}{'_reg' if with_reg else ''}"
+            out[f"{tag}_cost"] = c.detach().numpy()
+            out[f"{tag}_grad_vectors"] = covar.vectors.grad.numpy()
+            out[f"{tag}_grad_logsqrt"] = covar.log_sqrt_eigenvals.grad.numpy()
+            per = fn(covar.get_vectors_spatial_domain(), ims, plan, filt, noise_var, mean_aggregate=False, **kw)
+            out[f"{tag}_per_image"] = per.detach().numpy()
+    out["log_sqrt_eigenvals"] = covar.log_sqrt_eigenvals.detach().numpy()
+    out["vectors_normalised"] = covar.vectors.detach().numpy()
+    save(f"spatial_cost_L{L}_r{r}.npz", **out)
+
+
+class _TrainData(torch.utils.data.Dataset):
+    """What CovarTrainer reads from its dataset (images, pts_rot, filters, idx; mask; noise_var)."""
+
+    def __init__(self, images, pts, filters, noise_var):
+        self.images, self.pts_rot, self.filters, self.noise_var = images, pts, filters, noise_var
+        self.mask = None
+
+    def __len__(self):
+        return len(self.images)
+
+    def __getitem__(self, idx):
+        return self.images[idx], self.pts_rot[idx], self.filters[idx], idx
+
+    def to_fourier_domain(self):
+        pass
+
+    def to_spatial_domain(self):
+        pass
+
+
+def case_trainer(L=10, r=3, B=4, nbatch=2, seed=51):
+    """Two CovarTrainer.run_batch steps (covar_sgd.py:199-229) after setup_training
+    (covar_sgd.py:302-358; bilinear plan, ML objective, Adam) and compute_fourier_reg_term
+    (covar_sgd.py:420-430): cost of each step and the parameters after each Adam update."""
+    rng = np.random.default_rng(seed)
+    N = B * nbatch
+    vectors = rng.standard_normal((r, L, L, L)).astype(np.float32) * 0.1
+    reg_vecs = rng.standard_normal((r, L, L, L)).astype(np.float32) * 0.1
+    rotvecs = random_rotvecs(rng, N)
+    pts, _ = ref_points(rotvecs, np.zeros((N, 2), np.float32), L)
+    images = c32(rng, (N, L, L)) * np.float32(3.0)
+    filters = rng.uniform(0.2, 1.5, (N, L, L)).astype(np.float32)
+    noise_var, lr, reg = 7.5, 1e-3, 1.0
+    ds = _TrainData(torch.tensor(images).to(torch.complex128), pts, torch.tensor(filters, dtype=torch.float64),
+                    noise_var)
+    loader = torch.utils.data.DataLoader(ds, batch_size=B, shuffle=False)
+    covar = Covar(L, r, dtype=torch.float64, fourier_domain=True, vectors=torch.tensor(vectors, dtype=torch.float64))
+    trainer = covar_sgd.CovarTrainer(covar, loader, torch.device("cpu"))
+    trainer.setup_training(lr=lr, optim_type="Adam", reg=reg, nufft_disc="bilinear", objective_func="ml")
+    trainer.compute_fourier_reg_term(torch.tensor(reg_vecs, dtype=torch.float64))
+    out = dict(L=L, r=r, B=B, vectors=vectors, reg_vecs=reg_vecs, rotvecs=rotvecs, pts=pts.numpy(), images=images,
+               filters=filters, noise_var=noise_var, lr=lr, reg=reg, reg_scale=trainer.reg_scale,
+               fourier_reg=trainer.fourier_reg.numpy())
+    costs = []
+    for k, batch in enumerate(loader):
+        im, p, f = trainer.prepare_batch(batch)
+        costs.append(float(trainer.run_batch(im, p, f)))
+        out[f"step{k}_vectors"] = covar.vectors.detach().numpy().copy()
+        out[f"step{k}_log_sqrt"] = covar.log_sqrt_eigenvals.detach().numpy().copy()
+    out["costs"] = np.array(costs)
+    save(f"trainer_L{L}_r{r}.npz", **out)
+
+
+class _LatentData:
+    """What latentMAP / wiener_coords read from their dataset."""
+
+    def __init__(self, images, pts, filters, noise_var):
+        self.images, self.pts, self.filters, self.noise_var = images, pts, filters, noise_var
+
+    def __len__(self):
+        return len(self.images)
+
+    def __getitem__(self, idx):
+        return self.images[idx], self.pts[idx], self.filters[idx], idx
+
+
+def case_latent_dataset(L=10, r=3, N=40, batch=16, seed=61):
+    """latentMAP (wiener_coords.py:85-165) over a small dataset in ragged batches (16, 16, 8),
+    with the discretized bilinear plan and with the exact plan; wiener_coords
+    (wiener_coords.py:13-82, the per-image QR form) with the exact plan."""
+    rng = np.random.default_rng(seed)
+    rotvecs = random_rotvecs(rng, N)
+    pts, _ = ref_points(rotvecs, np.zeros((N, 2), np.float32), L)
+    eig = rng.standard_normal((r, L * L * L))
+    eig, _ = np.linalg.qr(eig.T)
+    eig = eig.T.reshape(r, L, L, L)
+    eigenvals = np.array([9.0, 4.0, 1.5])[:r]
+    filters = rng.uniform(0.2, 1.5, (N, L, L))
+    noise_var = 0.05
+    # images: projections of the eigenvolumes with N(0, eigenvals) coordinates, plus noise
+    plan = ExactNufftPlan((L,) * 3, batch_size=r)
+    plan.setpts(pts)
+    proj = projection_funcs.vol_forward(torch.tensor(eig), plan, torch.tensor(filters))
+    z = rng.standard_normal((N, r)) * np.sqrt(eigenvals)
+    images = np.einsum("nr,nrij->nij", z, proj.numpy()) + rng.standard_normal((N, L, L)) * np.sqrt(noise_var)
+    ds = _LatentData(torch.tensor(images), pts, torch.tensor(filters), noise_var)
+    e_t, l_t = torch.tensor(eig), torch.tensor(eigenvals)
+    out = dict(L=L, r=r, N=N, batch=batch, rotvecs=rotvecs, pts=pts.numpy(), eigenvecs=eig, eigenvals=eigenvals,
+               filters=filters, noise_var=noise_var, images=images, z_true=z)
+    c, cov = wiener_coords.latentMAP(ds, e_t, l_t, batch_size=batch, return_coords_covar=True,
+                                     nufft_plan=nufft_plan.NufftPlanDiscretized)
+    out["map_bilinear"], out["map_bilinear_covar"] = c.numpy(), cov.numpy()
+    saved = wiener_coords.NufftPlan
+    wiener_coords.NufftPlan = ExactNufftPlan
+    try:
+        c, cov = wiener_coords.latentMAP(ds, e_t, l_t, batch_size=batch, return_coords_covar=True,
+                                         nufft_plan=ExactNufftPlan)
+        out["map_exact"], out["map_exact_covar"] = c.numpy(), cov.numpy()
+        out["wiener_exact"] = wiener_coords.wiener_coords(ds, e_t, l_t, batch_size=batch).numpy()
+    finally:
+        wiener_coords.NufftPlan = saved
+    save(f"latent_dataset_L{L}_r{r}.npz", **out)
+
+
+def case_preprocess(L=10, us=2, B=6, seed=71):
+    """preprocess_image_batch (projection_funcs.py:199-252) with the discretized bilinear plan:
+    phase shift, projected-mean subtraction, and the soft mask from the projected volume mask
+    (get_mask_threshold, projection_funcs.py:255-269; soft_edged_kernel, utils.py:258-300)."""
+    from cov3d import utils
+
+    rng = np.random.default_rng(seed)
+    n = L * us
+    rotvecs = random_rotvecs(rng, B)
+    offsets = rng.uniform(-2, 2, (B, 2)).astype(np.float32)
+    pts, phase = ref_points(rotvecs, offsets, L)
+    images = (rng.standard_normal((B, L, L)) * 2).astype(np.float32)
+    filters = rng.uniform(0.2, 1.5, (B, L, L)).astype(np.float32)
+    mean_vol = rng.standard_normal((L, L, L)).astype(np.float32)
+    ax = np.arange(L) - L // 2
+    zz, yy, xx = np.meshgrid(ax, ax, ax, indexing="ij")
+    mask_vol = (np.sqrt(zz**2 + yy**2 + xx**2) < 0.35 * L).astype(np.float32)
+    plan = nufft_plan.NufftPlanDiscretized((L,) * 3, upsample_factor=us, mode="bilinear")
+    mean_f = projection_funcs.centered_fft3(torch.tensor(mean_vol, dtype=torch.float64).unsqueeze(0),
+                                            padding_size=(n,) * 3)
+    mask_f = projection_funcs.centered_fft3(torch.tensor(mask_vol, dtype=torch.float64).unsqueeze(0),
+                                            padding_size=(n,) * 3)
+    plan.setpts(pts)
+    thr = projection_funcs.get_mask_threshold(mask_f, plan)
+    soft = utils.soft_edged_kernel(radius=5, L=L, dim=2, in_fourier=True)
+    ims = torch.tensor(images, dtype=torch.float64)
+    filt = torch.tensor(filters, dtype=torch.float64)
+    nomask = projection_funcs.preprocess_image_batch(ims, plan, filt, (pts, phase), mean_f)
+    masked = projection_funcs.preprocess_image_batch(ims, plan, filt, (pts, phase), mean_f, mask_f, thr, soft)
+    masked_f = projection_funcs.preprocess_image_batch(ims, plan, filt, (pts, phase), mean_f, mask_f, thr, soft,
+                                                       fourier_domain=True)
+    save(f"preprocess_L{L}.npz", L=L, us=us, rotvecs=rotvecs, offsets=offsets, pts=pts.numpy(),
+         phase=phase.numpy(), images=images, filters=filters, mean_vol=mean_vol, mask_vol=mask_vol,
+         mask_threshold=np.array(thr), soft_kernel_fourier=soft.numpy(), nomask=nomask.numpy(),
+         masked=masked.numpy(), masked_fourier=masked_f.numpy())
+
+
+def case_state_dict(L=6, r=2, seed=81):
+    """The reference Covar's state_dict (covar.py:82-112) and CovarTrainer.results_dict
+    (covar_sgd.py:524-535) key sets, with values, for checkpoint compatibility tests."""
+    rng = np.random.default_rng(seed)
+    vectors = rng.standard_normal((r, L, L, L))
+    covar = Covar(L, r, dtype=torch.float64, fourier_domain=True, vectors=torch.tensor(vectors))
+    covar.init_grid_correction("bilinear")
+    sd = covar.state_dict()
+    out = {"L": L, "r": r, "vectors_init": vectors, "keys": np.array(sorted(sd.keys()))}
+    for k, v in sd.items():
+        if torch.is_tensor(v):
+            out["sd_" + k] = v.numpy()
+        elif v is not None:
+            out["sd_" + k] = np.array(v)
+    eig, lam = covar.eigenvecs
+    out["eigenvecs"], out["eigenvals"] = eig.numpy(), lam.numpy()
+    save(f"state_dict_L{L}_r{r}.npz", **out)
+
+
 if __name__ == "__main__":
     if len(sys.argv) > 2:
         globals()[sys.argv[2]]()
@@ -350,3 +584,8 @@ if __name__ == "__main__":
     case_cg()
     case_mean()
     case_halfsets()
+    case_spatial_costs()
+    case_trainer()
+    case_latent_dataset()
+    case_preprocess()
+    case_state_dict()

@@ -130,3 +130,95 @@ def test_latent_map_matches_reference(pkg, dev):
                                                         float(g["noise_var"]),
                                                         torch.tensor(g["eigenvals_inv"], device=dev))
     assert rel(z, g["z_real"]) < TOL_COST and rel(m, g["m_real"]) < TOL_COST
+
+
+def _es_case(L, r, B, seed):
+    rng = np.random.default_rng(seed)
+    vec = rng.standard_normal((r, L, L, L))
+    vec /= np.linalg.norm(vec.reshape(r, -1), axis=1)[:, None, None, None]
+    vec = vec.astype(np.float32)
+    ls = np.log(rng.uniform(2.0, 6.0, r)).astype(np.float32)
+    R = O.rotvec_to_rotmat(rng.standard_normal((B, 3))).astype(np.float32)
+    imgs = ((rng.standard_normal((B, L, L)) + 1j * rng.standard_normal((B, L, L))) * 3).astype(np.complex64)
+    ctf = rng.uniform(0.2, 1.3, (B, L, L)).astype(np.float32)
+    fr = rng.uniform(0.5, 2.0, (2 * L,) * 3).astype(np.float32)
+    return vec, ls, R, imgs, ctf, fr
+
+
+# the benchmark's own kernels at the benchmark's shapes: L = 128 (fine grid 256^3) with r = 10
+# (interp_kernel<ES,6,5>, spread_rows_kernel<ES,6,5,3,1>, the n = 256 line DFTs) and r = 20, and
+# L = 256 (fine grid 512^3, the full-pipeline configuration); the float64 reference is the
+# channel-streamed ES step of oracle/cpu_step.py (C loops + scipy FFTs)
+@pytest.mark.parametrize("L,r,B", [(128, 10, 4), (128, 20, 2), (256, 10, 1)])
+def test_fused_es_step_headline_shapes_match_fp64(pkg, dev, L, r, B):
+    from oracle import cpu_step
+
+    vec, ls, R, imgs, ctf, fr = _es_case(L, r, B, 7 * L + r)
+    step = pkg.FusedCovarStep(L, r, "nufft", 2, width=6, device=dev)
+    step.set_rotations(torch.tensor(R, device=dev))
+    val, gv, gl = step(torch.tensor(vec, device=dev), torch.tensor(ls, device=dev),
+                       torch.tensor(imgs, device=dev).reshape(B, -1), torch.tensor(ctf, device=dev).reshape(B, -1),
+                       5.0, reg_scale=0.01, fourier_reg=torch.tensor(fr, device=dev), sync_cost=True)
+    gv, gl = gv.cpu().numpy(), gl.cpu().numpy()
+    del step
+    torch.cuda.empty_cache()
+    ref = cpu_step.covar_cost_grad_es(vec, ls, R.astype(np.float64), imgs, ctf, 5.0, width=6, reg_scale=0.01,
+                                      fourier_reg=fr)
+    assert rel(val, ref[0]) < TOL_COST
+    assert rel(gv, ref[1]) < TOL_GRAD
+    assert rel(gl, ref[2]) < TOL_GRAD
+
+
+def test_fused_gradient_matches_fp64_finite_differences(pkg, dev):
+    """The hand-written adjoint against float64 central differences of the oracle's cost on
+    the L = 32, r = 5, N = 512 instance: <grad, d> for three random directions d of the
+    parameters (vectors and log-scales)."""
+    from oracle import cpu_step
+
+    L, r, B = 32, 5, 512
+    vec, ls, R, imgs, ctf, fr = _es_case(L, r, B, 3205)
+    step = pkg.FusedCovarStep(L, r, "nufft", 2, width=6, device=dev)
+    step.set_rotations(torch.tensor(R, device=dev))
+    _, gv, gl = step(torch.tensor(vec, device=dev), torch.tensor(ls, device=dev),
+                     torch.tensor(imgs, device=dev).reshape(B, -1), torch.tensor(ctf, device=dev).reshape(B, -1),
+                     5.0, reg_scale=0.01, fourier_reg=torch.tensor(fr, device=dev), sync_cost=True)
+    gv, gl = gv.cpu().numpy().astype(np.float64), gl.cpu().numpy().astype(np.float64)
+    rng = np.random.default_rng(11)
+    R64, v64, l64 = R.astype(np.float64), vec.astype(np.float64), ls.astype(np.float64)
+
+    def f(v, l):
+        return cpu_step.covar_cost_grad_es(v, l, R64, imgs, ctf, 5.0, width=6, reg_scale=0.01, fourier_reg=fr,
+                                           cost_only=True)
+
+    for _ in range(3):
+        dv = rng.standard_normal(v64.shape)
+        dv /= np.linalg.norm(dv)
+        dl = rng.standard_normal(r) * 0.1
+        h = 1e-4
+        fd = (f(v64 + h * dv, l64 + h * dl) - f(v64 - h * dv, l64 - h * dl)) / (2 * h)
+        an = float(np.sum(gv * dv) + np.sum(gl * dl))
+        assert abs(an - fd) / abs(fd) < TOL_GRAD, (an, fd)
+
+
+@pytest.mark.parametrize("objective", ["ml", "ls"])
+@pytest.mark.parametrize("with_reg", [False, True])
+def test_spatial_costs_match_reference(pkg, dev, objective, with_reg):
+    """cost / cost_maximum_liklihood (spatial eigenvolumes through the exact NufftPlan, spatial
+    images) against the reference run in float64 on the exact NUDFT (fixture)."""
+    c = load_golden("spatial_cost_L10_r3.npz")
+    L, r = int(c["L"]), int(c["r"])
+    covar = pkg.Covar(L, r, vectors=torch.tensor(c["vectors"])).to(dev)
+    plan = pkg.NufftPlan((L,) * 3, batch_size=r, device=dev, width=8)
+    plan.setpts(torch.tensor(c["pts"], dtype=torch.float32, device=dev))
+    fn = pkg.cost_maximum_liklihood if objective == "ml" else pkg.cost
+    kw = dict(reg_scale=float(c["reg_scale"]), fourier_reg=torch.tensor(c["fourier_reg"], device=dev)) if with_reg else {}
+    ims = torch.tensor(c["images"], device=dev)
+    filt = torch.tensor(c["filters"], device=dev)
+    val = fn(covar.get_vectors_spatial_domain(), ims, plan, filt, float(c["noise_var"]), **kw)
+    val.backward()
+    tag = objective + ("_reg" if with_reg else "")
+    assert rel(val, c[tag + "_cost"]) < TOL_COST
+    assert rel(covar.vectors.grad, c[tag + "_grad_vectors"]) < TOL_GRAD
+    assert rel(covar.log_sqrt_eigenvals.grad, c[tag + "_grad_logsqrt"]) < TOL_GRAD
+    per = fn(covar.get_vectors_spatial_domain(), ims, plan, filt, float(c["noise_var"]), mean_aggregate=False, **kw)
+    assert rel(per, c[tag + "_per_image"]) < TOL_COST

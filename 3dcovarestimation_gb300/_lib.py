@@ -38,7 +38,7 @@ class CostArgs(ctypes.Structure):
     _fields_ = [("objective", c_int), ("rank", c_int), ("d_vectors", c_void_p), ("d_log_sqrt", c_void_p),
                 ("d_images", c_void_p), ("d_ctf", c_void_p), ("noise_var", c_double), ("reg_scale", c_double),
                 ("d_fourier_reg", c_void_p), ("use_grid_correction", c_int), ("d_cost", c_void_p),
-                ("gram_bf16", c_int)]
+                ("gram_bf16", c_int), ("fourier_reg_per_channel", c_int)]
 
 
 _SIGNATURES = {

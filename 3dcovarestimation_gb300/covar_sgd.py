@@ -208,12 +208,23 @@ class FusedCovarStep:
         imgs = images.detach().to(torch.complex64).contiguous()
         ctf_t = None if ctf is None else ctf.detach().to(torch.float32).contiguous()
         fr = None if fourier_reg is None or reg_scale == 0 else fourier_reg.to(torch.float32).contiguous()
+        n3 = (self.L * self.plan.n // self.L) ** 3
+        per_channel = 0
+        if fr is not None:
+            # one regulariser for every eigenvolume (n^3), or one each (r, n^3) as
+            # CovarTrainer.compute_fourier_reg_term builds it (covar_sgd.py:420-430)
+            if fr.numel() == r * n3 and r > 1:
+                per_channel = 1
+            elif fr.numel() != n3:
+                raise ValueError(f"fourier_reg must hold n^3 or rank * n^3 values (n = {self.plan.n}); "
+                                 f"got shape {tuple(fr.shape)}")
         args = _lib.CostArgs(objective=objective, rank=r, d_vectors=vectors.data_ptr(), d_log_sqrt=log_sqrt.data_ptr(),
                              d_images=imgs.data_ptr(), d_ctf=ctf_t.data_ptr() if ctf_t is not None else None,
                              noise_var=float(noise_var), reg_scale=float(reg_scale),
                              d_fourier_reg=fr.data_ptr() if fr is not None else None,
                              use_grid_correction=0 if self.nufft_disc == "nufft_nogc" else 1,
-                             d_cost=self.d_cost.data_ptr(), gram_bf16=1 if self.gram_bf16 else 0)
+                             d_cost=self.d_cost.data_ptr(), gram_bf16=1 if self.gram_bf16 else 0,
+                             fourier_reg_per_channel=per_channel)
         host_cost = _lib.c_double() if sync_cost else None
         with torch.cuda.device(self.device):
             _lib.call("cov3d_covar_cost_grad", self.plan.bind(), _lib.ctypes.byref(args),

@@ -175,7 +175,7 @@ int launch_axis0_diag(cov3d_plan *p, float2 *g, const float *diag, int L, int n,
 int cg_operator_lines(cov3d_plan *p, const float2 *in, float2 *fine, float2 *out, const float2 *dotp,
                       const float *diag, int divide, const int *stop, const int *stop_last, double *dot);
 int step_forward_lines(cov3d_plan *p, const float *vec, const float *logs, const float *gc, int r, float2 *stage,
-                       float2 *grid, const float *fr, double coef, double *cost);
+                       float2 *grid, const float *fr, int64_t fr_stride, double coef, double *cost);
 int step_inverse_lines(cov3d_plan *p, float2 *grad_grid, const float *vec, const float *logs, const float *gc, int r,
                        float *gvec, double *glog);
 inline bool prunable(const cov3d_plan *p) { return p->L % 2 == 0 && p->n >= p->L + 2; }
@@ -209,7 +209,7 @@ int launch_pack(cov3d_plan *p, const float *vol_real, const void *vol_cplx, cons
 int launch_unpack_complex(cov3d_plan *p, const void *fine, int nchan, int use_gc, void *out);
 int launch_unpack_grad(cov3d_plan *p, const void *fine, const float *vectors, const float *log_scale, int use_gc,
                        int nchan, float *grad_vec, double *grad_log_acc);
-int launch_ml_reg(cov3d_plan *p, const void *grid, void *ggrid, const float *fr, int nchan, double coef,
+int launch_ml_reg(cov3d_plan *p, const void *grid, void *ggrid, const float *fr, int64_t fr_stride, int nchan, double coef,
                   double *cost_acc, int init);
 int launch_gc_volume(const cov3d_plan *p, float *out);
 int launch_zero(cov3d_plan *p, void *ptr, int64_t bytes);

@@ -670,6 +670,7 @@ int covar_cost_grad(cov3d_plan *p, const cov3d_cost_args *a, double *h_cost, dou
   const bool lines_inv = pruned && line_transforms_apply(p);
   const bool lines_fwd = lines_inv && p->n <= 256;
   const bool with_reg = a->d_fourier_reg && a->reg_scale != 0.0;
+  const int64_t fr_stride = a->fourier_reg_per_channel ? n3 : 0;
   const float *gcp = a->use_grid_correction ? p->gc1d.as<float>() : nullptr;
   cufftHandle fft = 0, fplanes = 0, faxis0 = 0;
   if (pruned) {
@@ -685,7 +686,8 @@ int covar_cost_grad(cov3d_plan *p, const cov3d_cost_args *a, double *h_cost, dou
   if (lines_fwd) {
     PhaseScope ps(p, kPhaseFftFwd);
     COV3D_TRY(step_forward_lines(p, a->d_vectors, a->d_log_sqrt, gcp, r, p->fine2.as<float2>(), p->fine.as<float2>(),
-                                 with_reg ? a->d_fourier_reg : nullptr, a->reg_scale / (2.0 * a->noise_var), acc + 1));
+                                 with_reg ? a->d_fourier_reg : nullptr, fr_stride, a->reg_scale / (2.0 * a->noise_var),
+                                 acc + 1));
   } else {
     PhaseScope ps(p, kPhasePack);
     COV3D_TRY(launch_pack(p, a->d_vectors, nullptr, a->d_log_sqrt, a->use_grid_correction, r,
@@ -739,8 +741,8 @@ int covar_cost_grad(cov3d_plan *p, const cov3d_cost_args *a, double *h_cost, dou
   // spread adds onto it and no zeroing pass is needed; without one, the grid is zeroed
   if (with_reg && !lines_fwd) {
     PhaseScope ps(p, kPhaseReg);
-    COV3D_TRY(launch_ml_reg(p, p->fine.ptr, p->fine2.ptr, a->d_fourier_reg, r, a->reg_scale / (2.0 * a->noise_var),
-                            acc + 1, 1));
+    COV3D_TRY(launch_ml_reg(p, p->fine.ptr, p->fine2.ptr, a->d_fourier_reg, fr_stride, r,
+                            a->reg_scale / (2.0 * a->noise_var), acc + 1, 1));
   }
   {
     PhaseScope ps(p, kPhaseSpread);

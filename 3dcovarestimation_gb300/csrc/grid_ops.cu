@@ -108,14 +108,16 @@ __global__ void unpack_grad_kernel(const float2 *__restrict__ fine, const float 
 // conjugate-Wirtinger derivative coef * fr * G to the fine-grid gradient (or, with `init`,
 // writes it there, so the grid needs no zeroing before the spread), accumulates its value.
 __global__ void ml_reg_kernel(const float2 *__restrict__ grid, float2 *__restrict__ gg, const float *__restrict__ fr,
-                              int nchan, int n, double coef, double *__restrict__ cost, int init) {
+                              int64_t frs, int nchan, int n, double coef, double *__restrict__ cost, int init) {
   // capped grid walking whole rows (no per-element division); the channel sum of one cell is
   // FP32, the running sum over cells FP64, one FP64 atomic per block
   const int64_t n3 = (int64_t)n * n * n;
   const int half = n / 2;
   const float cfs = (float)coef;
   // 16-byte accesses need an even row length and 16-byte aligned grids
-  const bool vec = (n & 1) == 0 && ((reinterpret_cast<uintptr_t>(grid) | reinterpret_cast<uintptr_t>(gg)) & 15) == 0;
+  // (with one regulariser per channel, frs != 0, the scalar path below reads each channel's)
+  const bool vec = frs == 0 && (n & 1) == 0 &&
+                   ((reinterpret_cast<uintptr_t>(grid) | reinterpret_cast<uintptr_t>(gg)) & 15) == 0;
   double part = 0.0;
   for (int64_t row = blockIdx.x; row < (int64_t)n * n; row += gridDim.x) {
     int s0 = (int)(row / n), s1 = (int)(row - (int64_t)s0 * n);
@@ -161,19 +163,19 @@ __global__ void ml_reg_kernel(const float2 *__restrict__ grid, float2 *__restric
     }
     for (int s2 = threadIdx.x; s2 < n; s2 += blockDim.x) {
       const int c2 = s2 + half >= n ? s2 + half - n : s2 + half;
-      const float w = __ldg(frow + c2);
-      const float cf = cfs * w;
       const int64_t cell = row * n + s2;
       float p32 = 0.0f;
       for (int c = 0; c < nchan; ++c) {
+        const float w = __ldg(frow + c * frs + c2);
+        const float cf = cfs * w;
         const float2 x = grid[c * n3 + cell];
         float2 y = init ? make_float2(0.f, 0.f) : gg[c * n3 + cell];
         y.x = fmaf(cf, x.x, y.x);
         y.y = fmaf(cf, x.y, y.y);
         gg[c * n3 + cell] = y;
-        p32 = fmaf(x.x, x.x, fmaf(x.y, x.y, p32));
+        p32 = fmaf(w, fmaf(x.x, x.x, x.y * x.y), p32);
       }
-      part += (double)(w * p32);
+      part += (double)p32;
     }
   }
 #pragma unroll
@@ -229,14 +231,14 @@ int launch_unpack_grad(cov3d_plan *p, const void *fine, const float *vectors, co
   return launched("unpack_grad_kernel");
 }
 
-int launch_ml_reg(cov3d_plan *p, const void *grid, void *ggrid, const float *fr, int nchan, double coef,
-                  double *cost_acc, int init) {
+int launch_ml_reg(cov3d_plan *p, const void *grid, void *ggrid, const float *fr, int64_t fr_stride, int nchan,
+                  double coef, double *cost_acc, int init) {
   const int64_t n3 = (int64_t)p->n * p->n * p->n;
   const int64_t rows = (int64_t)p->n * p->n;
   const unsigned blocks = (unsigned)(rows < 2432 ? rows : 2432);  // 16 blocks of 4 warps per SM
   (void)n3;
   ml_reg_kernel<<<blocks, 128, 0, p->stream>>>(static_cast<const float2 *>(grid), static_cast<float2 *>(ggrid), fr,
-                                               nchan, p->n, coef, cost_acc, init);
+                                               fr_stride, nchan, p->n, coef, cost_acc, init);
   return launched("ml_reg_kernel");
 }
 

@@ -251,6 +251,7 @@ struct LineArgs {
   double *glog;       // kUnpackRows: (r) d cost / d log_sqrt accumulators
   float2 *gout;       // kAxisFwd: transformed grid (channel stride cs)
   const float *fr;    // kAxisFwd: regulariser weights (n^3, centred) or null
+  int64_t frs;        // kAxisFwd: element stride between channels' weights (0: shared)
   double coef;        // kAxisFwd: regulariser coefficient
   double *cost;       // kAxisFwd: regulariser value accumulator
 };
@@ -358,7 +359,8 @@ __global__ void __launch_bounds__(256) line_kernel(const LineArgs a) {
     if (KIND == kAxisFwd) {
       const int s1 = (int)(line / n), s2 = (int)(line - (int64_t)(line / n) * n);
       float2 *gx = a.gout + c * a.cs + line;
-      const float *frl = a.fr ? a.fr + (int64_t)native_to_centered(s1, n) * n + native_to_centered(s2, n) : nullptr;
+      const float *frl =
+          a.fr ? a.fr + c * a.frs + (int64_t)native_to_centered(s1, n) * n + native_to_centered(s2, n) : nullptr;
       float part = 0.0f;  // this thread's N1 terms in FP32, then one FP64 block sum (FP64 is slow)
       line_dft<N1, N2, false>(
           ex, s_tw, role, [&](int i) { return in_support(i, L, n) ? ax[(int64_t)i * nn] : zero; },
@@ -496,7 +498,7 @@ int cg_operator_lines(cov3d_plan *p, const float2 *in, float2 *fine, float2 *out
 }
 
 int step_forward_lines(cov3d_plan *p, const float *vec, const float *logs, const float *gc, int r, float2 *stage,
-                       float2 *grid, const float *fr, double coef, double *cost) {
+                       float2 *grid, const float *fr, int64_t fr_stride, double coef, double *cost) {
   LineArgs a;
   COV3D_TRY(line_args(p, a));
   const int64_t n3 = (int64_t)p->n * p->n * p->n;
@@ -507,6 +509,7 @@ int step_forward_lines(cov3d_plan *p, const float *vec, const float *logs, const
   a.gc = gc;
   a.gout = grid;
   a.fr = fr;
+  a.frs = fr_stride;
   a.coef = coef;
   a.cost = cost;
   switch (p->n) {

@@ -167,11 +167,15 @@ typedef struct {
   const float *d_ctf;       /* (B, L^2) float32 or NULL */
   double noise_var;         /* Fourier-domain noise variance (dataset noise_var * L^2) */
   double reg_scale;         /* reg / N (covar_sgd.py:357) */
-  const float *d_fourier_reg; /* (n^3) float32 centered, or NULL (ML regulariser :1373-1376) */
+  const float *d_fourier_reg; /* (n^3) float32 centered, or NULL (ML regulariser :1373-1376); one array
+                                 per eigenvolume, (r, n^3), with fourier_reg_per_channel */
   int use_grid_correction;  /* divide by the kernel's deapodisation factors (init_grid_correction) */
   double *d_cost;           /* optional device scalar receiving the cost (no host sync needed) */
   int gram_bf16;            /* 1: per-image Gram contractions in BF16 on the tensor cores (FP32
                                accumulation, cov3d_gram_bf16); 0: FP32 on the CUDA cores */
+  int fourier_reg_per_channel; /* 0: d_fourier_reg is one (n^3) array for every eigenvolume; 1: it is
+                               (r, n^3), one per eigenvolume, as CovarTrainer.compute_fourier_reg_term
+                               builds it (covar_sgd.py:420-430) */
 } cov3d_cost_args;
 
 /* Outputs: d_grad_vectors (r, L^3) float32, d_grad_log_sqrt (r) float32, optional

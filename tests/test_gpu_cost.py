@@ -222,3 +222,23 @@ def test_spatial_costs_match_reference(pkg, dev, objective, with_reg):
     assert rel(covar.log_sqrt_eigenvals.grad, c[tag + "_grad_logsqrt"]) < TOL_GRAD
     per = fn(covar.get_vectors_spatial_domain(), ims, plan, filt, float(c["noise_var"]), mean_aggregate=False, **kw)
     assert rel(per, c[tag + "_per_image"]) < TOL_COST
+
+
+@pytest.mark.parametrize("L", [16, 64])
+def test_fused_step_per_channel_regulariser(pkg, dev, L):
+    """One Fourier regulariser per eigenvolume, (r, n^3), as CovarTrainer.compute_fourier_reg_term
+    builds it: the fallback regulariser kernel (L = 16) and the one fused in the line transform
+    (L = 64), against the float64 oracle."""
+    r, B = 3, 6
+    vec, ls, R, imgs, ctf, _ = _es_case(L, r, B, 99 + L)
+    fr = np.random.default_rng(L).uniform(0.5, 2.0, (r,) + (2 * L,) * 3).astype(np.float32)
+    step = pkg.FusedCovarStep(L, r, "nufft", 2, width=6, device=dev)
+    step.set_rotations(torch.tensor(R, device=dev))
+    val, gv, gl = step(torch.tensor(vec, device=dev), torch.tensor(ls, device=dev),
+                       torch.tensor(imgs, device=dev).reshape(B, -1), torch.tensor(ctf, device=dev).reshape(B, -1),
+                       5.0, reg_scale=0.05, fourier_reg=torch.tensor(fr, device=dev), sync_cost=True)
+    ref = O.covar_cost_grad(vec, ls, imgs, O.rotated_points(R.astype(np.float64), L), ctf, 5.0, kind="es", width=6,
+                            reg_scale=0.05, fourier_reg=fr)
+    assert rel(val, ref[0]) < TOL_COST
+    assert rel(gv, ref[1]) < TOL_GRAD
+    assert rel(gl, ref[2]) < TOL_GRAD

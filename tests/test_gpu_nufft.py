@@ -114,11 +114,10 @@ def test_batched_equals_looped(pkg, dev):
     base = rng.standard_normal((3, L, L, L)).astype(np.float32)
     v1 = T(base, dev).requires_grad_(True)
     plans = [pkg.NufftPlan((L,) * 3, 3, device=dev) for _ in range(B)]
-    fw = []
+    fw = torch.zeros((B, 3, L, L), device=dev)
     for i in range(B):
         plans[i].setpts(pts[i:i + 1])
-        fw.append(pkg.vol_forward(v1, plans[i]))
-    fw = torch.stack(fw)
+        fw[i] = pkg.vol_forward(v1, plans[i])  # (1, 3, L, L): one image, three volumes, as the reference
     torch.norm(fw).backward()
     v2 = T(base, dev).requires_grad_(True)
     bp = pkg.NufftPlan((L,) * 3, 3, device=dev)

@@ -20,7 +20,10 @@ KERNEL_ES, KERNEL_LINEAR, KERNEL_NEAREST = 0, 1, 2
 # grid orders
 GRID_CENTERED, GRID_FFT_NATIVE = 0, 1
 # epilogue flags
-APPLY_NYQUIST, APPLY_CTF = 1, 2
+APPLY_NYQUIST, APPLY_CTF, APPLY_CTF_PARAMS = 1, 2, 4
+# CTF parameters per image (pixel size, defocus u, v, astigmatism angle, kV, Cs, amplitude contrast,
+# phase shift)
+CTF_NPARAMS = 8
 
 c_int, c_int64, c_double, c_float, c_void_p = ctypes.c_int, ctypes.c_int64, ctypes.c_double, ctypes.c_float, ctypes.c_void_p
 
@@ -38,7 +41,7 @@ class CostArgs(ctypes.Structure):
     _fields_ = [("objective", c_int), ("rank", c_int), ("d_vectors", c_void_p), ("d_log_sqrt", c_void_p),
                 ("d_images", c_void_p), ("d_ctf", c_void_p), ("noise_var", c_double), ("reg_scale", c_double),
                 ("d_fourier_reg", c_void_p), ("use_grid_correction", c_int), ("d_cost", c_void_p),
-                ("gram_bf16", c_int), ("fourier_reg_per_channel", c_int)]
+                ("gram_bf16", c_int), ("ctf_params", c_int), ("fourier_reg_per_channel", c_int)]
 
 
 _SIGNATURES = {
@@ -59,6 +62,7 @@ _SIGNATURES = {
     "cov3d_execute_type2": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
     "cov3d_execute_type1": (c_int, [c_void_p, c_void_p, c_int, c_void_p]),
     "cov3d_grid_correction": (c_int, [c_void_p, c_void_p]),
+    "cov3d_ctf_images": (c_int, [c_void_p, c_void_p, c_int64, c_int, c_void_p]),
     "cov3d_covar_cost_grad": (c_int, [c_void_p, ctypes.POINTER(CostArgs), ctypes.POINTER(c_double), c_void_p,
                                       c_void_p, c_void_p]),
     "cov3d_launch_count": (ctypes.c_longlong, []),

@@ -193,8 +193,10 @@ class FusedCovarStep:
         self.plan.setpts(pts, wrap=self.nufft_disc == "nufft")
 
     def __call__(self, vectors, log_sqrt, images, ctf, noise_var, reg_scale=0.0, fourier_reg=None, objective=0,
-                 grad_vectors=None, grad_log_sqrt=None, per_image=None, sync_cost=False):
-        """Cost (device scalar, float64) and gradients w.r.t. (vectors, log_sqrt)."""
+                 grad_vectors=None, grad_log_sqrt=None, per_image=None, sync_cost=False, ctf_params=None):
+        """Cost (device scalar, float64) and gradients w.r.t. (vectors, log_sqrt).  ``ctf`` is the
+        (B, L^2) CTF array, or None with ``ctf_params`` (B, 8): the CTF is then computed in the
+        kernels from each image's parameters (see ``synthetic.ctf_params``)."""
         r = self.rank
         vectors = vectors.detach().to(torch.float32).contiguous()
         log_sqrt = log_sqrt.detach().to(torch.float32).contiguous()
@@ -207,6 +209,12 @@ class FusedCovarStep:
             raise ValueError("per_image must be a contiguous float64 tensor")
         imgs = images.detach().to(torch.complex64).contiguous()
         ctf_t = None if ctf is None else ctf.detach().to(torch.float32).contiguous()
+        if ctf_params is not None:
+            if ctf_t is not None:
+                raise ValueError("give ctf or ctf_params, not both")
+            ctf_t = ctf_params.detach().to(torch.float32).contiguous()
+            if ctf_t.shape != (self.plan.n_images, _lib.CTF_NPARAMS):
+                raise ValueError(f"ctf_params must be ({self.plan.n_images}, {_lib.CTF_NPARAMS})")
         fr = None if fourier_reg is None or reg_scale == 0 else fourier_reg.to(torch.float32).contiguous()
         n3 = (self.L * self.plan.n // self.L) ** 3
         per_channel = 0
@@ -224,7 +232,7 @@ class FusedCovarStep:
                              d_fourier_reg=fr.data_ptr() if fr is not None else None,
                              use_grid_correction=0 if self.nufft_disc == "nufft_nogc" else 1,
                              d_cost=self.d_cost.data_ptr(), gram_bf16=1 if self.gram_bf16 else 0,
-                             fourier_reg_per_channel=per_channel)
+                             ctf_params=1 if ctf_params is not None else 0, fourier_reg_per_channel=per_channel)
         host_cost = _lib.c_double() if sync_cost else None
         with torch.cuda.device(self.device):
             _lib.call("cov3d_covar_cost_grad", self.plan.bind(), _lib.ctypes.byref(args),

@@ -141,6 +141,45 @@ __device__ __forceinline__ float tap_weight(float t, int q, float beta) {
   return es_weight<W>(t - (float)(c0 + q), beta);
 }
 
+// CTF at pixel offsets (ka, kb) (row, column) from the image centre: sqrt(1 - w^2) sin(gamma) -
+// w cos(gamma) with gamma = c0 K + c1 D + c2 X + d K^2 - ps (see CtfCoef).  gamma reaches a few
+// hundred radians at high frequency, so its large terms are formed in double-float arithmetic
+// (exact products by fmaf, TwoSum), reduced modulo 2 pi by Cody-Waite with a 2 pi split into a
+// 12-bit head (n * head exact for |n| < 2^12) and a float tail, and only the reduced angle goes
+// to sincosf: the absolute phase error stays near float rounding of the reduced angle.
+__device__ __forceinline__ float ctf_eval(const CtfCoef &c, int ka, int kb) {
+  const float K = (float)(ka * ka + kb * kb), D = (float)(ka * ka - kb * kb), X = (float)(2 * ka * kb);
+  const float p0 = c.c0h * K, e0 = fmaf(c.c0h, K, -p0);
+  const float p1 = c.c1h * D, e1 = fmaf(c.c1h, D, -p1);
+  const float p2 = c.c2h * X, e2 = fmaf(c.c2h, X, -p2);
+  float s = p0 + p1;
+  float bb = s - p0;
+  float err = (p0 - (s - bb)) + (p1 - bb);
+  const float t = s + p2;
+  bb = t - s;
+  err += (s - (t - bb)) + (p2 - bb);
+  const float lo = err + e0 + e1 + e2 + fmaf(c.c0l, K, fmaf(c.c1l, D, c.c2l * X)) + c.d * K * K - c.ps;
+  constexpr float kTwoPiHead = 6.283203125f;          // 3217 / 512
+  constexpr float kTwoPiTail = -1.7817820413e-05f;    // 2 pi - head
+  constexpr float kInvTwoPi = 0.15915494309189535f;
+  const float nq = rintf((t + lo) * kInvTwoPi);
+  float r = fmaf(-nq, kTwoPiHead, t);
+  r = fmaf(-nq, kTwoPiTail, r) + lo;
+  float sn, cs;
+  sincosf(r, &sn, &cs);
+  return c.sw * sn - c.w * cs;
+}
+
+// The CTF factor of point id: the per-pixel array, or the per-image coefficients, or 1.
+__device__ __forceinline__ float ctf_factor(const float *ctf, const CtfCoef *ctfc, const PointGeom &g, int64_t id) {
+  if (ctf) return __ldg(ctf + id);
+  if (!ctfc) return 1.0f;
+  const int64_t b = id / g.P;
+  const int p = (int)(id - b * g.P);
+  const int row = p / g.Lp, col = p - (p / g.Lp) * g.Lp;
+  return ctf_eval(ctfc[b], row - g.Lp / 2, col - g.Lp / 2);
+}
+
 // Index maps of the fine grid (FFT-native storage: frequency / voxel offset k at k mod n).
 // centered index of storage index s on a grid of size m (fftshift)
 __device__ __forceinline__ int native_to_centered(int s, int m) {

@@ -112,6 +112,7 @@ struct cov3d_plan {
   cov3d::Bins bins{};
   int max_sub = 288;
   cov3d::DevBuf bin_count;     // int (nbins + 1), last = dead points
+  cov3d::DevBuf fine_count, fine_off;  // int (nbins * 64 + 1): points and offsets per corner block of a bin
   cov3d::DevBuf bin_off;       // int (nbins + 2)
   cov3d::DevBuf sub_off;       // int (nbins + 1)
   cov3d::DevBuf pt_bin, pt_rank;              // int (M)
@@ -126,6 +127,7 @@ struct cov3d_plan {
   cov3d::DevBuf acc;           // double accumulators
   cov3d::DevBuf cgw;           // mean / CG workspace (state, vectors, shell sums)
   cov3d::DevBuf xbf, gsum;     // BF16 Gram operands and real Gram sums
+  cov3d::DevBuf ctfc;          // per-image CTF coefficients (CtfCoef) from CTF parameters
   cov3d::DevBuf fftw;          // twiddles exp(-2 pi i j / fftw_n) of the fused axis-0 CG transform
   int fftw_n = 0;
   double *h_acc = nullptr;     // pinned host mirror of acc (64 doubles)
@@ -189,11 +191,26 @@ struct GridArgs {
   int64_t cell_stride, chan_stride;
   int shift;  // storage = (centered + shift) mod n
 };
+// Per-image coefficients of the CTF phase, prepared from the CTF parameters by
+// prepare_ctf_coef (grid_ops.cu) and evaluated per pixel by ctf_eval (cov3d_device.cuh):
+// gamma(ka, kb) = c0 K + c1 D + c2 X + d K^2 - ps at the pixel offsets (ka, kb) from the image
+// centre (row, column), K = ka^2 + kb^2, D = ka^2 - kb^2, X = 2 ka kb; c0..c2 as float pairs
+// (hi + lo) whose sum carries the double-precision coefficient.
+struct CtfCoef {
+  float c0h, c0l, c1h, c1l, c2h, c2l;
+  float d, ps, sw, w;  // K^2 coefficient, phase shift (rad), sqrt(1 - w^2), amplitude contrast
+  float pad0, pad1;
+};
+
 struct EpilogueArgs {
   const float *ctf;  // (n_images, P) or null
   int nyquist;       // zero row/col 0 when Lp even
   float scale;
+  const CtfCoef *ctfc = nullptr;  // per-image CTF coefficients (used when ctf is null), or null
 };
+// Coefficients of n_images CTFs from their parameters (n_images, COV3D_CTF_NPARAMS) into the
+// plan's workspace; *out receives the device pointer.
+int prepare_ctf_coef(cov3d_plan *p, const float *params, int64_t n_images, int L, const CtfCoef **out);
 int launch_interp(cov3d_plan *p, const GridArgs &g, int nchan, void *out, int64_t out_ps, int64_t out_cs,
                   const EpilogueArgs &e);
 

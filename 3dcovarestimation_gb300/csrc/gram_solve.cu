@@ -710,7 +710,8 @@ int covar_cost_grad(cov3d_plan *p, const cov3d_cost_args *a, double *h_cost, dou
   // 3. interpolate at the central slices with the fused projection epilogue -> Q (B*P, r)
   const int shift = p->n - p->n / 2;
   GridArgs ga{p->fine.ptr, 1, n3, shift};
-  EpilogueArgs ep{a->d_ctf, 1, 1.0f / (float)L};
+  EpilogueArgs ep{a->ctf_params ? nullptr : a->d_ctf, 1, 1.0f / (float)L};
+  if (a->ctf_params && a->d_ctf) COV3D_TRY(prepare_ctf_coef(p, a->d_ctf, B, L, &ep.ctfc));
   {
     PhaseScope ps(p, kPhaseInterp);
     COV3D_TRY(launch_interp(p, ga, r, p->q.ptr, r, 1, ep));

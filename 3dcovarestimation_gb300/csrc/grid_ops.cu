@@ -306,3 +306,85 @@ int get_fft(cov3d_plan *p, int nchan, cufftHandle *out) {
 }
 
 }  // namespace cov3d
+
+// ----------------------------------------------------------------------------- CTF from parameters
+namespace cov3d {
+namespace {
+
+// CtfCoef of one image from its parameters q[0..7] = pixel size (A), defocus u and v (A),
+// astigmatism angle (degrees), voltage (kV), spherical aberration (mm), amplitude contrast,
+// phase shift (degrees): the CTF sqrt(1 - w^2) sin(gamma) - w cos(gamma) with
+// gamma = 2 pi (-df lambda s^2 / 2 + Cs lambda^3 s^4 / 4) - phase shift, the defocus along the
+// frequency's direction df = (dfu + dfv + (dfu - dfv) cos(2 (angle - astigmatism angle))) / 2 and
+// the relativistic electron wavelength lambda = 12.2639 / sqrt(V + 0.97845e-6 V^2) (V in volts):
+// the standard weak-phase CTF in the form cryoDRGN's compute_ctf evaluates for the reference
+// (source.py:157-172), frequency s at pixel (row a, column b) = (a - L/2, b - L/2) / (L * pixel).
+// In double precision; the angle-dependent defocus is expanded with cos 2(t - d) = cos 2t cos 2d +
+// sin 2t sin 2d, cos 2t = (x^2 - y^2) / K, sin 2t = 2 x y / K, so no per-pixel angle is needed.
+__device__ CtfCoef make_ctf_coef(const float *q, int L) {
+  const double pi = 3.14159265358979323846;
+  const double apix = q[0], dfu = q[1], dfv = q[2], ang = (double)q[3] * pi / 180.0;
+  const double volt = (double)q[4] * 1e3, cs = (double)q[5] * 1e7, w = q[6], ps = (double)q[7] * pi / 180.0;
+  const double lam = 12.2639 / sqrt(volt + 0.97845e-6 * volt * volt);
+  const double u2 = 1.0 / (((double)L * apix) * ((double)L * apix));
+  const double a = -pi * lam * u2;
+  const double c0 = a * 0.5 * (dfu + dfv);
+  const double c1 = a * 0.5 * (dfu - dfv) * cos(2.0 * ang);
+  const double c2 = a * 0.5 * (dfu - dfv) * sin(2.0 * ang);
+  CtfCoef c;
+  c.c0h = (float)c0;
+  c.c0l = (float)(c0 - (double)c.c0h);
+  c.c1h = (float)c1;
+  c.c1l = (float)(c1 - (double)c.c1h);
+  c.c2h = (float)c2;
+  c.c2l = (float)(c2 - (double)c.c2h);
+  c.d = (float)(0.5 * pi * cs * lam * lam * lam * u2 * u2);
+  c.ps = (float)ps;
+  c.sw = (float)sqrt(1.0 - w * w);
+  c.w = (float)w;
+  c.pad0 = c.pad1 = 0.0f;
+  return c;
+}
+
+__global__ void ctf_coef_kernel(const float *__restrict__ prm, int64_t n, int L, CtfCoef *__restrict__ out) {
+  const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b < n) out[b] = make_ctf_coef(prm + b * COV3D_CTF_NPARAMS, L);
+}
+
+// One block per image: its coefficients once, then every pixel.
+__global__ void ctf_images_kernel(const float *__restrict__ prm, int L, float *__restrict__ out) {
+  __shared__ CtfCoef c;
+  const int64_t b = blockIdx.x;
+  if (threadIdx.x == 0) c = make_ctf_coef(prm + b * COV3D_CTF_NPARAMS, L);
+  __syncthreads();
+  const int P = L * L;
+  for (int p = threadIdx.x; p < P; p += blockDim.x) {
+    const int row = p / L, col = p - (p / L) * L;
+    out[b * P + p] = ctf_eval(c, row - L / 2, col - L / 2);
+  }
+}
+
+}  // namespace
+
+int prepare_ctf_coef(cov3d_plan *p, const float *params, int64_t n_images, int L, const CtfCoef **out) {
+  COV3D_TRY(grow(p->ctfc, n_images * (int64_t)sizeof(CtfCoef)));
+  ctf_coef_kernel<<<(unsigned)((n_images + 127) / 128), 128, 0, p->stream>>>(params, n_images, L,
+                                                                           p->ctfc.as<CtfCoef>());
+  COV3D_LAUNCHED("ctf_coef_kernel");
+  *out = p->ctfc.as<CtfCoef>();
+  return COV3D_OK;
+}
+
+}  // namespace cov3d
+
+extern "C" int cov3d_ctf_images(void *stream, const float *d_params, int64_t n_images, int L, float *d_out) {
+  using namespace cov3d;
+  if (!d_params || !d_out || n_images < 0 || L < 1) {
+    set_error("invalid ctf_images arguments");
+    return COV3D_EINVAL;
+  }
+  if (n_images == 0) return COV3D_OK;
+  ctf_images_kernel<<<(unsigned)n_images, 256, 0, static_cast<cudaStream_t>(stream)>>>(d_params, L, d_out);
+  COV3D_LAUNCHED("ctf_images_kernel");
+  return COV3D_OK;
+}

@@ -28,6 +28,7 @@ struct InterpParams {
   float2 *out;
   int64_t ops, ocs;
   const float *ctf;
+  const CtfCoef *ctfc;
   int nyquist;
   float scale;
 };
@@ -108,7 +109,7 @@ __global__ void __launch_bounds__(kInterpWarps * 32) interp_kernel(const InterpP
     const SortedPoint sp = a.pts[first + k];
     s_sp[k] = sp;
     float sc = (a.nyquist && sp_nyquist(sp.idf)) ? 0.0f : a.scale;
-    if (a.ctf) sc *= __ldg(a.ctf + sp_id(sp.idf));
+    sc *= ctf_factor(a.ctf, a.ctfc, a.g, sp_id(sp.idf));
     s_sc[k] = sc;
   }
   const float2 *gbase = a.grid + (int64_t)a.ch0 * a.chs;
@@ -310,6 +311,7 @@ __global__ void __launch_bounds__(kGroupWarps * 32, 1) interp_group_kernel(const
   int *tcounter = ktoff + kGroupKeys + 1;
   __shared__ long long s_rowoff[T * T];
   __shared__ int s_coloff[T];
+  __shared__ int s_lo[3], s_hi[3];  // corner extents of the subproblem's points
   const int sub = blockIdx.x;
   if (sub >= *a.nsub) return;
   const int bin = a.sub_bin[sub];
@@ -340,30 +342,56 @@ __global__ void __launch_bounds__(kGroupWarps * 32, 1) interp_group_kernel(const
     s_coloff[e] = m2 >= n ? m2 - n : m2;
   }
   for (int e = tid; e < kGroupKeys; e += blockDim.x) kcnt[e] = 0;
+  if (tid < 3) {
+    s_lo[tid] = kBin;
+    s_hi[tid] = -1;
+  }
   if (tid == 0) *tcounter = 0;
   __syncthreads();
-  // the tile, asynchronously: in flight while the points are sorted
-  const float2 *gbase = a.grid + (int64_t)a.ch0 * a.chs;
-  for (int e = tid; e < CH * T * T * T; e += blockDim.x) {
-    const int c2 = e % T;
-    const int rowi = (e / T) % (T * T);
-    const int ch = e / (T * T * T);
-    const bool ok = ch < a.nch;
-    const float2 *src = ok ? gbase + s_rowoff[rowi] + (int64_t)s_coloff[c2] * a.cs + (int64_t)ch * a.chs : gbase;
-    const unsigned dst = (unsigned)__cvta_generic_to_shared(tile + (rowi * T + c2) * CH + ch);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(dst), "l"(src), "r"(ok ? 8 : 0) : "memory");
-  }
-  asm volatile("cp.async.commit_group;\n" ::: "memory");
-  // block keys of the window corners and ranks within a key
-  for (int k = tid; k < cnt; k += blockDim.x) {
-    const SortedPoint sp = a.pts[first + k];
-    const int l0 = wrap1(first_cell<COV3D_KERNEL_ES, W>(sp.t0), n) - ts0;
-    const int l1 = wrap1(first_cell<COV3D_KERNEL_ES, W>(sp.t1), n) - ts1;
-    const int l2 = wrap1(first_cell<COV3D_KERNEL_ES, W>(sp.t2), n) - ts2;
-    const int key = ((l0 >> 1) * 4 + (l1 >> 1)) * 4 + (l2 >> 1);
-    pkey[k] = key | (atomicAdd(kcnt + key, 1) << 8);
+  // block keys of the window corners, ranks within a key, and the corners' extents
+  {
+    int lo0 = kBin, lo1 = kBin, lo2 = kBin, hi0 = -1, hi1 = -1, hi2 = -1;
+    for (int k = tid; k < cnt; k += blockDim.x) {
+      const SortedPoint sp = a.pts[first + k];
+      const int l0 = wrap1(first_cell<COV3D_KERNEL_ES, W>(sp.t0), n) - ts0;
+      const int l1 = wrap1(first_cell<COV3D_KERNEL_ES, W>(sp.t1), n) - ts1;
+      const int l2 = wrap1(first_cell<COV3D_KERNEL_ES, W>(sp.t2), n) - ts2;
+      const int key = ((l0 >> 1) * 4 + (l1 >> 1)) * 4 + (l2 >> 1);
+      pkey[k] = key | (atomicAdd(kcnt + key, 1) << 8);
+      lo0 = min(lo0, l0), lo1 = min(lo1, l1), lo2 = min(lo2, l2);
+      hi0 = max(hi0, l0), hi1 = max(hi1, l1), hi2 = max(hi2, l2);
+    }
+    lo0 = __reduce_min_sync(0xffffffffu, lo0), lo1 = __reduce_min_sync(0xffffffffu, lo1);
+    lo2 = __reduce_min_sync(0xffffffffu, lo2);
+    hi0 = __reduce_max_sync(0xffffffffu, hi0), hi1 = __reduce_max_sync(0xffffffffu, hi1);
+    hi2 = __reduce_max_sync(0xffffffffu, hi2);
+    if ((tid & 31) == 0 && hi0 >= 0) {
+      atomicMin(s_lo + 0, lo0), atomicMin(s_lo + 1, lo1), atomicMin(s_lo + 2, lo2);
+      atomicMax(s_hi + 0, hi0), atomicMax(s_hi + 1, hi1), atomicMax(s_hi + 2, hi2);
+    }
   }
   __syncthreads();
+  // the tile cells the points' windows reach ([lo, hi + W) per axis), asynchronously: in flight
+  // while the points are sorted
+  const float2 *gbase = a.grid + (int64_t)a.ch0 * a.chs;
+  {
+    const int b0 = s_lo[0], b1 = s_lo[1], b2 = s_lo[2];
+    const int x0 = s_hi[0] - b0 + W, x1 = s_hi[1] - b1 + W, x2 = s_hi[2] - b2 + W;
+    const int box = x0 * x1 * x2;
+    for (int e = tid; e < CH * box; e += blockDim.x) {
+      const int ch = e / box;
+      const int rem = e - ch * box;
+      const int c2 = b2 + rem % x2;
+      const int r01 = rem / x2;
+      const int c1 = b1 + r01 % x1, c0 = b0 + r01 / x1;
+      const int rowi = c0 * T + c1;
+      const bool ok = ch < a.nch;
+      const float2 *src = ok ? gbase + s_rowoff[rowi] + (int64_t)s_coloff[c2] * a.cs + (int64_t)ch * a.chs : gbase;
+      const unsigned dst = (unsigned)__cvta_generic_to_shared(tile + (rowi * T + c2) * CH + ch);
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(dst), "l"(src), "r"(ok ? 8 : 0) : "memory");
+    }
+  }
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
   if (tid < 32) {  // point offsets and task offsets per key (two keys per lane), and the task list
     const int k0 = 2 * tid;
     const int c0 = kcnt[k0], c1 = kcnt[k0 + 1];
@@ -412,7 +440,7 @@ __global__ void __launch_bounds__(kGroupWarps * 32, 1) interp_group_kernel(const
       for (int j = 0; j < 8; ++j) ws[d * 8 + j] = j < W ? w[d][j] : 0.0f;
     pid[slot] = sp_id(sp.idf);
     float sc = (a.nyquist && sp_nyquist(sp.idf)) ? 0.0f : a.scale;
-    if (a.ctf) sc *= __ldg(a.ctf + sp_id(sp.idf));
+    sc *= ctf_factor(a.ctf, a.ctfc, a.g, sp_id(sp.idf));
     psc[slot] = sc;
     pcor[slot] = c0 | (c1 << 8) | (c2 << 16);
   }
@@ -585,6 +613,7 @@ int launch_interp(cov3d_plan *p, const GridArgs &ga, int nchan, void *out, int64
   a.ops = out_ps;
   a.ocs = out_cs;
   a.ctf = e.ctf;
+  a.ctfc = e.ctfc;
   a.nyquist = e.nyquist;
   a.scale = e.scale;
   const int64_t mb = p->bins.nbins + p->n_points / p->max_sub + 1;

@@ -324,7 +324,8 @@ int cov3d_plan_destroy(cov3d_plan *p) {
   }
   DevBuf *bufs[] = {&p->gc1d, &p->pts, &p->rot, &p->bin_count, &p->bin_off, &p->sub_off, &p->pt_bin, &p->pt_rank,
                     &p->sorted, &p->sub_bin, &p->sub_first, &p->sub_count, &p->nsub, &p->fine, &p->fine2, &p->q,
-                    &p->small, &p->acc, &p->cgw, &p->xbf, &p->gsum, &p->fftw};
+                    &p->small, &p->acc, &p->cgw, &p->xbf, &p->gsum, &p->fftw, &p->fine_count, &p->fine_off,
+                    &p->ctfc};
   for (DevBuf *b : bufs) release(*b);
   if (p->h_acc) cudaFreeHost(p->h_acc);
   if (p->ev_pool) {
@@ -392,6 +393,17 @@ int cov3d_setrot(cov3d_plan *p, const float *d_rot, int64_t n_images, int points
   return finish_points(p);
 }
 
+// The projection epilogue / prologue of a call: the per-pixel filter array, or the CTF computed
+// from per-image parameters (coefficients prepared once per call), Nyquist zeroing, scale.
+static int epilogue_args(cov3d_plan *p, const float *d_ctf, int flags, float scale, EpilogueArgs *e) {
+  e->ctf = (flags & COV3D_APPLY_CTF) && !(flags & COV3D_APPLY_CTF_PARAMS) ? d_ctf : nullptr;
+  e->nyquist = (flags & COV3D_APPLY_NYQUIST) ? 1 : 0;
+  e->scale = scale;
+  e->ctfc = nullptr;
+  if (flags & COV3D_APPLY_CTF_PARAMS) COV3D_TRY(prepare_ctf_coef(p, d_ctf, p->n_images, p->points_L, &e->ctfc));
+  return COV3D_OK;
+}
+
 static int layout_shift(const cov3d_plan *p, const cov3d_grid_layout *l) {
   return l->order == COV3D_GRID_CENTERED ? 0 : p->n - p->n / 2;
 }
@@ -402,12 +414,13 @@ int cov3d_interp(cov3d_plan *p, const void *d_grid, const cov3d_grid_layout *lay
     set_error("invalid interp arguments");
     return COV3D_EINVAL;
   }
-  if ((flags & COV3D_APPLY_CTF) && !d_ctf) {
-    set_error("COV3D_APPLY_CTF without a filter array");
+  if ((flags & (COV3D_APPLY_CTF | COV3D_APPLY_CTF_PARAMS)) && !d_ctf) {
+    set_error("COV3D_APPLY_CTF / COV3D_APPLY_CTF_PARAMS without a filter or parameter array");
     return COV3D_EINVAL;
   }
   GridArgs g{d_grid, layout->cell_stride, layout->chan_stride, layout_shift(p, layout)};
-  EpilogueArgs e{(flags & COV3D_APPLY_CTF) ? d_ctf : nullptr, (flags & COV3D_APPLY_NYQUIST) ? 1 : 0, scale};
+  EpilogueArgs e;
+  COV3D_TRY(epilogue_args(p, d_ctf, flags, scale, &e));
   return launch_interp(p, g, nchan, d_out, out_point_stride, out_chan_stride, e);
 }
 
@@ -418,8 +431,8 @@ int cov3d_spread(cov3d_plan *p, const void *d_values, int64_t in_point_stride, i
     set_error("invalid spread arguments");
     return COV3D_EINVAL;
   }
-  if ((flags & COV3D_APPLY_CTF) && !d_ctf) {
-    set_error("COV3D_APPLY_CTF without a filter array");
+  if ((flags & (COV3D_APPLY_CTF | COV3D_APPLY_CTF_PARAMS)) && !d_ctf) {
+    set_error("COV3D_APPLY_CTF / COV3D_APPLY_CTF_PARAMS without a filter or parameter array");
     return COV3D_EINVAL;
   }
   const int64_t n3 = (int64_t)p->n * p->n * p->n;
@@ -432,7 +445,8 @@ int cov3d_spread(cov3d_plan *p, const void *d_values, int64_t in_point_stride, i
     }
     COV3D_TRY(launch_zero(p, d_grid, n3 * nchan * 8));
   }
-  EpilogueArgs e{(flags & COV3D_APPLY_CTF) ? d_ctf : nullptr, (flags & COV3D_APPLY_NYQUIST) ? 1 : 0, scale};
+  EpilogueArgs e;
+  COV3D_TRY(epilogue_args(p, d_ctf, flags, scale, &e));
   return launch_spread(p, d_values, in_point_stride, in_chan_stride, nchan, e, d_grid, layout->cell_stride,
                        layout->chan_stride, layout_shift(p, layout));
 }
@@ -449,7 +463,8 @@ int cov3d_spread_unaggregated(cov3d_plan *p, const void *d_values, int64_t in_po
   }
   const int64_t n3 = (int64_t)p->n * p->n * p->n;
   COV3D_TRY(launch_zero(p, d_grids, p->n_images * n3 * 8));
-  EpilogueArgs e{(flags & COV3D_APPLY_CTF) ? d_ctf : nullptr, (flags & COV3D_APPLY_NYQUIST) ? 1 : 0, scale};
+  EpilogueArgs e;
+  COV3D_TRY(epilogue_args(p, d_ctf, flags, scale, &e));
   return launch_spread_unaggregated(p, d_values, in_point_stride, e, d_grids);
 }
 

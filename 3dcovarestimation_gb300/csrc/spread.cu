@@ -25,6 +25,7 @@ struct SpreadParams {
   int ch0;
   int nch;  // channels of this launch
   const float *ctf;
+  const CtfCoef *ctfc;
   int nyquist;
   float scale;
   float2 *grid;
@@ -34,11 +35,11 @@ struct SpreadParams {
 };
 
 // Prologue factor of im_backward: CTF multiply, Nyquist zeroing, scale (projection_funcs.py:385-399).
-__device__ __forceinline__ float prologue(const PointGeom &g, int64_t id, const float *ctf, int nyquist, float scale) {
+__device__ __forceinline__ float prologue(const PointGeom &g, int64_t id, const float *ctf, const CtfCoef *ctfc,
+                                          int nyquist, float scale) {
   float sc = scale;
   if (nyquist && on_nyquist(g, id)) sc = 0.0f;
-  if (ctf) sc *= __ldg(ctf + id);
-  return sc;
+  return sc * ctf_factor(ctf, ctfc, g, id);
 }
 
 constexpr int kLMin = -8;   // window corners relative to the bin lie in [kLMin, kLMin + 16)
@@ -196,7 +197,7 @@ __device__ __forceinline__ void stage_subproblem(const SpreadParams &a, const St
     }
     const int id = sp_id(sp.idf);
     float sc = (a.nyquist && sp_nyquist(sp.idf)) ? 0.0f : a.scale;
-    if (a.ctf) sc *= __ldg(a.ctf + id);
+    sc *= ctf_factor(a.ctf, a.ctfc, a.g, id);
     s.pid[slot] = id;
     s.sc[slot] = sc;
   }
@@ -574,10 +575,11 @@ int launch_w(SpreadParams a, int nchan, bool comp, int64_t max_blocks, cudaStrea
 // Per-image adjoint (no sum over images): direct global atomics, one thread per point.
 template <int KT, int W>
 __global__ void spread_unagg_kernel(PointGeom g, KernelSpec k, int64_t M, const float2 *__restrict__ vals,
-                                    int64_t ips, const float *ctf, int nyquist, float scale, float2 *grids) {
+                                    int64_t ips, const float *ctf, const CtfCoef *ctfc, int nyquist, float scale,
+                                    float2 *grids) {
   const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (id >= M) return;
-  const float sc = prologue(g, id, ctf, nyquist, scale);
+  const float sc = prologue(g, id, ctf, ctfc, nyquist, scale);
   if (sc == 0.0f) return;
   const int n = g.n;
   float t[3];
@@ -631,6 +633,7 @@ int launch_spread(cov3d_plan *p, const void *values, int64_t in_ps, int64_t in_c
   a.ips = in_ps;
   a.ics = in_cs;
   a.ctf = e.ctf;
+  a.ctfc = e.ctfc;
   a.nyquist = e.nyquist;
   a.scale = e.scale;
   a.grid = static_cast<float2 *>(grid);
@@ -673,18 +676,18 @@ int launch_spread_unaggregated(cov3d_plan *p, const void *values, int64_t in_ps,
   switch (p->kernel) {
     case COV3D_KERNEL_NEAREST:
       spread_unagg_kernel<COV3D_KERNEL_NEAREST, 1>
-          <<<blocks, 256, 0, p->stream>>>(g, k, p->n_points, v, in_ps, e.ctf, e.nyquist, e.scale, out);
+          <<<blocks, 256, 0, p->stream>>>(g, k, p->n_points, v, in_ps, e.ctf, e.ctfc, e.nyquist, e.scale, out);
       break;
     case COV3D_KERNEL_LINEAR:
       spread_unagg_kernel<COV3D_KERNEL_LINEAR, 2>
-          <<<blocks, 256, 0, p->stream>>>(g, k, p->n_points, v, in_ps, e.ctf, e.nyquist, e.scale, out);
+          <<<blocks, 256, 0, p->stream>>>(g, k, p->n_points, v, in_ps, e.ctf, e.ctfc, e.nyquist, e.scale, out);
       break;
     default:
       switch (p->width) {
 #define COV3D_UW(Wv)                                                                                     \
   case Wv:                                                                                             \
     spread_unagg_kernel<COV3D_KERNEL_ES, Wv>                                                           \
-        <<<blocks, 256, 0, p->stream>>>(g, k, p->n_points, v, in_ps, e.ctf, e.nyquist, e.scale, out); \
+        <<<blocks, 256, 0, p->stream>>>(g, k, p->n_points, v, in_ps, e.ctf, e.ctfc, e.nyquist, e.scale, out); \
     break;
         COV3D_UW(4) COV3D_UW(5) COV3D_UW(6) COV3D_UW(7) COV3D_UW(8)
 #undef COV3D_UW

@@ -67,6 +67,36 @@ def ctf_images(defocus_um, L, pixel_size, voltage_kv=300.0, cs_mm=2.7, amplitude
     return (-(math.sqrt(1 - A * A) * torch.sin(chi) + A * torch.cos(chi))).to(torch.float32)
 
 
+def ctf_params(defocus_um, pixel_size, voltage_kv=300.0, cs_mm=2.7, amplitude_contrast=0.1, defocus_v_um=None,
+               astigmatism_deg=None, phase_shift_deg=None, device="cuda"):
+    """(n, 8) CTF parameters (pixel size, defocus u and v in A, astigmatism angle, kV, Cs, amplitude
+    contrast, phase shift) in the column order of the reference's ``ctf_params``
+    (``source.py:157-172``), for the kernels to compute the CTF from."""
+    dev = torch.device(device)
+    du = defocus_um.to(dev, torch.float32).reshape(-1) * 1e4
+    n = du.shape[0]
+    dv = du if defocus_v_um is None else defocus_v_um.to(dev, torch.float32).reshape(-1) * 1e4
+    z = torch.zeros((n,), device=dev)
+    ang = z if astigmatism_deg is None else astigmatism_deg.to(dev, torch.float32).reshape(-1)
+    ph = z if phase_shift_deg is None else phase_shift_deg.to(dev, torch.float32).reshape(-1)
+    cols = [torch.full((n,), float(pixel_size), device=dev), du, dv, ang, torch.full((n,), float(voltage_kv), device=dev),
+            torch.full((n,), float(cs_mm), device=dev), torch.full((n,), float(amplitude_contrast), device=dev), ph]
+    return torch.stack(cols, dim=1).contiguous()
+
+
+def ctf_from_params(params, L):
+    """(n, L, L) float32 CTF images from (n, 8) parameters, computed by the library's kernel
+    (``cov3d_ctf_images``): the CTF the fused step evaluates in-kernel with ``ctf_params``."""
+    from . import _lib
+
+    params = params.to(torch.float32).contiguous()
+    out = torch.empty((params.shape[0], L, L), dtype=torch.float32, device=params.device)
+    with torch.cuda.device(params.device):
+        _lib.call("cov3d_ctf_images", _lib.stream_ptr(params.device), _lib.ptr(params), params.shape[0], int(L),
+                  _lib.ptr(out))
+    return out
+
+
 def vmf_cluster_rotations(n, clusters=8, kappa=5.0, generator=None, device="cuda"):
     """(n, 3, 3) rotations whose viewing directions (third column, the normal of the projected
     Fourier plane) follow an equal-weight mixture of ``clusters`` von Mises-Fisher

@@ -77,6 +77,13 @@ typedef struct {
 /* Epilogue / prologue flags of the projection operators (reference projection_funcs.py:346-399). */
 #define COV3D_APPLY_NYQUIST 1 /* zero pixel row 0 and column 0 when L is even */
 #define COV3D_APPLY_CTF 2     /* multiply by a per-pixel real filter (B, L*L) */
+#define COV3D_APPLY_CTF_PARAMS 4 /* multiply by the CTF computed from per-image parameters: the d_ctf
+                                    argument then holds (B, COV3D_CTF_NPARAMS) floats */
+/* CTF parameters per image, in order: pixel size (A), defocus u (A), defocus v (A), astigmatism
+ * angle (degrees), voltage (kV), spherical aberration Cs (mm), amplitude contrast, phase shift
+ * (degrees) -- the columns of the reference's ctf_params (source.py:157-172), which it hands to
+ * cryoDRGN's compute_ctf. */
+#define COV3D_CTF_NPARAMS 8
 
 /* ------------------------------------------------------------------ library */
 
@@ -145,6 +152,12 @@ int cov3d_execute_type2(cov3d_plan *plan, const float *d_vol_real, const void *d
  * complex64 (NufftPlan.execute_adjoint, nufft_plan.py:366-392). */
 int cov3d_execute_type1(cov3d_plan *plan, const void *d_values, int nchan, void *d_vol_out);
 
+/* CTF images (n_images, L, L) float32 from per-image parameters (n_images, COV3D_CTF_NPARAMS):
+ * the reference's ImageSource.get_ctf (source.py:157-172), which evaluates cryoDRGN's
+ * compute_ctf on its frequency lattice (row index = first frequency coordinate).  The phase is
+ * formed in double-float arithmetic and reduced modulo 2 pi before the float sine and cosine. */
+int cov3d_ctf_images(void *stream, const float *d_params, int64_t n_images, int L, float *d_out);
+
 /* Deapodisation factors of the plan's kernel on the L^3 voxel grid, float32 (the ES
  * analogue of VolumeBase.init_grid_correction, covar.py:45-65). */
 int cov3d_grid_correction(const cov3d_plan *plan, float *d_out);
@@ -173,6 +186,8 @@ typedef struct {
   double *d_cost;           /* optional device scalar receiving the cost (no host sync needed) */
   int gram_bf16;            /* 1: per-image Gram contractions in BF16 on the tensor cores (FP32
                                accumulation, cov3d_gram_bf16); 0: FP32 on the CUDA cores */
+  int ctf_params;           /* 1: d_ctf holds (B, COV3D_CTF_NPARAMS) CTF parameters and the CTF is
+                               computed in the kernels (nothing of size (B, L^2)); 0: d_ctf is (B, L^2) */
   int fourier_reg_per_channel; /* 0: d_fourier_reg is one (n^3) array for every eigenvolume; 1: it is
                                (r, n^3), one per eigenvolume, as CovarTrainer.compute_fourier_reg_term
                                builds it (covar_sgd.py:420-430) */

@@ -825,3 +825,31 @@ def regularize_mean_from_halfsets(m1, rhs1, lhs1, m2, rhs2, lhs2, rtol=1e-6):
         vol = x.reshape((L,) * 3).real
     vol = np.real(centered_ifft3(centered_fft3(vol) * sphere_mask(L)))
     return vol / grid_correction_discretized(L, us, "nearest"), it
+
+
+# ----------------------------------------------------------------------------- CTF from parameters
+
+
+def ctf_from_params(params, L):
+    """(N, 8) CTF parameters -> (N, L, L) float64 CTF images: the weak-phase CTF
+    ``sqrt(1 - w^2) sin(gamma) - w cos(gamma)``, ``gamma = 2 pi (-df lam s^2 / 2 + Cs lam^3 s^4 / 4) -
+    phase``, ``df = (dfu + dfv + (dfu - dfv) cos(2 (atan2(fy, fx) - dfang))) / 2``,
+    ``lam = 12.2639 / sqrt(V + 0.97845e-6 V^2)``, as cryoDRGN's ``compute_ctf`` defines it for the
+    reference's ``ImageSource.get_ctf`` (``source.py:157-172``), on the frequency lattice of
+    ``get_phase_shift_grid`` (``poses.py:70-89``; first coordinate along image rows) divided by
+    the pixel size.  Columns: pixel size (A), dfu, dfv (A), dfang (deg), voltage (kV), Cs (mm),
+    amplitude contrast, phase shift (deg).  cryoDRGN is not installed here, so this restatement
+    of its published formula is the CTF's only pin (parity unpinned against cryoDRGN itself)."""
+    p = np.asarray(params, np.float64).reshape(-1, 8)
+    apix, dfu, dfv, dfang, volt, cs, w, ps = [p[:, i, None, None] for i in range(8)]
+    k = np.ceil(np.arange(-L / 2, L / 2))
+    fx = k[None, :, None] / (L * apix)
+    fy = k[None, None, :] / (L * apix)
+    volt = volt * 1e3
+    cs = cs * 1e7
+    lam = 12.2639 / np.sqrt(volt + 0.97845e-6 * volt**2)
+    ang = np.arctan2(fy, fx)
+    s2 = fx**2 + fy**2
+    df = 0.5 * (dfu + dfv + (dfu - dfv) * np.cos(2 * (ang - dfang * np.pi / 180)))
+    gamma = 2 * np.pi * (-0.5 * df * lam * s2 + 0.25 * cs * lam**3 * s2**2) - ps * np.pi / 180
+    return np.sqrt(1 - w**2) * np.sin(gamma) - w * np.cos(gamma)

@@ -242,3 +242,44 @@ def test_fused_step_per_channel_regulariser(pkg, dev, L):
     assert rel(val, ref[0]) < TOL_COST
     assert rel(gv, ref[1]) < TOL_GRAD
     assert rel(gl, ref[2]) < TOL_GRAD
+
+
+def _ctf_params(rng, B):
+    apix = np.full(B, 1.5)
+    dfu = rng.uniform(1e4, 3e4, B)
+    dfv = dfu * rng.uniform(0.9, 1.1, B)
+    ang = rng.uniform(0, 180, B)
+    ps = rng.uniform(0, 30, B)
+    return np.stack([apix, dfu, dfv, ang, np.full(B, 300.0), np.full(B, 2.7), np.full(B, 0.1), ps], 1).astype(np.float32)
+
+
+@pytest.mark.parametrize("L", [32, 128, 129])
+def test_ctf_from_params_matches_fp64_formula(pkg, dev, L):
+    """The in-kernel CTF (double-float phase, reduced modulo 2 pi) against the float64 formula,
+    with astigmatism and phase shifts, up to Nyquist at 1.5 A pixels (phases of hundreds of
+    radians): absolute error below 2e-6 (the float32 rounding of the reduced angle)."""
+    rng = np.random.default_rng(L)
+    prm = _ctf_params(rng, 16)
+    got = pkg.synthetic.ctf_from_params(torch.tensor(prm, device=dev), L).cpu().numpy()
+    want = O.ctf_from_params(prm, L)
+    assert np.abs(got - want).max() < 2e-6
+
+
+def test_fused_step_with_ctf_params_matches_fp64(pkg, dev):
+    """The fused step with the CTF computed in-kernel from parameters against the float64
+    oracle given the float64 CTF images (r = 10: the grouped interpolation path)."""
+    L, r, B = 64, 10, 6
+    vec, ls, R, imgs, _, fr = _es_case(L, r, B, 64)
+    prm = _ctf_params(np.random.default_rng(3), B)
+    ctf64 = O.ctf_from_params(prm, L)
+    step = pkg.FusedCovarStep(L, r, "nufft", 2, width=6, device=dev)
+    step.set_rotations(torch.tensor(R, device=dev))
+    val, gv, gl = step(torch.tensor(vec, device=dev), torch.tensor(ls, device=dev),
+                       torch.tensor(imgs, device=dev).reshape(B, -1), None, 5.0, reg_scale=0.01,
+                       fourier_reg=torch.tensor(fr, device=dev), sync_cost=True,
+                       ctf_params=torch.tensor(prm, device=dev))
+    ref = O.covar_cost_grad(vec, ls, imgs, O.rotated_points(R.astype(np.float64), L), ctf64, 5.0, kind="es", width=6,
+                            reg_scale=0.01, fourier_reg=fr)
+    assert rel(val, ref[0]) < TOL_COST
+    assert rel(gv, ref[1]) < TOL_GRAD
+    assert rel(gl, ref[2]) < TOL_GRAD

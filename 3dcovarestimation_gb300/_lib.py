@@ -24,6 +24,8 @@ APPLY_NYQUIST, APPLY_CTF, APPLY_CTF_PARAMS = 1, 2, 4
 # CTF parameters per image (pixel size, defocus u, v, astigmatism angle, kV, Cs, amplitude contrast,
 # phase shift)
 CTF_NPARAMS = 8
+# cov3d_plan_reserve flags
+RESERVE_POINTS, RESERVE_GRAM_BF16 = 1, 2
 
 c_int, c_int64, c_double, c_float, c_void_p = ctypes.c_int, ctypes.c_int64, ctypes.c_double, ctypes.c_float, ctypes.c_void_p
 
@@ -50,6 +52,7 @@ _SIGNATURES = {
     "cov3d_status_string": (ctypes.c_char_p, [c_int]),
     "cov3d_plan_create": (c_int, [c_int, c_int, c_double, ctypes.POINTER(Opts), ctypes.POINTER(c_void_p)]),
     "cov3d_plan_destroy": (c_int, [c_void_p]),
+    "cov3d_plan_reserve": (c_int, [c_void_p, c_int64, c_int, c_int, c_int]),
     "cov3d_plan_set_stream": (c_int, [c_void_p, c_void_p]),
     "cov3d_plan_info": (c_int, [c_void_p, ctypes.POINTER(c_int), ctypes.POINTER(c_int), ctypes.POINTER(c_double)]),
     "cov3d_setpts": (c_int, [c_void_p, c_void_p, c_int64, c_int, c_int64, c_int64, c_int]),

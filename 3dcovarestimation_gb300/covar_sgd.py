@@ -174,7 +174,7 @@ class FusedCovarStep:
     """
 
     def __init__(self, resolution, rank, nufft_disc="nufft", upsampling_factor=2, width=6, eps=1e-6,
-                 compensated=True, device=None, bin_size=0, gram_precision="fp32"):
+                 compensated=True, device=None, bin_size=0, gram_precision="fp32", max_batch=None):
         kernel = {"nufft": _lib.KERNEL_ES, "bilinear": _lib.KERNEL_LINEAR, "nearest": _lib.KERNEL_NEAREST}[nufft_disc]
         if gram_precision not in ("fp32", "bf16"):
             raise ValueError("gram_precision must be 'fp32' or 'bf16'")
@@ -184,6 +184,8 @@ class FusedCovarStep:
                           device=device)
         self.L, self.rank, self.nufft_disc = resolution, rank, nufft_disc
         self.device = self.plan.device
+        if max_batch:  # every workspace sized now: steps of up to max_batch images allocate nothing
+            self.plan.reserve(max_batch, resolution, rank, points=True, gram_bf16=self.gram_bf16)
         self.d_cost = torch.zeros((1,), dtype=torch.float64, device=self.device)
 
     def set_rotations(self, rotmats):
@@ -404,7 +406,7 @@ class CovarTrainer:
             ds.to_fourier_domain() if self.optimize_in_fourier_domain else ds.to_spatial_domain()
         self.step_fn = FusedCovarStep(self.covar.resolution, self.covar.rank, nufft_disc, self.covar.upsampling_factor,
                                       width=width, compensated=compensated, device=self.device,
-                                      gram_precision=gram_precision)
+                                      gram_precision=gram_precision, max_batch=self.batch_size)
         if nufft_disc == "nufft":
             self.covar.grid_correction = self.step_fn.plan.grid_correction().to(self.device)
         else:

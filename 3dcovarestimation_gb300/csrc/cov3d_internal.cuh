@@ -184,6 +184,9 @@ inline bool prunable(const cov3d_plan *p) { return p->L % 2 == 0 && p->n >= p->L
 
 // points_sort.cu
 int sort_points(cov3d_plan *p);
+int reserve_sort(cov3d_plan *p, int64_t M);
+// gram_tc.cu: the BF16 Gram's operand and sum buffers for B images of P pixels at rank r
+int reserve_gram_bf16(cov3d_plan *p, int B, int P, int r);
 
 // interp.cu
 struct GridArgs {

@@ -253,6 +253,14 @@ __global__ void gram_from_real_kernel(const float *__restrict__ G, int B, int r,
 
 }  // namespace
 
+int reserve_gram_bf16(cov3d_plan *p, int B, int P, int r) {
+  const int C = 2 * (r + 1);
+  const int Ppad = (P + kKT - 1) / kKT * kKT;
+  COV3D_TRY(grow(p->xbf, (int64_t)B * C * Ppad * 2));
+  COV3D_TRY(grow(p->gsum, (int64_t)B * C * C * 4 + 16));
+  return COV3D_OK;
+}
+
 int launch_gram_bf16(cov3d_plan *p, cudaStream_t st, int B, int P, int r, const void *q, int64_t is, int64_t ps,
                      int64_t cs, const void *images, void *gram, void *h, float *yy) {
   const int C = 2 * (r + 1);
@@ -265,8 +273,7 @@ int launch_gram_bf16(cov3d_plan *p, cudaStream_t st, int B, int P, int r, const 
   const int N = ((img_per_tile * C + 15) / 16) * 16;
   const int groups = (B + img_per_tile - 1) / img_per_tile;
   const int ksplit = Ppad / kKT >= 2 * kStages ? 2 : 1;
-  COV3D_TRY(grow(p->xbf, (int64_t)B * C * Ppad * 2));
-  COV3D_TRY(grow(p->gsum, (int64_t)B * C * C * 4 + 16));
+  COV3D_TRY(reserve_gram_bf16(p, B, P, r));
   __nv_bfloat16 *X = p->xbf.as<__nv_bfloat16>();
   float *G = p->gsum.as<float>();
   int *err = reinterpret_cast<int *>(G + (int64_t)B * C * C);

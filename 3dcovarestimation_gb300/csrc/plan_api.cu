@@ -316,6 +316,28 @@ int cov3d_plan_create(int L, int n_trans, double eps, const cov3d_opts *opts, co
   return COV3D_OK;
 }
 
+int cov3d_plan_reserve(cov3d_plan *p, int64_t max_images, int points_L, int nchan, int flags) {
+  if (!valid(p) || max_images < 0 || points_L < 1 || nchan < 1 || nchan > p->n_trans) {
+    set_error("invalid reserve arguments (nchan must be in 1..n_trans)");
+    return COV3D_EINVAL;
+  }
+  const int64_t P = (int64_t)points_L * points_L;
+  const int64_t M = max_images * P;
+  const int64_t n3 = (int64_t)p->n * p->n * p->n;
+  COV3D_TRY(reserve_sort(p, M));
+  COV3D_TRY(grow(p->rot, max_images * 9 * 4));
+  if (flags & COV3D_RESERVE_POINTS) COV3D_TRY(grow(p->pts, max_images * 3 * P * 4));
+  // the covariance step: fine grid and its gradient, projections, per-image matrices
+  COV3D_TRY(grow(p->fine, n3 * nchan * 8));
+  COV3D_TRY(grow(p->fine2, n3 * nchan * 8));
+  COV3D_TRY(grow(p->q, M * nchan * 8));
+  COV3D_TRY(grow(p->small, max_images * (nchan * nchan * 8 * 2 + nchan * 8 * 2 + 8 + 8) + 64));
+  COV3D_TRY(grow(p->ctfc, max_images * (int64_t)sizeof(CtfCoef)));
+  if (line_transforms_apply(p)) COV3D_TRY(ensure_twiddles(p, p->n));
+  if (flags & COV3D_RESERVE_GRAM_BF16) COV3D_TRY(reserve_gram_bf16(p, (int)max_images, (int)P, nchan));
+  return check_cuda(cudaStreamSynchronize(p->stream), "reserve");
+}
+
 int cov3d_plan_destroy(cov3d_plan *p) {
   if (!p) return COV3D_OK;
   if (p->ffts) {

@@ -172,13 +172,8 @@ void launch_count(cov3d_plan *p, const PointGeom &g, const KernelSpec &k, int bl
 
 }  // namespace
 
-int sort_points(cov3d_plan *p) {
-  const int64_t M = p->n_points;
-  if (M <= 0) return COV3D_OK;
-  if (M >= (int64_t)(1 << 30)) {
-    set_error("too many points (%lld); the limit is 2^30-1 per plan", (long long)M);
-    return COV3D_EINVAL;
-  }
+// Every buffer the sort of M points uses (a no-op when they are large enough already).
+int reserve_sort(cov3d_plan *p, int64_t M) {
   const int64_t nb = p->bins.nbins;
   const int64_t max_subs = nb + M / p->max_sub + 1;
   COV3D_TRY(grow(p->bin_count, (nb + 2) * 4));
@@ -193,7 +188,18 @@ int sort_points(cov3d_plan *p) {
   COV3D_TRY(grow(p->sub_first, max_subs * 4));
   COV3D_TRY(grow(p->sub_count, max_subs * 4));
   COV3D_TRY(grow(p->nsub, 16));
+  return COV3D_OK;
+}
 
+int sort_points(cov3d_plan *p) {
+  const int64_t M = p->n_points;
+  if (M <= 0) return COV3D_OK;
+  if (M >= (int64_t)(1 << 30)) {
+    set_error("too many points (%lld); the limit is 2^30-1 per plan", (long long)M);
+    return COV3D_EINVAL;
+  }
+  COV3D_TRY(reserve_sort(p, M));
+  const int64_t nb = p->bins.nbins;
   COV3D_CUDA(cudaMemsetAsync(p->fine_count.as<int>(), 0, (nb * kSubKeys + 1) * sizeof(int), p->stream));
   const PointGeom g = make_geom(p);
   const KernelSpec k = make_kernel(p);

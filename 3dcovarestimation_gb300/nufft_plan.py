@@ -99,6 +99,13 @@ class _Plan:
             _lib.call("cov3d_setrot", h, _lib.ptr(rot), rot.shape[0], int(points_L))
         self.n_images, self.points_L = rot.shape[0], int(points_L)
 
+    def reserve(self, max_images, points_L, nchan, points=False, gram_bf16=False):
+        """Size the plan's workspaces at set-up (``cov3d_plan_reserve``) so that later calls on
+        up to ``max_images`` images allocate nothing."""
+        flags = (_lib.RESERVE_POINTS if points else 0) | (_lib.RESERVE_GRAM_BF16 if gram_bf16 else 0)
+        with torch.cuda.device(self.device):
+            _lib.call("cov3d_plan_reserve", self.bind(), int(max_images), int(points_L), int(nchan), flags)
+
     def timing(self, enable=True):
         """Enable CUDA-event timing of the plan's phases (sort, pack, FFTs, interp, gram, ...)."""
         _lib.call("cov3d_plan_timing", self.handle, 1 if enable else 0)

@@ -30,7 +30,8 @@ sys.path.insert(0, ROOT)
 
 METRIC = "cov-SGD images/s (L=128,r=10)"
 WORKLOAD = ("cov-SGD step, GPU drop-in plain FP32 config: L=128, pixel 1.5 A, r=10 Gaussian-blob eigenvolumes, "
-            "batch 1024, uniform SO(3) poses, CTF 300 kV / Cs 2.7 mm / AC 0.1 / defocus U[1,3] um, SNR 0.05, "
+            "batch 1024, uniform SO(3) poses, CTF 300 kV / Cs 2.7 mm / AC 0.1 / defocus U[1,3] um (from per-image "
+            "parameters), SNR 0.05, "
             "NUFFT upsampling 2, ML objective + Fourier regulariser, Adam")
 GPU_INTERP = "ES kernel width 6 (tol 1e-6), periodic, compensated FP32 spreading"
 REF_INTERP = ("reference NufftPlanDiscretized bilinear (grid_sample), the reference command line's default; its ES "
@@ -42,7 +43,7 @@ def shared_config(args, world):
     return {"workload": WORKLOAD, "global_batch": args.batch * world, "L": args.L, "rank": args.rank, "upsample": 2,
             "objective": "ml + Fourier regulariser", "optimizer": "Adam", "snr": 0.05, "seed": args.seed,
             "l2": "inputs larger than L2: each GPU step reads a distinct resident 1024-image batch "
-                  "(134 MB images + 67 MB CTF) and 1.34 GB fine grids",
+                  "(134 MB images; CTF computed in the kernels from 32 bytes of parameters per image) and 1.34 GB fine grids",
             "parallelism": f"dp{world}"}
 
 
@@ -219,7 +220,8 @@ def make_dataset(pkg, args, dev, n_images):
     sqrt_lam = torch.linspace(1.0, 0.3, r, device=dev) * L**1.5
     rot = syn.uniform_rotations(n_images, generator=g, device=dev)
     defocus = torch.rand((n_images,), generator=g, device=dev) * 2.0 + 1.0
-    ctf = syn.ctf_images(defocus, L, 1.5, device=dev)
+    prm = syn.ctf_params(defocus, 1.5, device=dev)  # the CTF is computed in the kernels from these
+    ctf = syn.ctf_from_params(prm, L)
     images = torch.empty((n_images, L * L), dtype=torch.complex64, device=dev)
     plan = pkg.NufftPlan((L,) * 3, batch_size=r, device=dev, width=args.width)
     B = args.batch
@@ -231,7 +233,7 @@ def make_dataset(pkg, args, dev, n_images):
     signal_var = float((images.abs() ** 2).mean())
     noise_var = signal_var / 0.05
     images += torch.randn(images.shape, generator=g, device=dev, dtype=torch.complex64) * (noise_var ** 0.5)
-    return images, rot, ctf.reshape(n_images, -1), noise_var
+    return images, rot, prm, noise_var
 
 
 def run_mean_cg(pkg, args, dev):
@@ -323,15 +325,16 @@ def run_gb300(args):
     pkg = importlib.import_module("3dcovarestimation_gb300")
     from importlib import import_module
 
+    syn = import_module("3dcovarestimation_gb300.synthetic")
     L, r, B = args.L, args.rank, args.batch
     nb = max(2, args.resident_batches)
-    images, rot, ctf, noise_var = make_dataset(pkg, args, dev, nb * B)
+    images, rot, prm, noise_var = make_dataset(pkg, args, dev, nb * B)
     images = images.reshape(nb, B, -1)
     rot = rot.reshape(nb, B, 3, 3).contiguous()
-    ctf = ctf.reshape(nb, B, -1)
+    prm = prm.reshape(nb, B, -1)
     covar = pkg.Covar(L, r, upsampling_factor=2).to(dev)
     step_fn = pkg.FusedCovarStep(L, r, "nufft", 2, width=args.width, device=dev,
-                                 compensated=not args.uncompensated)
+                                 compensated=not args.uncompensated, max_batch=B)
     covar.vectors.grad = torch.zeros_like(covar.vectors)
     covar.log_sqrt_eigenvals.grad = torch.zeros_like(covar.log_sqrt_eigenvals)
     groups = covar.grad_lr_factor()
@@ -350,13 +353,13 @@ def run_gb300(args):
     def grads_allreduce():
         dp.allreduce_mean_([covar.vectors.grad, covar.log_sqrt_eigenvals.grad])
 
-    def step(k, imgs=None, ctfs=None, rots=None):
+    def step(k, imgs=None, prms=None, rots=None):
         b = (k * world + rank) % nb
         step_fn.set_rotations(rot[b] if rots is None else rots)
         c, _, _ = step_fn(covar.vectors.detach(), covar.log_sqrt_eigenvals.detach(),
-                          images[b] if imgs is None else imgs, ctf[b] if ctfs is None else ctfs, noise_var,
-                          reg_scale, fourier_reg, grad_vectors=covar.vectors.grad,
-                          grad_log_sqrt=covar.log_sqrt_eigenvals.grad)
+                          images[b] if imgs is None else imgs, None, noise_var, reg_scale, fourier_reg,
+                          grad_vectors=covar.vectors.grad, grad_log_sqrt=covar.log_sqrt_eigenvals.grad,
+                          ctf_params=prm[b] if prms is None else prms)
         grads_allreduce()
         opt.step()
         return c.reshape(())
@@ -406,9 +409,9 @@ def run_gb300(args):
     e2e_steps = args.e2e_steps or args.steps
     nhost = min(nb, 4)
     h_images = images[:nhost].cpu().pin_memory()
-    h_ctf = ctf[:nhost].cpu().pin_memory()
+    h_prm = prm[:nhost].cpu().pin_memory()
     h_rot = rot[:nhost].cpu().pin_memory()
-    bufs = [(torch.empty_like(images[0]), torch.empty_like(ctf[0]), torch.empty_like(rot[0])) for _ in range(2)]
+    bufs = [(torch.empty_like(images[0]), torch.empty_like(prm[0]), torch.empty_like(rot[0])) for _ in range(2)]
     ready = [torch.cuda.Event() for _ in range(2)]
     free = [torch.cuda.Event() for _ in range(2)]
     copy_stream = torch.cuda.Stream()
@@ -418,7 +421,7 @@ def run_gb300(args):
         j, slot = k % nhost, k % 2
         with torch.cuda.stream(copy_stream):
             copy_stream.wait_event(free[slot])
-            for dst, src in zip(bufs[slot], (h_images[j], h_ctf[j], h_rot[j])):
+            for dst, src in zip(bufs[slot], (h_images[j], h_prm[j], h_rot[j])):
                 dst.copy_(src, non_blocking=True)
             ready[slot].record(copy_stream)
 
@@ -448,14 +451,14 @@ def run_gb300(args):
     bf16 = None
     if not args.no_bf16:
         step_bf = pkg.FusedCovarStep(L, r, "nufft", 2, width=args.width, device=dev,
-                                     compensated=not args.uncompensated, gram_precision="bf16")
+                                     compensated=not args.uncompensated, gram_precision="bf16", max_batch=B)
 
         def step16(k):
             b = (k * world + rank) % nb
             step_bf.set_rotations(rot[b])
-            c, _, _ = step_bf(covar.vectors.detach(), covar.log_sqrt_eigenvals.detach(), images[b], ctf[b], noise_var,
+            c, _, _ = step_bf(covar.vectors.detach(), covar.log_sqrt_eigenvals.detach(), images[b], None, noise_var,
                               reg_scale, fourier_reg, grad_vectors=covar.vectors.grad,
-                              grad_log_sqrt=covar.log_sqrt_eigenvals.grad)
+                              grad_log_sqrt=covar.log_sqrt_eigenvals.grad, ctf_params=prm[b])
             return c
 
         for k in range(2):
@@ -481,20 +484,21 @@ def run_gb300(args):
     # grid_sample semantics): the like-for-like comparison with the reference's CPU arm
     bilinear = None
     if not args.no_bilinear:
-        step_bl = pkg.FusedCovarStep(L, r, "bilinear", 2, device=dev, compensated=not args.uncompensated)
+        step_bl = pkg.FusedCovarStep(L, r, "bilinear", 2, device=dev, compensated=not args.uncompensated,
+                                     max_batch=B)
         covar_bl = pkg.Covar(L, r, upsampling_factor=2).to(dev)
         covar_bl.vectors.grad = torch.zeros_like(covar_bl.vectors)
         covar_bl.log_sqrt_eigenvals.grad = torch.zeros_like(covar_bl.log_sqrt_eigenvals)
         opt_bl = torch.optim.Adam([{"params": covar_bl.vectors, "lr": 1e-6 * B},
                                    {"params": covar_bl.log_sqrt_eigenvals, "lr": 1e-4 * B}])
 
-        def step_bilinear(k, imgs=None, ctfs=None, rots=None):
+        def step_bilinear(k, imgs=None, prms=None, rots=None):
             b = (k * world + rank) % nb
             step_bl.set_rotations(rot[b] if rots is None else rots)
             c, _, _ = step_bl(covar_bl.vectors.detach(), covar_bl.log_sqrt_eigenvals.detach(),
-                              images[b] if imgs is None else imgs, ctf[b] if ctfs is None else ctfs, noise_var,
-                              reg_scale, fourier_reg, grad_vectors=covar_bl.vectors.grad,
-                              grad_log_sqrt=covar_bl.log_sqrt_eigenvals.grad)
+                              images[b] if imgs is None else imgs, None, noise_var, reg_scale, fourier_reg,
+                              grad_vectors=covar_bl.vectors.grad, grad_log_sqrt=covar_bl.log_sqrt_eigenvals.grad,
+                              ctf_params=prm[b] if prms is None else prms)
             dp.allreduce_mean_([covar_bl.vectors.grad, covar_bl.log_sqrt_eigenvals.grad])
             opt_bl.step()
             return c.reshape(())
@@ -544,7 +548,7 @@ def run_gb300(args):
 
         def wbatch(b):
             wplan.setrot(rot[b])
-            q = pkg.vol_forward(eigv, wplan, ctf[b].reshape(B, L, L), fourier_domain=True)
+            q = pkg.vol_forward(eigv, wplan, syn.ctf_from_params(prm[b], L), fourier_domain=True)
             return wc.compute_latentMAP_batch(images[b], q, noise_var, linv)[0]
 
         wbatch(0)

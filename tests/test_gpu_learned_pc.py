@@ -57,3 +57,35 @@ def test_committed_network_beats_the_circulant_preconditioner(pkg, dev):
     ax = pkg.centered_ifft3(reg * pkg.centered_fft3(xx, padding_size=(n,) * 3), cropping_size=(128,) * 3)
     b = prob.b.to(torch.complex128)
     assert float(torch.linalg.vector_norm(b - ax) / torch.linalg.vector_norm(b)) < 2e-5
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                                                    "3dcovarestimation_gb300", "learned_pc_weights.npz")),
+                    reason="no trained weights")
+def test_committed_network_against_the_diagonal_preconditioner(pkg, dev):
+    """The fallback the learned preconditioner is judged against: the Fourier-diagonal 1/reg_lhs
+    on the fine grid.  Same problem, same rtol, both converge; the learned symbol (features +
+    network + the L^3 symbol, timed inside the solve) takes less wall time than the diagonal
+    preconditioner, whose every iteration costs a second fine-grid transform pair."""
+    import time
+
+    lp = pkg.learned_pc
+    pc = lp.LearnedPreconditioner(device=dev)
+    gen = lp.ProblemGenerator(128, 60000, dev)
+    prob = gen(78, solve_rtol=1e-5)
+    # warm both paths (transform plans, network kernels)
+    pkg.cg_solve(prob.reg, prob.b, prob.x0, 128, rtol=1e-1, maxiter=2, precond="diagonal")
+    pkg.cg_solve(prob.reg, prob.b, prob.x0, 128, rtol=1e-1, maxiter=2, precond=pc.symbol(prob.reg, 128))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    _, info_d = pkg.cg_solve(prob.reg, prob.b, prob.x0, 128, rtol=1e-5, maxiter=20000, precond="diagonal")
+    torch.cuda.synchronize()
+    t_diag = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    sym = pc.symbol(prob.reg, 128)
+    _, info_l = pkg.cg_solve(prob.reg, prob.b, prob.x0, 128, rtol=1e-5, maxiter=20000, precond=sym)
+    torch.cuda.synchronize()
+    t_learned = time.perf_counter() - t0
+    assert info_d.converged and info_l.converged
+    print(f"diagonal PC {info_d.iters} iterations {t_diag:.3f} s; learned {info_l.iters} iterations {t_learned:.3f} s")
+    assert t_learned < t_diag

@@ -112,7 +112,6 @@ struct cov3d_plan {
   cov3d::Bins bins{};
   int max_sub = 288;
   cov3d::DevBuf bin_count;     // int (nbins + 1), last = dead points
-  cov3d::DevBuf fine_count, fine_off;  // int (nbins * 64 + 1): points and offsets per corner block of a bin
   cov3d::DevBuf bin_off;       // int (nbins + 2)
   cov3d::DevBuf sub_off;       // int (nbins + 1)
   cov3d::DevBuf pt_bin, pt_rank;              // int (M)

@@ -2,8 +2,6 @@
 // bin-sorted points: each subproblem's tile of the fine grid is read from HBM once into shared
 // memory and reused by all its points; the projection epilogue (Nyquist zeroing, CTF
 // multiply, 1/L) is fused.
-#include <cstdlib>
-
 #include "cov3d_device.cuh"
 
 namespace cov3d {
@@ -215,320 +213,6 @@ __global__ void __launch_bounds__(kInterpWarps * 32) interp_kernel(const InterpP
   }
 }
 
-// ----------------------------------------------------------------------------- grouped points
-// Register-blocked ES interpolation for many channels (the covariance step's r eigenvolumes).
-//
-// The points of a subproblem are counting-sorted by the 2x2x2 block of their window corner
-// (64 blocks per 8^3 bin); the points of one block all lie in the union window of W + 1 cells
-// per axis that starts at the block's smallest corner (W along an axis where they share the
-// corner).  A warp task is up to Q * kGroupP points of one block: lane (g, c) owns channel c of
-// kGroupP points (group g), so every row of the union is read once per task -- the same
-// addresses for the Q groups, a shared-memory broadcast -- and each loaded value feeds
-// kGroupP points: per row and point, the row is reduced with the point's axis-2 weights
-// (zero outside its window) and added with its axis-0 x axis-1 weight.  The work per point is
-// (W + 1)^2 (W + 2) multiply-adds per channel against W^3 (1.8x at W = 6), in exchange for
-// four times fewer shared loads per multiply-add than one point per lane; the tile staging and
-// the epilogue (Nyquist zeroing, CTF, scale) are those of interp_kernel.
-constexpr int kGroupWarps = 16;
-// COV3D_INTERP_GROUP=0 selects the one-point-per-warp kernel for every channel count
-// (comparison runs); read once per process.
-inline bool interp_group_disabled() {
-  static const bool off = [] {
-    const char *v = getenv("COV3D_INTERP_GROUP");
-    return v && v[0] == '0';
-  }();
-  return off;
-}
-constexpr int kGroupP = 4;  // points per lane
-constexpr int kGroupKeys = 64;
-
-// Complex channels per pass: the T^3 tile of CH channels and the per-point weight records must
-// fit in shared memory next to each other.
-template <int W>
-struct GroupCH {
-  static constexpr int value = W <= 6 ? 10 : (W == 7 ? 8 : 6);
-};
-
-__host__ __device__ constexpr size_t group_smem_bytes(int T, int CH, int max_sub) {
-  return (size_t)T * T * T * CH * 8 + (size_t)max_sub * (24 * 4 + 6 * 4) + (size_t)(kGroupKeys * 3 + 4) * 4;
-}
-
-// One task of a warp: the union window rows [u0, u0 + e0) x [u1, u1 + e1) x [u2, u2 + E2) of the
-// tile; acc[p] += sum over the window of w0 w1 w2 * value for this lane's kGroupP points.
-template <int W, int CH, int E2>
-__device__ __forceinline__ void group_rows(const float2 *__restrict__ tile, int u0, int u1, int u2, int e0, int e1,
-                                           int cl, const float (&w1r)[kGroupP][W + 1],
-                                           const float (&w2r)[kGroupP][W + 1], const int (&o0)[kGroupP],
-                                           const int (&slot)[kGroupP], const bool (&valid)[kGroupP],
-                                           const float *__restrict__ wts, float2 (&acc)[kGroupP]) {
-  constexpr int T = kBin + W - 1;
-  for (int i0 = 0; i0 < e0; ++i0) {
-    float w0c[kGroupP];
-#pragma unroll
-    for (int p = 0; p < kGroupP; ++p) {
-      const int j = i0 - o0[p];
-      w0c[p] = (valid[p] && j >= 0 && j < W) ? wts[slot[p] * 24 + j] : 0.0f;
-    }
-    const float2 *row = tile + (((u0 + i0) * T + u1) * T + u2) * CH + cl;
-#pragma unroll
-    for (int i1 = 0; i1 < W + 1; ++i1) {
-      if (i1 < e1) {
-        float2 v[E2];
-#pragma unroll
-        for (int k = 0; k < E2; ++k) v[k] = row[(i1 * T + k) * CH];
-#pragma unroll
-        for (int p = 0; p < kGroupP; ++p) {
-          float2 t = __fmul2_rn(make_float2(w2r[p][0], w2r[p][0]), v[0]);
-#pragma unroll
-          for (int k = 1; k < E2; ++k) t = __ffma2_rn(make_float2(w2r[p][k], w2r[p][k]), v[k], t);
-          const float rw = w0c[p] * w1r[p][i1];
-          acc[p] = __ffma2_rn(make_float2(rw, rw), t, acc[p]);
-        }
-      }
-    }
-  }
-}
-
-template <int W, int CH>
-__global__ void __launch_bounds__(kGroupWarps * 32, 1) interp_group_kernel(const InterpParams a) {
-  constexpr int T = kBin + W - 1;
-  constexpr int Q = 32 / CH;
-  constexpr int TP = Q * kGroupP;  // points per task (<= 32)
-  constexpr int U = W + 1;
-  static_assert(TP <= 32, "a task's points are read by one lane each");
-  extern __shared__ float4 smem4[];
-  float2 *tile = reinterpret_cast<float2 *>(smem4);                 // T^3 * CH, [cell][channel]
-  float *wts = reinterpret_cast<float *>(tile + T * T * T * CH);     // max_sub * 24: w0[8] w1[8] w2[8]
-  int *pid = reinterpret_cast<int *>(wts + a.max_sub * 24);          // point id, sorted order
-  float *psc = reinterpret_cast<float *>(pid + a.max_sub);           // epilogue factor
-  int *pcor = reinterpret_cast<int *>(psc + a.max_sub);              // corners l0 | l1 << 8 | l2 << 16
-  int *pkey = pcor + a.max_sub;                                      // key | rank << 8, input order
-  int *tfirst = pkey + a.max_sub;                                    // task -> first sorted slot
-  int *tcount = tfirst + a.max_sub;                                  // task -> points
-  int *kcnt = tcount + a.max_sub;                                    // kGroupKeys
-  int *koff = kcnt + kGroupKeys;                                     // kGroupKeys + 1
-  int *ktoff = koff + kGroupKeys + 1;                                // kGroupKeys + 1
-  int *tcounter = ktoff + kGroupKeys + 1;
-  __shared__ long long s_rowoff[T * T];
-  __shared__ int s_coloff[T];
-  __shared__ int s_lo[3], s_hi[3];  // corner extents of the subproblem's points
-  const int sub = blockIdx.x;
-  if (sub >= *a.nsub) return;
-  const int bin = a.sub_bin[sub];
-  const int first = a.sub_first[sub];
-  const int cnt = a.sub_count[sub];
-  const int nb12 = a.bins.nb[1] * a.bins.nb[2];
-  const int ts0 = (bin / nb12) * kBin;
-  const int ts1 = ((bin / a.bins.nb[2]) % a.bins.nb[1]) * kBin;
-  const int ts2 = (bin % a.bins.nb[2]) * kBin;
-  const int n = a.g.n;
-  const int tid = threadIdx.x;
-
-  for (int e = tid; e < T * T; e += blockDim.x) {
-    const int c0 = e / T, c1 = e - (e / T) * T;
-    int m0 = ts0 + c0, m1 = ts1 + c1;
-    m0 = m0 >= n ? m0 - n : m0;
-    m1 = m1 >= n ? m1 - n : m1;
-    m0 += a.shift;
-    m1 += a.shift;
-    m0 = m0 >= n ? m0 - n : m0;
-    m1 = m1 >= n ? m1 - n : m1;
-    s_rowoff[e] = ((int64_t)m0 * n + m1) * n * a.cs;
-  }
-  for (int e = tid; e < T; e += blockDim.x) {
-    int m2 = ts2 + e;
-    m2 = m2 >= n ? m2 - n : m2;
-    m2 += a.shift;
-    s_coloff[e] = m2 >= n ? m2 - n : m2;
-  }
-  for (int e = tid; e < kGroupKeys; e += blockDim.x) kcnt[e] = 0;
-  if (tid < 3) {
-    s_lo[tid] = kBin;
-    s_hi[tid] = -1;
-  }
-  if (tid == 0) *tcounter = 0;
-  __syncthreads();
-  // block keys of the window corners, ranks within a key, and the corners' extents
-  {
-    int lo0 = kBin, lo1 = kBin, lo2 = kBin, hi0 = -1, hi1 = -1, hi2 = -1;
-    for (int k = tid; k < cnt; k += blockDim.x) {
-      const SortedPoint sp = a.pts[first + k];
-      const int l0 = wrap1(first_cell<COV3D_KERNEL_ES, W>(sp.t0), n) - ts0;
-      const int l1 = wrap1(first_cell<COV3D_KERNEL_ES, W>(sp.t1), n) - ts1;
-      const int l2 = wrap1(first_cell<COV3D_KERNEL_ES, W>(sp.t2), n) - ts2;
-      const int key = ((l0 >> 1) * 4 + (l1 >> 1)) * 4 + (l2 >> 1);
-      pkey[k] = key | (atomicAdd(kcnt + key, 1) << 8);
-      lo0 = min(lo0, l0), lo1 = min(lo1, l1), lo2 = min(lo2, l2);
-      hi0 = max(hi0, l0), hi1 = max(hi1, l1), hi2 = max(hi2, l2);
-    }
-    lo0 = __reduce_min_sync(0xffffffffu, lo0), lo1 = __reduce_min_sync(0xffffffffu, lo1);
-    lo2 = __reduce_min_sync(0xffffffffu, lo2);
-    hi0 = __reduce_max_sync(0xffffffffu, hi0), hi1 = __reduce_max_sync(0xffffffffu, hi1);
-    hi2 = __reduce_max_sync(0xffffffffu, hi2);
-    if ((tid & 31) == 0 && hi0 >= 0) {
-      atomicMin(s_lo + 0, lo0), atomicMin(s_lo + 1, lo1), atomicMin(s_lo + 2, lo2);
-      atomicMax(s_hi + 0, hi0), atomicMax(s_hi + 1, hi1), atomicMax(s_hi + 2, hi2);
-    }
-  }
-  __syncthreads();
-  // the tile cells the points' windows reach ([lo, hi + W) per axis), asynchronously: in flight
-  // while the points are sorted
-  const float2 *gbase = a.grid + (int64_t)a.ch0 * a.chs;
-  {
-    const int b0 = s_lo[0], b1 = s_lo[1], b2 = s_lo[2];
-    const int x0 = s_hi[0] - b0 + W, x1 = s_hi[1] - b1 + W, x2 = s_hi[2] - b2 + W;
-    const int box = x0 * x1 * x2;
-    for (int e = tid; e < CH * box; e += blockDim.x) {
-      const int ch = e / box;
-      const int rem = e - ch * box;
-      const int c2 = b2 + rem % x2;
-      const int r01 = rem / x2;
-      const int c1 = b1 + r01 % x1, c0 = b0 + r01 / x1;
-      const int rowi = c0 * T + c1;
-      const bool ok = ch < a.nch;
-      const float2 *src = ok ? gbase + s_rowoff[rowi] + (int64_t)s_coloff[c2] * a.cs + (int64_t)ch * a.chs : gbase;
-      const unsigned dst = (unsigned)__cvta_generic_to_shared(tile + (rowi * T + c2) * CH + ch);
-      asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(dst), "l"(src), "r"(ok ? 8 : 0) : "memory");
-    }
-  }
-  asm volatile("cp.async.commit_group;\n" ::: "memory");
-  if (tid < 32) {  // point offsets and task offsets per key (two keys per lane), and the task list
-    const int k0 = 2 * tid;
-    const int c0 = kcnt[k0], c1 = kcnt[k0 + 1];
-    const int t0 = (c0 + TP - 1) / TP, t1 = (c1 + TP - 1) / TP;
-    int ip = c0 + c1, it = t0 + t1;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int xp = __shfl_up_sync(0xffffffffu, ip, o), xt = __shfl_up_sync(0xffffffffu, it, o);
-      if (tid >= o) {
-        ip += xp;
-        it += xt;
-      }
-    }
-    const int bp = ip - (c0 + c1), bt = it - (t0 + t1);
-    koff[k0] = bp;
-    koff[k0 + 1] = bp + c0;
-    ktoff[k0] = bt;
-    ktoff[k0 + 1] = bt + t0;
-    for (int j = 0; j < t0; ++j) {
-      tfirst[bt + j] = bp + j * TP;
-      tcount[bt + j] = min(TP, c0 - j * TP);
-    }
-    for (int j = 0; j < t1; ++j) {
-      tfirst[bt + t0 + j] = bp + c0 + j * TP;
-      tcount[bt + t0 + j] = min(TP, c1 - j * TP);
-    }
-    if (tid == 31) {
-      koff[kGroupKeys] = ip;
-      ktoff[kGroupKeys] = it;
-    }
-  }
-  __syncthreads();
-  // per point, in sorted order: the axis weights, the id, the epilogue factor, the corners
-  for (int k = tid; k < cnt; k += blockDim.x) {
-    const SortedPoint sp = a.pts[first + k];
-    const int kr = pkey[k];
-    const int slot = koff[kr & 255] + (kr >> 8);
-    float w[3][W];
-    const int c0 = wrap1(taps<COV3D_KERNEL_ES, W>(sp.t0, a.k.beta, w[0]), n) - ts0;
-    const int c1 = wrap1(taps<COV3D_KERNEL_ES, W>(sp.t1, a.k.beta, w[1]), n) - ts1;
-    const int c2 = wrap1(taps<COV3D_KERNEL_ES, W>(sp.t2, a.k.beta, w[2]), n) - ts2;
-    float *ws = wts + slot * 24;
-#pragma unroll
-    for (int d = 0; d < 3; ++d)
-#pragma unroll
-      for (int j = 0; j < 8; ++j) ws[d * 8 + j] = j < W ? w[d][j] : 0.0f;
-    pid[slot] = sp_id(sp.idf);
-    float sc = (a.nyquist && sp_nyquist(sp.idf)) ? 0.0f : a.scale;
-    sc *= ctf_factor(a.ctf, a.ctfc, a.g, sp_id(sp.idf));
-    psc[slot] = sc;
-    pcor[slot] = c0 | (c1 << 8) | (c2 << 16);
-  }
-  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-  __syncthreads();
-
-  const int ntasks = ktoff[kGroupKeys];
-  const int lane = tid & 31;
-  const int g = lane / CH;
-  const bool live = g < Q;
-  const int gl = live ? g : 0;
-  const int cl = live ? lane - g * CH : 0;
-  for (;;) {
-    int task = 0;
-    if (lane == 0) task = atomicAdd(tcounter, 1);
-    task = __shfl_sync(0xffffffffu, task, 0);
-    if (task >= ntasks) break;
-    const int tf = tfirst[task], tn = tcount[task];
-    // union window of the task's points: smallest corner and extent (W, or W + 1 where the
-    // corners differ) per axis
-    const int cor = pcor[tf + (lane < tn ? lane : 0)];
-    const int l0 = cor & 255, l1 = (cor >> 8) & 255, l2 = cor >> 16;
-    const int u0 = __reduce_min_sync(0xffffffffu, l0), u1 = __reduce_min_sync(0xffffffffu, l1);
-    const int u2 = __reduce_min_sync(0xffffffffu, l2);
-    const int e0 = __reduce_max_sync(0xffffffffu, l0) - u0 + W;
-    const int e1 = __reduce_max_sync(0xffffffffu, l1) - u1 + W;
-    const int e2 = __reduce_max_sync(0xffffffffu, l2) - u2 + W;
-    float w1r[kGroupP][U], w2r[kGroupP][U];
-    int o0[kGroupP], slot[kGroupP];
-    bool valid[kGroupP];
-#pragma unroll
-    for (int p = 0; p < kGroupP; ++p) {
-      const int idx = gl * kGroupP + p;
-      valid[p] = live && idx < tn;
-      slot[p] = tf + (valid[p] ? idx : 0);
-      const int cp = pcor[slot[p]];
-      o0[p] = (cp & 255) - u0;
-      const int o1 = ((cp >> 8) & 255) - u1, o2 = (cp >> 16) - u2;
-      const float4 *wp = reinterpret_cast<const float4 *>(wts + slot[p] * 24);
-      const float4 a1 = wp[2], b1 = wp[3], a2 = wp[4], b2 = wp[5];
-      const float x1[8] = {a1.x, a1.y, a1.z, a1.w, b1.x, b1.y, b1.z, b1.w};
-      const float x2[8] = {a2.x, a2.y, a2.z, a2.w, b2.x, b2.y, b2.z, b2.w};
-#pragma unroll
-      for (int k = 0; k < U; ++k) {
-        // tap k - o of the point (o = 0 or 1), zero outside its window
-        const float y1 = o1 ? (k > 0 ? x1[k - 1] : 0.0f) : (k < W ? x1[k] : 0.0f);
-        const float y2 = o2 ? (k > 0 ? x2[k - 1] : 0.0f) : (k < W ? x2[k] : 0.0f);
-        w1r[p][k] = valid[p] ? y1 : 0.0f;
-        w2r[p][k] = valid[p] ? y2 : 0.0f;
-      }
-    }
-    float2 acc[kGroupP];
-#pragma unroll
-    for (int p = 0; p < kGroupP; ++p) acc[p] = make_float2(0.f, 0.f);
-    if (e2 == W) {
-      group_rows<W, CH, W>(tile, u0, u1, u2, e0, e1, cl, w1r, w2r, o0, slot, valid, wts, acc);
-    } else {
-      group_rows<W, CH, W + 1>(tile, u0, u1, u2, e0, e1, cl, w1r, w2r, o0, slot, valid, wts, acc);
-    }
-    // epilogue: vol_forward's Nyquist zeroing, CTF multiply and 1/L (projection_funcs.py:355-370)
-    if (live && cl < a.nch) {
-#pragma unroll
-      for (int p = 0; p < kGroupP; ++p) {
-        if (!valid[p]) continue;
-        const float sc = psc[slot[p]];
-        a.out[(int64_t)pid[slot[p]] * a.ops + (int64_t)(a.ch0 + cl) * a.ocs] = make_float2(acc[p].x * sc, acc[p].y * sc);
-      }
-    }
-  }
-}
-
-template <int W>
-int launch_group(InterpParams a, int nchan, int64_t max_blocks, cudaStream_t st) {
-  constexpr int T = kBin + W - 1;
-  constexpr int CH = GroupCH<W>::value;
-  const size_t smem = group_smem_bytes(T, CH, a.max_sub);
-  cudaError_t e = cudaFuncSetAttribute(interp_group_kernel<W, CH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem);
-  if (e != cudaSuccess) return check_cuda(e, "cudaFuncSetAttribute(interp_group_kernel)");
-  for (int done = 0; done < nchan; done += CH) {
-    a.ch0 = done;
-    a.nch = min(CH, nchan - done);
-    interp_group_kernel<W, CH><<<(unsigned)max_blocks, kGroupWarps * 32, smem, st>>>(a);
-    COV3D_TRY(launched("interp_group_kernel"));
-  }
-  return COV3D_OK;
-}
-
 // Points whose window lies entirely outside the grid (zero padding) get zero outputs.
 __global__ void interp_dead_kernel(const SortedPoint *__restrict__ pts, const int *__restrict__ off, int64_t nbins,
                                    int nchan, float2 *__restrict__ out, int64_t ops, int64_t ocs) {
@@ -557,8 +241,6 @@ int launch_cp(const InterpParams &a, int64_t max_blocks, cudaStream_t st) {
 template <int KT, int W>
 int launch_w(InterpParams a, int nchan, int64_t max_blocks, cudaStream_t st) {
   constexpr int CPMAX = InterpCP<W>::value;
-  if (KT == COV3D_KERNEL_ES && W >= 4 && nchan >= 8 && a.max_sub <= 288 && !interp_group_disabled())
-    return launch_group<W < 4 ? 4 : W>(a, nchan, max_blocks, st);
   int done = 0;
   while (done < nchan) {
     const int left = nchan - done;

@@ -346,8 +346,7 @@ int cov3d_plan_destroy(cov3d_plan *p) {
   }
   DevBuf *bufs[] = {&p->gc1d, &p->pts, &p->rot, &p->bin_count, &p->bin_off, &p->sub_off, &p->pt_bin, &p->pt_rank,
                     &p->sorted, &p->sub_bin, &p->sub_first, &p->sub_count, &p->nsub, &p->fine, &p->fine2, &p->q,
-                    &p->small, &p->acc, &p->cgw, &p->xbf, &p->gsum, &p->fftw, &p->fine_count, &p->fine_off,
-                    &p->ctfc};
+                    &p->small, &p->acc, &p->cgw, &p->xbf, &p->gsum, &p->fftw, &p->ctfc};
   for (DevBuf *b : bufs) release(*b);
   if (p->h_acc) cudaFreeHost(p->h_acc);
   if (p->ev_pool) {

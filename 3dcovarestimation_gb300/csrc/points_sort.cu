@@ -1,9 +1,5 @@
 // Spatial binning of nonuniform points (counting sort by the first cell of each point's
-// kernel window) and the subproblem table used by the interpolation and spreading kernels.
-// Inside a bin the points are ordered by the 2x2x2 block of their window corner (64 blocks per
-// 8^3 bin), so a subproblem -- a run of at most max_sub points of one bin -- holds whole blocks:
-// the grouped interpolation kernel shares the row loads of a block's union window between its
-// points.
+// kernel window) and the subproblem table used by the spreading kernel.
 //
 // The reference hands unsorted points to cuFINUFFT with gpu_sort=0 (nufft_plan.py:297) or to
 // grid_sample; here every point set is sorted once per setpts/setrot so that interpolation
@@ -18,8 +14,6 @@ namespace {
 // Bin of every point (dead points, whose window misses the grid, go to bin nbins) and its
 // rank in the bin.  The lanes of a warp that share a bin (neighbouring pixels mostly do) take
 // their ranks from one atomic on the bin's counter, in lane order.
-constexpr int kSubKeys = 64;  // 4 x 4 x 4 corner blocks per bin
-
 template <int KT, int W>
 __global__ void bin_count_kernel(PointGeom g, KernelSpec k, Bins bins, int64_t M, int *__restrict__ count,
                                  int *__restrict__ pt_bin, int *__restrict__ pt_rank) {
@@ -29,7 +23,7 @@ __global__ void bin_count_kernel(PointGeom g, KernelSpec k, Bins bins, int64_t M
   if (valid) {
     float t[3];
     point_index(g, id, t);
-    int b[3], sk[3];
+    int b[3];
     bool dead = false;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
@@ -45,11 +39,8 @@ __global__ void bin_count_kernel(PointGeom g, KernelSpec k, Bins bins, int64_t M
         c0 = min(max(c0, 0), g.n - 1);
       }
       b[d] = c0 / bins.bs[d];
-      sk[d] = (c0 - b[d] * bins.bs[d]) * 4 / bins.bs[d];  // corner block inside the bin, 0..3
     }
-    // fine bucket: bin * 64 + corner block (the dead points in bucket nbins * 64)
-    bin = dead ? (int)bins.nbins * kSubKeys
-               : ((b[0] * bins.nb[1] + b[1]) * bins.nb[2] + b[2]) * kSubKeys + (sk[0] * 4 + sk[1]) * 4 + sk[2];
+    bin = dead ? (int)bins.nbins : (b[0] * bins.nb[1] + b[1]) * bins.nb[2] + b[2];
   }
   const unsigned grp = __match_any_sync(0xffffffffu, bin);
   const int lane = threadIdx.x & 31;
@@ -60,34 +51,6 @@ __global__ void bin_count_kernel(PointGeom g, KernelSpec k, Bins bins, int64_t M
   if (!valid) return;
   pt_bin[id] = bin;
   pt_rank[id] = base + __popc(grp & ((1u << lane) - 1u));
-}
-
-// Per bin, one warp: exclusive scan of its 64 bucket counts (offsets inside the bin) and the bin's
-// total; the dead bucket is a bin of its own.
-__global__ void fine_scan_kernel(const int *__restrict__ fine_count, int64_t nbins, int *__restrict__ fine_off,
-                                 int *__restrict__ bin_count) {
-  const int64_t bin = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (bin > nbins) return;
-  if (bin == nbins) {
-    if (lane == 0) {
-      fine_off[nbins * kSubKeys] = 0;
-      bin_count[nbins] = fine_count[nbins * kSubKeys];
-    }
-    return;
-  }
-  const int *c = fine_count + bin * kSubKeys;
-  const int a = c[2 * lane], b = c[2 * lane + 1];
-  int incl = a + b;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const int t = __shfl_up_sync(0xffffffffu, incl, o);
-    if (lane >= o) incl += t;
-  }
-  const int base = incl - (a + b);
-  fine_off[bin * kSubKeys + 2 * lane] = base;
-  fine_off[bin * kSubKeys + 2 * lane + 1] = base + a;
-  if (lane == 31) bin_count[bin] = incl;
 }
 
 // Single-block exclusive scans over the bin counts: point offsets, and subproblem offsets
@@ -134,12 +97,10 @@ __global__ void bin_scan_kernel(const int *__restrict__ count, int64_t nbins, in
 }
 
 __global__ void scatter_kernel(PointGeom g, int64_t M, const int *__restrict__ pt_bin, const int *__restrict__ pt_rank,
-                               const int *__restrict__ off, const int *__restrict__ fine_off,
-                               SortedPoint *__restrict__ sorted) {
+                               const int *__restrict__ off, SortedPoint *__restrict__ sorted) {
   const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (id >= M) return;
-  const int fine = pt_bin[id];
-  const int pos = off[fine / kSubKeys] + fine_off[fine] + pt_rank[id];
+  const int pos = off[pt_bin[id]] + pt_rank[id];
   float t[3];
   point_index(g, id, t);
   SortedPoint sp;
@@ -166,8 +127,8 @@ __global__ void subproblem_kernel(int64_t nbins, int max_sub, const int *__restr
 
 template <int KT, int W>
 void launch_count(cov3d_plan *p, const PointGeom &g, const KernelSpec &k, int blocks) {
-  bin_count_kernel<KT, W><<<blocks, 256, 0, p->stream>>>(g, k, p->bins, p->n_points, p->fine_count.as<int>(),
-                                                        p->pt_bin.as<int>(), p->pt_rank.as<int>());
+  bin_count_kernel<KT, W><<<blocks, 256, 0, p->stream>>>(g, k, p->bins, p->n_points, p->bin_count.as<int>(), p->pt_bin.as<int>(),
+                                                        p->pt_rank.as<int>());
 }
 
 }  // namespace
@@ -177,8 +138,6 @@ int reserve_sort(cov3d_plan *p, int64_t M) {
   const int64_t nb = p->bins.nbins;
   const int64_t max_subs = nb + M / p->max_sub + 1;
   COV3D_TRY(grow(p->bin_count, (nb + 2) * 4));
-  COV3D_TRY(grow(p->fine_count, (nb * kSubKeys + 1) * 4));
-  COV3D_TRY(grow(p->fine_off, (nb * kSubKeys + 1) * 4));
   COV3D_TRY(grow(p->bin_off, (nb + 2) * 4));
   COV3D_TRY(grow(p->sub_off, (nb + 2) * 4));
   COV3D_TRY(grow(p->pt_bin, M * 4));
@@ -200,7 +159,8 @@ int sort_points(cov3d_plan *p) {
   }
   COV3D_TRY(reserve_sort(p, M));
   const int64_t nb = p->bins.nbins;
-  COV3D_CUDA(cudaMemsetAsync(p->fine_count.as<int>(), 0, (nb * kSubKeys + 1) * sizeof(int), p->stream));
+
+  COV3D_CUDA(cudaMemsetAsync(p->bin_count.as<int>(), 0, (nb + 1) * sizeof(int), p->stream));
   const PointGeom g = make_geom(p);
   const KernelSpec k = make_kernel(p);
   const int blocks = (int)((M + 255) / 256);
@@ -220,13 +180,10 @@ int sort_points(cov3d_plan *p) {
       }
   }
   COV3D_LAUNCHED("bin_count_kernel");
-  fine_scan_kernel<<<(unsigned)((nb + 1 + 7) / 8), 256, 0, p->stream>>>(p->fine_count.as<int>(), nb,
-                                                                       p->fine_off.as<int>(), p->bin_count.as<int>());
-  COV3D_LAUNCHED("fine_scan_kernel");
   bin_scan_kernel<<<1, 1024, 0, p->stream>>>(p->bin_count.as<int>(), nb, p->max_sub, p->bin_off.as<int>(), p->sub_off.as<int>(), p->nsub.as<int>());
   COV3D_LAUNCHED("bin_scan_kernel");
   scatter_kernel<<<blocks, 256, 0, p->stream>>>(g, M, p->pt_bin.as<int>(), p->pt_rank.as<int>(), p->bin_off.as<int>(),
-                                                p->fine_off.as<int>(), p->sorted.as<SortedPoint>());
+                                                p->sorted.as<SortedPoint>());
   COV3D_LAUNCHED("scatter_kernel");
   subproblem_kernel<<<(int)((nb + 255) / 256), 256, 0, p->stream>>>(nb, p->max_sub, p->bin_count.as<int>(), p->bin_off.as<int>(),
                                                                     p->sub_off.as<int>(), p->sub_bin.as<int>(), p->sub_first.as<int>(),

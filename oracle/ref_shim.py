@@ -10,7 +10,8 @@ What it does:
 
 * serves placeholder modules for packages that the reference imports at module scope
   but that the discretized hot path never calls (ASPIRE, cuFINUFFT/FINUFFT, cryoDRGN,
-  mrcfile, pandas, starfile, colorlog, matplotlib, umap, seaborn, recovar);
+  mrcfile, pandas, starfile, colorlog, matplotlib, umap, seaborn, recovar; tqdm and
+  scikit-learn only where they are not installed, tqdm as a pass-through progress bar);
 * restates ``aspire.utils.grid_2d`` / ``grid_3d`` from their mathematical definition
   (normalised grid ``ceil(arange(-n/2, n/2)) / (n/2)``), because ``poses.py:197-215``,
   ``fsc_utils.py:43-47`` and ``mean.py:412-414`` do call them.
@@ -111,6 +112,8 @@ class _StubLoader(importlib.abc.Loader):
         if module.__name__ == "aspire.utils":
             module.grid_2d = grid_2d
             module.grid_3d = grid_3d
+        if module.__name__ == "tqdm":
+            module.tqdm = _Progress
 
 
 class _StubFinder(importlib.abc.MetaPathFinder):
@@ -120,8 +123,42 @@ class _StubFinder(importlib.abc.MetaPathFinder):
         return None
 
 
+class _Progress:
+    """Stand-in for ``tqdm.tqdm`` where tqdm is not installed: iterates what it wraps and
+    ignores progress updates."""
+
+    def __init__(self, iterable=None, *args, **kwargs):
+        self.iterable = iterable
+
+    def __iter__(self):
+        return iter(self.iterable if self.iterable is not None else ())
+
+    def update(self, *args, **kwargs):
+        pass
+
+    def set_description(self, *args, **kwargs):
+        pass
+
+    def close(self):
+        pass
+
+
+# optional packages the reference imports at module scope and the timed / fixture paths do
+# not need: stubbed only where they are not installed (the GPU machines lack them)
+OPTIONAL_ROOTS = {"tqdm", "sklearn"}
+
+
+def _installed(name):
+    import importlib.util
+
+    return importlib.util.find_spec(name) is not None
+
+
 def install(reference_root):
     """Put the stub finder first on ``sys.meta_path`` and the reference on ``sys.path``."""
+    for name in OPTIONAL_ROOTS:
+        if name not in STUB_ROOTS and not _installed(name):
+            STUB_ROOTS.add(name)
     if not any(isinstance(f, _StubFinder) for f in sys.meta_path):
         sys.meta_path.insert(0, _StubFinder())
     if reference_root not in sys.path:

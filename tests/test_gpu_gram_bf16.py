@@ -137,3 +137,67 @@ def test_bf16_training_recovers_the_fp32_subspace(pkg, dev):
     if np.dot(a.ravel(), b.ravel()) < 0:
         b = -b
     assert _fsc(a, b)[: L // 4].min() > 0.95
+
+
+def test_bf16_training_at_rank_20_matches_the_fp64_oracle(pkg, dev):
+    """The precision configuration's check at its rank, r = 20: the same covariance SGD (same
+    initial parameters, batches, Adam settings) run with the BF16 tensor-core Gram on the GPU
+    and in float64 by the oracle (ES cost and gradient from oracle/cpu_step.py, Adam in numpy);
+    the principal angles between the two learned 20-dimensional eigen-subspaces and the FSC of
+    the leading eigenvolume (L = 24, 40 steps of 64 images)."""
+    from oracle import cpu_step
+
+    syn = pkg.synthetic
+    L, r, B, nb, steps = 24, 20, 64, 8, 40
+    g = torch.Generator(device=dev).manual_seed(21)
+    eig = syn.gaussian_blob_volumes(r, L, blobs=12, generator=g, device=dev)
+    scales = torch.linspace(3.0, 0.5, r, device=dev).reshape(r, 1, 1, 1)
+    eig = syn.orthonormalize(eig.reshape(r, -1)).reshape(r, L, L, L) * scales * L**1.5
+    plan = pkg.NufftPlan((L,) * 3, batch_size=r, device=dev)
+    batches = []
+    for _ in range(nb):
+        R = syn.uniform_rotations(B, generator=g, device=dev)
+        plan.setrot(R)
+        proj = pkg.vol_forward(eig, plan, None, fourier_domain=True)
+        z = torch.randn((B, r, 1, 1), generator=g, device=dev)
+        img = (proj * z).sum(1).reshape(B, -1)
+        img = img + torch.randn(img.shape, generator=g, device=dev, dtype=torch.complex64) * 0.5 * img.abs().mean()
+        batches.append((R, img.contiguous()))
+    noise_var = float((0.5 * batches[0][1].abs().mean()) ** 2)
+    torch.manual_seed(0)
+    covar = pkg.Covar(L, r).to(dev)
+    v0 = covar.vectors.detach().double().cpu().numpy()
+    l0 = covar.log_sqrt_eigenvals.detach().double().cpu().numpy()
+    lr_v, lr_l = 1e-3, 1e-1
+    # GPU, BF16 Gram
+    covar.vectors.grad = torch.zeros_like(covar.vectors)
+    covar.log_sqrt_eigenvals.grad = torch.zeros_like(covar.log_sqrt_eigenvals)
+    opt = torch.optim.Adam([{"params": covar.vectors, "lr": lr_v}, {"params": covar.log_sqrt_eigenvals, "lr": lr_l}])
+    step = pkg.FusedCovarStep(L, r, "nufft", 2, device=dev, gram_precision="bf16")
+    for k in range(steps):
+        R, img = batches[k % nb]
+        step.set_rotations(R)
+        step(covar.vectors.detach(), covar.log_sqrt_eigenvals.detach(), img, None, noise_var,
+             grad_vectors=covar.vectors.grad, grad_log_sqrt=covar.log_sqrt_eigenvals.grad)
+        opt.step()
+    gpu = covar.get_vectors_spatial_domain().detach().reshape(r, -1).double().cpu().numpy()
+    # float64 oracle with the same Adam (torch's update rule, bias-corrected)
+    host = [(R.double().cpu().numpy(), img.cpu().numpy().reshape(B, L, L)) for R, img in batches]
+    theta = [v0.copy(), l0.copy()]
+    m = [np.zeros_like(t) for t in theta]
+    v = [np.zeros_like(t) for t in theta]
+    for k in range(steps):
+        R, img = host[k % nb]
+        _, gv, gl = cpu_step.covar_cost_grad_es(theta[0], theta[1], R, img, np.ones((B, L, L)), noise_var, width=6)
+        for i, (gr, lr) in enumerate(((gv, lr_v), (gl, lr_l))):
+            m[i] = 0.9 * m[i] + 0.1 * gr
+            v[i] = 0.999 * v[i] + 0.001 * gr * gr
+            mh, vh = m[i] / (1 - 0.9 ** (k + 1)), v[i] / (1 - 0.999 ** (k + 1))
+            theta[i] = theta[i] - lr * mh / (np.sqrt(vh) + 1e-8)
+    ref = (theta[0] * np.exp(theta[1])[:, None, None, None]).reshape(r, -1)
+    ang = _principal_angles_deg(ref, gpu)
+    assert ang.max() < 5.0, ang
+    a, b = ref[0].reshape((L,) * 3), gpu[0].reshape((L,) * 3)
+    if np.dot(a.ravel(), b.ravel()) < 0:
+        b = -b
+    assert _fsc(a, b)[: L // 4].min() > 0.95

@@ -6,7 +6,7 @@ The directory name starts with a digit, so import it with
 ``importlib.import_module("3dcovarestimation_gb300")``.
 """
 
-from . import _lib, dataset, fsc_utils, learned_pc, mean, synthetic, utils, wiener_coords
+from . import _lib, dataset, fsc_utils, learned_pc, mean, results, synthetic, utils, wiener_coords
 from .covar import Covar, Mean
 from .mean import (MeanBackprojector, cg_solve, circulant_symbol, complex_conjugate_gradient,
                    correct_upsampling_padding, get_grid_correction, reconstruct_mean, reconstruct_mean_from_halfsets,

@@ -246,12 +246,13 @@ class MeanBackprojector:
 
 def solve_mean(rhs: torch.Tensor, lhs: torch.Tensor, L: int, upsampling_factor: int = 2, mask=None,
                do_grid_correction: bool = True, rtol: float = 1e-6, maxiter: Optional[int] = None,
-               precond: Union[None, str, torch.Tensor] = None, return_info: bool = False):
-    """The solve part of ``reconstruct_mean`` (reference ``mean.py:215-259``, without
-    init_vol): regularize_lhs, Fourier-diagonal solve, CG padding correction, sphere mask,
-    grid correction, mask."""
+               precond: Union[None, str, torch.Tensor] = None, return_info: bool = False,
+               reg_lhs: Optional[torch.Tensor] = None):
+    """The solve part of ``reconstruct_mean`` (reference ``mean.py:215-259``): regularize_lhs (or
+    the given regularised kernel ``reg_lhs``), Fourier-diagonal solve, CG padding correction,
+    sphere mask, grid correction, mask."""
     dev = rhs.device
-    reg = regularize_lhs(lhs)
+    reg = regularize_lhs(lhs) if reg_lhs is None else reg_lhs.to(device=dev, dtype=torch.float32).contiguous()
     plan = _MeanSolver.get(L, upsampling_factor, dev)
     src = rhs.to(torch.complex64).contiguous()
     b = torch.empty((L, L, L), dtype=torch.complex64, device=dev)
@@ -282,8 +283,6 @@ def reconstruct_mean(dataset, init_vol: Optional[torch.Tensor] = None, mask: Opt
     whose ``.dataset`` has ``offsets``, ``contrasts`` and ``resolution`` (the reference's
     CovarDataset contract), or such a dataset itself.  Images are taken in the Fourier domain.
     Returns the volume, or (volume, rhs, lhs) with ``return_lhs_rhs``."""
-    if init_vol is not None:
-        raise NotImplementedError("init_vol regularisation (mean.py:220-233) is not on the GB300 path")
     if not isinstance(dataset, torch.utils.data.DataLoader):
         if idx is None:
             idx = torch.arange(len(dataset))
@@ -299,8 +298,18 @@ def reconstruct_mean(dataset, init_vol: Optional[torch.Tensor] = None, mask: Opt
     acc = MeanBackprojector(L, upsampling_factor, device)
     for images, pts_rot, filters, batch_idx in loader:
         acc.add(images, filters, ds.offsets[batch_idx], ds.contrasts[batch_idx], pts_rot=pts_rot)
+    reg_lhs = None
+    if init_vol is not None:
+        # regulariser from the initial volume (mean.py:220-233): noise_var over its radial PSD,
+        # upsampled to the fine grid, / L, added to the kernel (which is real: the backprojection
+        # of real |CTF|^2 at point pairs +-k); the reference's diagnostic plot is not made
+        from .fsc_utils import rpsd, upsample_and_expand_fourier_shell
+
+        r = rpsd(init_vol.squeeze(0).to(device))
+        reg = ds.noise_var / upsample_and_expand_fourier_shell(r, L * upsampling_factor, 3) / L
+        reg_lhs = acc.lhs.real + reg.reshape(acc.lhs.shape)
     vol = solve_mean(acc.rhs, acc.lhs, L, upsampling_factor, mask=mask, do_grid_correction=do_grid_correction,
-                     rtol=rtol, precond=precond)
+                     rtol=rtol, precond=precond, reg_lhs=reg_lhs)
     if return_lhs_rhs:
         return vol, acc.rhs, acc.lhs
     return vol

@@ -77,7 +77,17 @@ def grid_3d(n, shifted=False, normalized=True, indexing="zyx", dtype=np.float32)
     return {"x": x, "y": y, "z": z, "r": r, "phi": phi, "theta": theta}
 
 
-class _Placeholder:
+class _PlaceholderMeta(type):
+    """Attribute access on a placeholder class (``plt.figure`` after ``from matplotlib import
+    pyplot as plt``) yields another placeholder."""
+
+    def __getattr__(cls, name):
+        if name.startswith("__"):
+            raise AttributeError(name)
+        return _Placeholder()
+
+
+class _Placeholder(metaclass=_PlaceholderMeta):
     """Stands in for any class or function of a missing package."""
 
     def __init__(self, *args, **kwargs):

@@ -264,6 +264,29 @@ def case_mean(L=10, us=2, N=96, seed=21):
          iters=np.array(handler.iters))
 
 
+def case_mean_initvol(L=10, us=2, N=96, seed=23):
+    """reconstruct_mean with an initial volume (mean.py:220-233): the regulariser
+    noise_var / (radial PSD of init_vol, upsampled) / L added to the kernel instead of
+    regularize_lhs, then the same solve."""
+    rng = np.random.default_rng(seed)
+    rotvecs = random_rotvecs(rng, N)
+    offsets = rng.uniform(-2, 2, (N, 2)).astype(np.float32)
+    contrasts = rng.uniform(0.7, 1.3, N).astype(np.float32)
+    pts, _ = ref_points(rotvecs, np.zeros((N, 2), np.float32), L)
+    images = c32(rng, (N, L, L))
+    filters = rng.uniform(0.2, 1.5, (N, L, L)).astype(np.float32)
+    init_vol = rng.standard_normal((L, L, L)) * 0.5
+    ds = _MeanDataset(torch.tensor(images).to(torch.complex128), pts, torch.tensor(filters, dtype=torch.float64),
+                      torch.tensor(offsets, dtype=torch.float64), torch.tensor(contrasts, dtype=torch.float64), L)
+    ds.noise_var = 2.0
+    loader = torch.utils.data.DataLoader(ds, batch_size=32, shuffle=False)
+    vol, rhs, lhs = mean.reconstruct_mean(loader, init_vol=torch.tensor(init_vol).unsqueeze(0), upsampling_factor=us,
+                                          return_lhs_rhs=True)
+    save(f"mean_initvol_L{L}.npz", L=L, us=us, rotvecs=rotvecs, offsets=offsets, contrasts=contrasts, pts=pts.numpy(),
+         images=images, filters=filters, init_vol=init_vol, noise_var=2.0, volume=vol.numpy(), rhs=rhs.numpy(),
+         lhs=lhs.numpy())
+
+
 class _GainDataset:
     """Stand-in for CovarDataset with what get_total_gain / get_total_covar_gain read."""
 
@@ -589,3 +612,4 @@ if __name__ == "__main__":
     case_latent_dataset()
     case_preprocess()
     case_state_dict()
+    case_mean_initvol()

@@ -213,3 +213,35 @@ def test_cg_iterates_at_n512_match_torch_fft_cg(pkg, dev, precond):
                             precond=pc)
     assert not info.converged and info.iters == 2
     assert rel(xd.reshape(-1).to(torch.complex128), x) < TOL_CG
+
+
+class _MeanData(torch.utils.data.Dataset):
+    """What reconstruct_mean reads from its dataset (the reference's CovarDataset contract)."""
+
+    def __init__(self, g, dev):
+        self.images = torch.tensor(g["images"], device=dev)
+        self.pts_rot = torch.tensor(g["pts"], dtype=torch.float32, device=dev)
+        self.filters = torch.tensor(g["filters"], device=dev)
+        self.offsets = torch.tensor(g["offsets"], device=dev)
+        self.contrasts = torch.tensor(g["contrasts"], device=dev)
+        self.resolution = int(g["L"])
+        self.noise_var = float(g["noise_var"])
+
+    def __len__(self):
+        return len(self.images)
+
+    def __getitem__(self, i):
+        return self.images[i], self.pts_rot[i], self.filters[i], i
+
+
+def test_reconstruct_mean_with_initial_volume_matches_reference(pkg, dev):
+    """reconstruct_mean with init_vol (mean.py:220-233): the kernel regularised by noise_var
+    over the initial volume's radial PSD instead of regularize_lhs; backprojections to 1e-5,
+    the CG solution to the CG tolerance (fixture from the reference in float64)."""
+    g = load_golden("mean_initvol_L10.npz")
+    ds = _MeanData(g, dev)
+    loader = torch.utils.data.DataLoader(ds, batch_size=32, shuffle=False)
+    vol, rhs, lhs = pkg.reconstruct_mean(loader, init_vol=torch.tensor(g["init_vol"], device=dev).unsqueeze(0),
+                                         upsampling_factor=int(g["us"]), return_lhs_rhs=True, device=dev)
+    assert rel(rhs, g["rhs"]) < TOL_FP32 and rel(lhs, g["lhs"]) < TOL_FP32
+    assert rel(vol, g["volume"]) < TOL_CG

@@ -225,3 +225,23 @@ def test_train_covar_halfsets_on_resident_dataset(pkg, dev):
     assert len(costs) == 6 and np.isfinite(costs).all()  # 3 half-set epochs, then 3 on all the data
     assert costs[5] < costs[3]
     assert ds._in_spatial_domain  # complete_training switched the data back
+
+
+def test_recorded_data_has_the_reference_fields(pkg, dev):
+    """recorded_data (workflow.py:477-518) for a Covar on the latent fixture's dataset: the
+    reference's keys, and coordinates equal to latentMAP's for the same eigenvectors."""
+    g = load_golden("latent_dataset_L10_r3.npz")
+    ds = _latent_dataset(g, dev)
+    cov = pkg.Covar(10, 3, vectors=torch.tensor(g["eigenvecs"] * np.sqrt(g["eigenvals"])[:, None, None, None],
+                                                 dtype=torch.float32)).to(dev)
+    gt = torch.tensor(g["eigenvecs"] * np.sqrt(g["eigenvals"])[:, None, None, None], dtype=torch.float32, device=dev)
+    rec = pkg.results.recorded_data(cov, ds, gt_eigenvecs=gt, batch_size=16)
+    keys = {"eigen_est", "eigenval_est", "coords_est", "coords_covar_inv_est", "mean_est", "particles_path", "ctf_path",
+            "poses_path", "ind", "data_sign_inverted", "lazy", "eigenvals_GT", "eigenvectors_GT", "coords_GT",
+            "coords_covar_inv_GT"}
+    assert set(rec) == keys
+    e, lam = cov.eigenvecs
+    c = pkg.wiener_coords.latentMAP(ds, e, lam, batch_size=16)
+    assert rel(rec["coords_est"], c) < 1e-6
+    assert rec["coords_covar_inv_est"].shape == (len(ds), 3, 3)
+    assert rel(np.sort(rec["eigenvals_GT"]), np.sort(g["eigenvals"])) < 1e-5

@@ -64,6 +64,9 @@ _SIGNATURES = {
     "cov3d_spread_unaggregated": (c_int, [c_void_p, c_void_p, c_int64, c_void_p, c_int, c_float, c_void_p]),
     "cov3d_execute_type2": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
     "cov3d_execute_type1": (c_int, [c_void_p, c_void_p, c_int, c_void_p]),
+    "cov3d_project": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_int64, c_int64, c_void_p, c_int,
+                              c_float]),
+    "cov3d_backproject": (c_int, [c_void_p, c_void_p, c_int64, c_int64, c_int, c_void_p, c_int, c_float, c_void_p]),
     "cov3d_grid_correction": (c_int, [c_void_p, c_void_p]),
     "cov3d_ctf_images": (c_int, [c_void_p, c_void_p, c_int64, c_int, c_void_p]),
     "cov3d_covar_cost_grad": (c_int, [c_void_p, ctypes.POINTER(CostArgs), ctypes.POINTER(c_double), c_void_p,

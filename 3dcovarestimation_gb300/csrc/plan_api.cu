@@ -489,7 +489,9 @@ int cov3d_spread_unaggregated(cov3d_plan *p, const void *d_values, int64_t in_po
   return launch_spread_unaggregated(p, d_values, in_point_stride, e, d_grids);
 }
 
-int cov3d_execute_type2(cov3d_plan *p, const float *d_vol_real, const void *d_vol_complex, int nchan, void *d_out) {
+// type 2 with the projection epilogue, output (point, channel) at out[point * ops + ch * ocs]
+static int type2(cov3d_plan *p, const float *d_vol_real, const void *d_vol_complex, int nchan, void *d_out,
+                 int64_t ops, int64_t ocs, const EpilogueArgs &e) {
   if (!valid(p) || (!d_vol_real && !d_vol_complex) || !d_out || nchan < 1 || nchan > p->n_trans) {
     set_error("invalid type-2 arguments (nchan must be in 1..n_trans)");
     return COV3D_EINVAL;
@@ -502,11 +504,32 @@ int cov3d_execute_type2(cov3d_plan *p, const float *d_vol_real, const void *d_vo
   COV3D_TRY(check_cufft(cufftExecC2C(fft, p->fine.as<cufftComplex>(), p->fine.as<cufftComplex>(), CUFFT_FORWARD),
                         "cufftExecC2C(forward)"));
   GridArgs g{p->fine.ptr, 1, n3, p->n - p->n / 2};
-  EpilogueArgs e{nullptr, 0, 1.0f};
-  return launch_interp(p, g, nchan, d_out, 1, p->n_points, e);
+  return launch_interp(p, g, nchan, d_out, ops, ocs, e);
 }
 
-int cov3d_execute_type1(cov3d_plan *p, const void *d_values, int nchan, void *d_vol_out) {
+int cov3d_execute_type2(cov3d_plan *p, const float *d_vol_real, const void *d_vol_complex, int nchan, void *d_out) {
+  EpilogueArgs e{nullptr, 0, 1.0f};
+  return type2(p, d_vol_real, d_vol_complex, nchan, d_out, 1, p ? p->n_points : 0, e);
+}
+
+int cov3d_project(cov3d_plan *p, const float *d_vol_real, const void *d_vol_complex, int nchan, void *d_out,
+                  int64_t out_point_stride, int64_t out_chan_stride, const float *d_ctf, int flags, float scale) {
+  if ((flags & (COV3D_APPLY_CTF | COV3D_APPLY_CTF_PARAMS)) && !d_ctf) {
+    set_error("COV3D_APPLY_CTF / COV3D_APPLY_CTF_PARAMS without a filter or parameter array");
+    return COV3D_EINVAL;
+  }
+  if (!valid(p)) {
+    set_error("invalid plan");
+    return COV3D_EINVAL;
+  }
+  EpilogueArgs e;
+  COV3D_TRY(epilogue_args(p, d_ctf, flags, scale, &e));
+  return type2(p, d_vol_real, d_vol_complex, nchan, d_out, out_point_stride, out_chan_stride, e);
+}
+
+// type 1 with the backprojection prologue, input (point, channel) at values[point * ips + ch * ics]
+static int type1(cov3d_plan *p, const void *d_values, int64_t ips, int64_t ics, int nchan, void *d_vol_out,
+                 const EpilogueArgs &e) {
   if (!valid(p) || !d_values || !d_vol_out || nchan < 1 || nchan > p->n_trans) {
     set_error("invalid type-1 arguments (nchan must be in 1..n_trans)");
     return COV3D_EINVAL;
@@ -514,13 +537,32 @@ int cov3d_execute_type1(cov3d_plan *p, const void *d_values, int nchan, void *d_
   const int64_t n3 = (int64_t)p->n * p->n * p->n;
   COV3D_TRY(grow(p->fine, n3 * nchan * 8));
   COV3D_TRY(launch_zero(p, p->fine.ptr, n3 * nchan * 8));
-  EpilogueArgs e{nullptr, 0, 1.0f};
-  COV3D_TRY(launch_spread(p, d_values, 1, p->n_points, nchan, e, p->fine.ptr, 1, n3, p->n - p->n / 2));
+  COV3D_TRY(launch_spread(p, d_values, ips, ics, nchan, e, p->fine.ptr, 1, n3, p->n - p->n / 2));
   cufftHandle fft;
   COV3D_TRY(get_fft(p, nchan, &fft));
   COV3D_TRY(check_cufft(cufftExecC2C(fft, p->fine.as<cufftComplex>(), p->fine.as<cufftComplex>(), CUFFT_INVERSE),
                         "cufftExecC2C(inverse)"));
   return launch_unpack_complex(p, p->fine.ptr, nchan, 1, d_vol_out);
+}
+
+int cov3d_execute_type1(cov3d_plan *p, const void *d_values, int nchan, void *d_vol_out) {
+  EpilogueArgs e{nullptr, 0, 1.0f};
+  return type1(p, d_values, 1, p ? p->n_points : 0, nchan, d_vol_out, e);
+}
+
+int cov3d_backproject(cov3d_plan *p, const void *d_values, int64_t in_point_stride, int64_t in_chan_stride, int nchan,
+                      const float *d_ctf, int flags, float scale, void *d_vol_out) {
+  if ((flags & (COV3D_APPLY_CTF | COV3D_APPLY_CTF_PARAMS)) && !d_ctf) {
+    set_error("COV3D_APPLY_CTF / COV3D_APPLY_CTF_PARAMS without a filter or parameter array");
+    return COV3D_EINVAL;
+  }
+  if (!valid(p)) {
+    set_error("invalid plan");
+    return COV3D_EINVAL;
+  }
+  EpilogueArgs e;
+  COV3D_TRY(epilogue_args(p, d_ctf, flags, scale, &e));
+  return type1(p, d_values, in_point_stride, in_chan_stride, nchan, d_vol_out, e);
 }
 
 int cov3d_grid_correction(const cov3d_plan *p, float *d_out) {

@@ -179,6 +179,35 @@ class _Plan:
             _lib.call("cov3d_execute_type1", self.bind(), _lib.ptr(vals), C, _lib.ptr(out))
         return out
 
+    def project(self, vol, ctf=None, flags=0, scale=1.0):
+        """Type 2 with vol_forward's epilogue fused (cov3d_project): (C, L, L, L) -> (C, n_points)."""
+        C = vol.shape[0]
+        out = torch.empty((C, self.n_points), dtype=torch.complex64, device=self.device)
+        ctf_t = None if ctf is None else ctf.detach().to(device=self.device, dtype=torch.float32).contiguous()
+        fl = flags | (_lib.APPLY_CTF if ctf_t is not None else 0)
+        with torch.cuda.device(self.device):
+            if vol.is_complex():
+                v = vol.to(torch.complex64).contiguous()
+                _lib.call("cov3d_project", self.bind(), None, _lib.ptr(v), C, _lib.ptr(out), 1, self.n_points,
+                          _lib.ptr(ctf_t), fl, float(scale))
+            else:
+                v = vol.to(torch.float32).contiguous()
+                _lib.call("cov3d_project", self.bind(), _lib.ptr(v), None, C, _lib.ptr(out), 1, self.n_points,
+                          _lib.ptr(ctf_t), fl, float(scale))
+        return out
+
+    def backproject(self, values, ctf=None, flags=0, scale=1.0):
+        """Type 1 with im_backward's prologue fused (cov3d_backproject): (C, n_points) -> (C, L, L, L)."""
+        C = values.shape[0]
+        vals = values.to(torch.complex64).contiguous()
+        out = torch.empty((C, self.L, self.L, self.L), dtype=torch.complex64, device=self.device)
+        ctf_t = None if ctf is None else ctf.detach().to(device=self.device, dtype=torch.float32).contiguous()
+        fl = flags | (_lib.APPLY_CTF if ctf_t is not None else 0)
+        with torch.cuda.device(self.device):
+            _lib.call("cov3d_backproject", self.bind(), _lib.ptr(vals), 1, self.n_points, C, _lib.ptr(ctf_t), fl,
+                      float(scale), _lib.ptr(out))
+        return out
+
     def grid_correction(self):
         out = torch.empty((self.L,) * 3, dtype=torch.float32, device=self.device)
         with torch.cuda.device(self.device):
@@ -219,6 +248,41 @@ class _SpreadFn(torch.autograd.Function):
     @staticmethod
     def backward(ctx, g):
         return ctx.plan.interp(g, ctx.ctf, ctx.flags, ctx.scale), None, None, None, None
+
+
+class _ProjectFn(torch.autograd.Function):
+    """Exact projection with its epilogue (Nyquist zeroing, CTF, scale) in one launch sequence;
+    backward is the exact adjoint with the same prologue."""
+
+    @staticmethod
+    def forward(ctx, vol, plan, ctf, flags, scale):
+        ctx.plan, ctx.ctf, ctx.flags, ctx.scale = plan, ctf, flags, scale
+        ctx.complex_input = vol.is_complex()
+        return plan.project(vol, ctf, flags, scale)
+
+    @staticmethod
+    def backward(ctx, g):
+        if not ctx.needs_input_grad[0]:
+            return None, None, None, None, None
+        grad = ctx.plan.backproject(g, ctx.ctf, ctx.flags, ctx.scale)
+        return (grad if ctx.complex_input else grad.real), None, None, None, None
+
+
+class _BackprojectFn(torch.autograd.Function):
+    """Exact adjoint with im_backward's prologue; backward is the projection."""
+
+    @staticmethod
+    def forward(ctx, values, plan, ctf, flags, scale):
+        ctx.plan, ctx.ctf, ctx.flags, ctx.scale = plan, ctf, flags, scale
+        ctx.complex_input = values.is_complex()
+        return plan.backproject(values, ctf, flags, scale)
+
+    @staticmethod
+    def backward(ctx, g):
+        if not ctx.needs_input_grad[0]:
+            return None, None, None, None, None
+        grad = ctx.plan.project(g, ctx.ctf, ctx.flags, ctx.scale)
+        return (grad if ctx.complex_input else grad.real), None, None, None, None
 
 
 class BaseNufftPlan(ABC):

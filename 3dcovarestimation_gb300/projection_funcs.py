@@ -14,8 +14,8 @@ from typing import List, Optional, Tuple, Union
 import torch
 
 from . import _lib
-from .nufft_plan import (BaseNufftPlan, NufftPlan, NufftPlanDiscretized, NufftSpec, _InterpFn, _SpreadFn,
-                         nufft_adjoint, nufft_forward)
+from .nufft_plan import (BaseNufftPlan, NufftPlan, NufftPlanDiscretized, NufftSpec, _BackprojectFn, _InterpFn,
+                         _ProjectFn, _SpreadFn, nufft_adjoint, nufft_forward)
 
 
 def pad_tensor(tensor: torch.Tensor, size: List[int], dims: Optional[List[int]] = None) -> torch.Tensor:
@@ -112,6 +112,13 @@ def vol_forward(volume: torch.Tensor, plan: Union[BaseNufftPlan, List[BaseNufftP
         proj = proj.reshape(volume.shape[0], vp.n_images, vp.points_L, vp.points_L).transpose(0, 1)
         if volume.is_complex() and volume.dtype != proj.dtype:
             proj = proj.to(volume.dtype)
+    elif isinstance(plan, NufftPlan) and plan._plan is not None and volume.is_cuda:
+        # the exact plan: deapodise + pad + FFT + interpolation with the epilogue fused
+        vol = volume if volume.ndim == 4 else volume.unsqueeze(0)
+        vp = plan._plan
+        proj = _ProjectFn.apply(vol, vp, filters, _lib.APPLY_NYQUIST, 1.0 / L)
+        proj = proj.reshape(vol.shape[0], vp.n_images, vp.points_L, vp.points_L).transpose(0, 1)
+        proj = proj.to(plan.complex_dtype)
     else:
         proj = nufft_forward(volume, plan)
         proj = proj.reshape((*volume.shape[:-3], -1, proj.shape[-2], proj.shape[-1])).transpose(0, 1)
@@ -135,6 +142,11 @@ def im_backward(image: torch.Tensor, plan: BaseNufftPlan, filters: Optional[torc
         if im_fft.dtype == torch.complex128:
             out = out.to(torch.complex128)
         return out.real if not fourier_domain else out
+    if isinstance(plan, NufftPlan) and plan._plan is not None and im_fft.is_cuda:
+        # the exact adjoint with the prologue (CTF, Nyquist zeroing, 1/L) fused into the spreading
+        back = _BackprojectFn.apply(im_fft.reshape(1, -1), plan._plan, filters, _lib.APPLY_NYQUIST, 1.0 / L)
+        back = back.to(plan.complex_dtype)
+        return back.real if not fourier_domain else back
     im_fft = im_fft.clone()
     if filters is not None:
         im_fft = im_fft * filters

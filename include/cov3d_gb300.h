@@ -168,6 +168,19 @@ int cov3d_execute_type1(cov3d_plan *plan, const void *d_values, int nchan, void 
  * formed in double-float arithmetic and reduced modulo 2 pi before the float sine and cosine. */
 int cov3d_ctf_images(void *stream, const float *d_params, int64_t n_images, int L, float *d_out);
 
+/* The exact projection operator: cov3d_execute_type2 with vol_forward's epilogue fused into the
+ * interpolation (Nyquist zeroing, CTF multiply or CTF from parameters, scale; the reference's
+ * vol_forward on a NufftPlan, projection_funcs.py:321-370), output element (point, channel) at
+ * d_out[point*out_point_stride + ch*out_chan_stride]. */
+int cov3d_project(cov3d_plan *plan, const float *d_vol_real, const void *d_vol_complex, int nchan, void *d_out,
+                  int64_t out_point_stride, int64_t out_chan_stride, const float *d_ctf, int flags, float scale);
+
+/* Its exact adjoint: cov3d_execute_type1 with im_backward's prologue fused into the spreading
+ * (projection_funcs.py:373-399); (point, channel) input at d_values[point*in_point_stride +
+ * ch*in_chan_stride], (nchan, L^3) complex64 output. */
+int cov3d_backproject(cov3d_plan *plan, const void *d_values, int64_t in_point_stride, int64_t in_chan_stride,
+                      int nchan, const float *d_ctf, int flags, float scale, void *d_vol_out);
+
 /* Deapodisation factors of the plan's kernel on the L^3 voxel grid, float32 (the ES
  * analogue of VolumeBase.init_grid_correction, covar.py:45-65). */
 int cov3d_grid_correction(const cov3d_plan *plan, float *d_out);

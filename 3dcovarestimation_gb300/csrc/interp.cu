@@ -43,7 +43,7 @@ struct InterpCP {
 
 // One block per subproblem.  The block stages the bin's tile (bin + (W-1)-cell halo) of 2*CP
 // channels in shared memory as [cell][channel] complex, then each warp takes one point at a
-// time: lane (j, q) reads the two channels 2q, 2q+1 of tile[row][corner2 + j] for the W*W
+// time (32 / (W*CP) points for the narrow bilinear and nearest windows): lane (j, q) reads the two channels 2q, 2q+1 of tile[row][corner2 + j] for the W*W
 // window rows -- W*CP contiguous 16-byte values per row, no bank conflicts -- and accumulates
 // weight * value; the W partial sums of each pair are combined through shared memory and the
 // epilogue (Nyquist zeroing, CTF, scale) is applied.
@@ -52,6 +52,9 @@ __global__ void __launch_bounds__(kInterpWarps * 32) interp_kernel(const InterpP
   constexpr int T = kBin + W - 1;
   constexpr int CH = 2 * CP;
   constexpr int LANES = W * CP;
+  // points per warp iteration: several when a point's W*CP lanes (and its 3W weights) fit more
+  // than once into the warp, as for the bilinear and nearest kernels
+  constexpr int PPW = (LANES >= 3 * W && 32 / LANES > 1) ? 32 / LANES : 1;
   extern __shared__ float4 tile4[];  // T^3 * CP float4 (= 2 complex), then kInterpWarps * 32 float4
   float2 *tile = reinterpret_cast<float2 *>(tile4);
   float4 *red = tile4 + T * T * T * CP;
@@ -129,28 +132,34 @@ __global__ void __launch_bounds__(kInterpWarps * 32) interp_kernel(const InterpP
   __syncthreads();
 
   const int warp = tid >> 5, lane = tid & 31;
-  const int j = lane / CP, q = lane - (lane / CP) * CP;  // window cell along axis 2, channel pair
+  // lane = (point slot pp, window cell j along axis 2, channel pair q)
+  const int pp = lane / LANES, sl = lane - (lane / LANES) * LANES;
+  const int j = sl / CP, q = sl - (sl / CP) * CP;
+  const int lane0 = (pp < PPW ? pp : 0) * LANES;  // first lane of this lane's point slot
+  const int wl = PPW == 1 ? lane : sl;             // this lane's tap among the point's 3W weights
   float4 *wred = red + warp * 32;
-  for (int k = warp; k < cnt; k += kInterpWarps) {
-    const SortedPoint sp = s_sp[k];
+  for (int k0 = warp * PPW; k0 < cnt; k0 += kInterpWarps * PPW) {
+    const int k = k0 + pp;
+    const bool pt_ok = pp < PPW && k < cnt;
+    const SortedPoint sp = s_sp[pt_ok ? k : k0];
     int c0[3];
     c0[0] = first_cell<KT, W>(sp.t0);
     c0[1] = first_cell<KT, W>(sp.t1);
     c0[2] = first_cell<KT, W>(sp.t2);
-    // one kernel weight per lane < 3W, then shared through the warp
+    // one kernel weight per lane wl < 3W, then shared through the warp
     float myw = 0.0f;
-    if (lane < 3 * W) {
-      const int d = lane / W, tq = lane - (lane / W) * W;
+    if (wl < 3 * W) {
+      const int d = wl / W, tq = wl - (wl / W) * W;
       const float td = d == 0 ? sp.t0 : d == 1 ? sp.t1 : sp.t2;
       myw = tap_weight<KT, W>(td, tq, a.k.beta);
     }
     float w0[W], w1[W];
 #pragma unroll
     for (int r = 0; r < W; ++r) {
-      w0[r] = __shfl_sync(0xffffffffu, myw, r);
-      w1[r] = __shfl_sync(0xffffffffu, myw, W + r);
+      w0[r] = __shfl_sync(0xffffffffu, myw, lane0 + r);
+      w1[r] = __shfl_sync(0xffffffffu, myw, lane0 + W + r);
     }
-    const float wj = __shfl_sync(0xffffffffu, myw, 2 * W + (j < W ? j : 0));
+    const float wj = __shfl_sync(0xffffffffu, myw, lane0 + 2 * W + (j < W ? j : 0));
     int l0 = c0[0], l1 = c0[1], l2 = c0[2];
     if (KT == COV3D_KERNEL_ES) {
       l0 = wrap1(l0, n);
@@ -161,7 +170,7 @@ __global__ void __launch_bounds__(kInterpWarps * 32) interp_kernel(const InterpP
     l1 -= ts1;
     l2 -= ts2;
     const int cell2 = l2 + j;
-    const bool lane_ok = lane < LANES && cell2 >= 0;
+    const bool lane_ok = pt_ok && cell2 >= 0;
     const float4 *base = tile4 + cell2 * CP + q;
     // two packed FP32 accumulators (FFMA2: one instruction per channel pair of values; the
     // same rounding as two fmaf); each window plane is summed over its rows with the axis-1
@@ -192,11 +201,11 @@ __global__ void __launch_bounds__(kInterpWarps * 32) interp_kernel(const InterpP
     }
     wred[lane] = make_float4(a01.x, a01.y, a23.x, a23.y);
     __syncwarp();
-    if (lane < CP) {
+    if (pt_ok && sl < CP) {
       float4 s = wred[lane];
 #pragma unroll
       for (int r = 1; r < W; ++r) {
-        const float4 x = wred[r * CP + lane];
+        const float4 x = wred[lane + r * CP];
         s.x += x.x;
         s.y += x.y;
         s.z += x.z;
@@ -205,9 +214,9 @@ __global__ void __launch_bounds__(kInterpWarps * 32) interp_kernel(const InterpP
       // epilogue: vol_forward's Nyquist zeroing, CTF multiply and 1/L (projection_funcs.py:355-370)
       const int64_t id = sp_id(sp.idf);
       const float sc = s_sc[k];
-      float2 *o = a.out + id * a.ops + (int64_t)(a.ch0 + 2 * lane) * a.ocs;
-      if (2 * lane < a.nch) o[0] = make_float2(s.x * sc, s.y * sc);
-      if (2 * lane + 1 < a.nch) o[a.ocs] = make_float2(s.z * sc, s.w * sc);
+      float2 *o = a.out + id * a.ops + (int64_t)(a.ch0 + 2 * sl) * a.ocs;
+      if (2 * sl < a.nch) o[0] = make_float2(s.x * sc, s.y * sc);
+      if (2 * sl + 1 < a.nch) o[a.ocs] = make_float2(s.z * sc, s.w * sc);
     }
     __syncwarp();
   }
@@ -250,18 +259,23 @@ int launch_w(InterpParams a, int nchan, int64_t max_blocks, cudaStream_t st) {
       ch = 2 * CPMAX;
       a.nch = ch;
       s = launch_cp<KT, W, CPMAX>(a, max_blocks, st);
-    } else if (left > 4) {
-      ch = left;  // up to 2*CPMAX - 1 channels in the full-size tile
-      a.nch = ch;
-      s = launch_cp<KT, W, CPMAX>(a, max_blocks, st);
-    } else if (left > 2) {
-      ch = left;
-      a.nch = ch;
-      s = launch_cp<KT, W, (CPMAX > 2 ? 2 : CPMAX)>(a, max_blocks, st);
     } else {
       ch = left;
       a.nch = ch;
-      s = launch_cp<KT, W, 1>(a, max_blocks, st);
+      if constexpr (W <= 2) {
+        // narrow windows: the smallest tile that holds the pass, with several points per warp
+        const int need = (left + 1) / 2;
+        if (need <= 3) s = launch_cp<KT, W, 3>(a, max_blocks, st);
+        else if (need <= 4) s = launch_cp<KT, W, 4>(a, max_blocks, st);
+        else if (need <= 5) s = launch_cp<KT, W, 5>(a, max_blocks, st);
+        else if (need <= 8) s = launch_cp<KT, W, 8>(a, max_blocks, st);
+        else s = launch_cp<KT, W, CPMAX>(a, max_blocks, st);
+      } else {
+        // up to 2*CPMAX - 1 channels in the full-size tile; 3-4 and 1-2 channels in smaller ones
+        if (left > 4) s = launch_cp<KT, W, CPMAX>(a, max_blocks, st);
+        else if (left > 2) s = launch_cp<KT, W, (CPMAX > 2 ? 2 : CPMAX)>(a, max_blocks, st);
+        else s = launch_cp<KT, W, 1>(a, max_blocks, st);
+      }
     }
     if (s != COV3D_OK) return s;
     done += ch;

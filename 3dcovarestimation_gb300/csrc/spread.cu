@@ -2,8 +2,6 @@
 // reference's grid_sample backward with FP32 global atomics, nufft_plan.py:171-242), over the
 // bin-sorted point records of points_sort.cu.  See spread_kernel for the decomposition.
 
-#include <cstdlib>
-
 #include "cov3d_device.cuh"
 
 namespace cov3d {
@@ -12,16 +10,6 @@ namespace {
 
 constexpr int kBin = 8;
 constexpr int kSpreadWarps = 16;
-
-// COV3D_SPREAD_PAIRS=0 selects the row-group kernel for every ES spread with many channels
-// (comparison runs); read once per process.
-inline bool spread_pairs_disabled() {
-  static const bool off = [] {
-    const char *v = getenv("COV3D_SPREAD_PAIRS");
-    return v && v[0] == '0';
-  }();
-  return off;
-}
 
 struct SpreadParams {
   PointGeom g;
@@ -132,7 +120,7 @@ __device__ __forceinline__ SubTile sub_tile(const SpreadParams &a, int sub) {
 __device__ __forceinline__ void put_weight(float2 *e, float x) { *e = make_float2(x, x); }
 __device__ __forceinline__ void put_weight(float *e, float x) { *e = x; }
 
-template <int KT, int W, int ROWS, typename E, bool SLICED = false>
+template <int KT, int W, int ROWS, typename E>
 __device__ __forceinline__ void stage_subproblem(const SpreadParams &a, const StageSmem &s, const SubTile &st) {
   using Rec = PointRec<W, ROWS>;
   constexpr int T = Rec::T;
@@ -149,16 +137,7 @@ __device__ __forceinline__ void stage_subproblem(const SpreadParams &a, const St
       c0 = wrap1(c0, n);
       c1 = wrap1(c1, n);
     }
-    int key;
-    if (SLICED) {  // (axis-2 corner pair, l1, l0), the corners of ES points lying in [0, 8)
-      int c2 = first_cell<KT, W>(sp.t2);
-      if (KT == COV3D_KERNEL_ES) c2 = wrap1(c2, n);
-      const int l0 = min(max(c0 - st.ts0, 0), 7), l1 = min(max(c1 - st.ts1, 0), 7);
-      const int l2 = min(max(c2 - st.ts2, 0), 7);
-      key = ((l2 >> 1) << 6) | (l1 << 3) | l0;
-    } else {
-      key = (min(max(c1 - st.ts1 - kLMin, 0), 15) << 4) | min(max(c0 - st.ts0 - kLMin, 0), 15);
-    }
+    const int key = (min(max(c1 - st.ts1 - kLMin, 0), 15) << 4) | min(max(c0 - st.ts0 - kLMin, 0), 15);
     s.key[k] = key | (atomicAdd(s.cnt + key, 1) << 8);
   }
   __syncthreads();
@@ -546,163 +525,6 @@ __global__ void __launch_bounds__(kSpreadWarps * 32, 1) spread_rows_kernel(const
   }
 }
 
-// Plane-pair tasks with a column window sliding over the tile, for many channels and the ES
-// kernel (window corners l in [0, 8) per axis).  Stage 1 sorts the points by (axis-2 corner pair
-// s = l2 / 2, l1, l0).  A task is ROWS consecutive rows of two adjacent planes; lane (p, h, j)
-// owns, for plane 2 pp + p and the channels of half h, the cells of those rows in one column of
-// a window of W + 1 columns.  The task walks the corner pairs s = 0 .. 3 in order; for pair s
-// the window is columns [2 s, 2 s + W + 1) -- exactly the columns its points reach -- so a
-// point's values go to 2 (W + 1) column lanes of each half instead of all T columns, and to
-// both planes of the pair in one visit.  After pair s the two leftmost columns are final (no
-// later pair reaches them): they go to the grid, and every lane takes the sums of the lane two
-// columns to its right (a warp shuffle), the two new rightmost columns starting at zero.  The
-// summation (FP32 groups of kFoldRanges ranges, TwoSum folds with COMP) and the flush atomics
-// are those of spread_rows_kernel.
-template <int W, int CH, int ROWS, bool COMP>
-__global__ void __launch_bounds__(kSpreadWarps * 32, 1) spread_pairs_kernel(const SpreadParams a) {
-  constexpr int T = kBin + W - 1;
-  constexpr int WIN = W + 1;                 // columns of a corner pair's window
-  constexpr int NS = kBin / 2;               // corner pairs along axis 2
-  constexpr int NPP = (T + 1) / 2;           // plane pairs
-  constexpr int HS = (CH + 1) / 2 * 2;       // float2 per half of a point's values (even)
-  constexpr int PS = 2 * HS;                 // float2 of values per point
-  constexpr int RG = (T + ROWS - 1) / ROWS;  // row groups per plane
-  static_assert(4 * WIN <= 32, "two planes x two channel halves x W + 1 columns per warp");
-  using Rec = PointRec<W, ROWS>;
-  constexpr int F2 = Rec::F2;
-  extern __shared__ float4 smem4[];
-  float2 *s_val = reinterpret_cast<float2 *>(smem4);  // max_sub * PS
-  const StageSmem s = carve(s_val + a.max_sub * PS, a.max_sub, T, F2, sizeof(float));
-  const float *recs = static_cast<const float *>(s.rec);
-  const int sub = blockIdx.x;
-  if (sub >= *a.nsub) return;
-  const SubTile st = sub_tile(a, sub);
-  stage_subproblem<COV3D_KERNEL_ES, W, ROWS, float, true>(a, s, st);
-
-  const int tid = threadIdx.x, lane = tid & 31;
-  const bool lane_live = lane < 4 * WIN;
-  const int lv = lane_live ? lane : 0;
-  const int p2 = lv / (2 * WIN), hv = (lv / WIN) & 1, j = lv - (lv / WIN) * WIN;
-  for (int p0 = 0; p0 < a.nch; p0 += 2 * CH) {  // channel groups of 2 * CH
-    __syncthreads();
-    // this group's scaled channel values, in sorted order: half hh holds p0 + hh * CH + ch
-    for (int e = tid; e < st.cnt * 2 * CH; e += blockDim.x) {
-      const int slot = e / (2 * CH), r = e - slot * (2 * CH);
-      const int hh = r / CH, ch = r - hh * CH;
-      const float sc = s.sc[slot];
-      float2 v = make_float2(0.f, 0.f);
-      if (p0 + r < a.nch) {
-        const float2 x = __ldg(a.vals + (int64_t)s.pid[slot] * a.ips + (int64_t)(a.ch0 + p0 + r) * a.ics);
-        v = make_float2(x.x * sc, x.y * sc);
-      }
-      s_val[slot * PS + hh * HS + ch] = v;
-    }
-    if (tid == 0) *s.task = 0;
-    __syncthreads();
-
-    for (;;) {
-      int task = 0;
-      if (lane == 0) task = atomicAdd(s.task, 1);
-      task = __shfl_sync(0xffffffffu, task, 0);
-      if (task >= NPP * RG) break;
-      const int pp = task / RG;
-      const int rb = (task - pp * RG) * ROWS;  // first row of the task
-      const int pa0 = 2 * pp, pa = pa0 + p2;   // this lane's plane (pa == T: a zero plane weight)
-      const int b0lo = max(pa0 - W + 1, 0), b0hi = min(pa0 + 1, kBin - 1);
-      const int l1lo = max(rb - W + 1, 0), l1hi = min(rb + ROWS - 1, kBin - 1);
-      float2 hi[ROWS][CH], lo[ROWS][CH];  // cell sums and their TwoSum errors
-#pragma unroll
-      for (int q = 0; q < ROWS; ++q)
-#pragma unroll
-        for (int ch = 0; ch < CH; ++ch) hi[q][ch] = lo[q][ch] = make_float2(0.f, 0.f);
-      for (int sl = 0; sl < NS; ++sl) {
-        const float *w2c = recs + Rec::W2 + (lane_live ? 2 * sl + j : T);  // this lane's column weight
-        for (int l1g = l1hi; l1g >= l1lo; l1g -= kFoldRanges) {
-          float2 part[ROWS][CH];
-#pragma unroll
-          for (int q = 0; q < ROWS; ++q)
-#pragma unroll
-            for (int ch = 0; ch < CH; ++ch) part[q][ch] = make_float2(0.f, 0.f);
-          bool got = false;
-#pragma unroll
-          for (int sr = 0; sr < kFoldRanges; ++sr) {
-            const int l1 = l1g - sr;
-            if (l1 < l1lo) continue;
-            const int kb = (sl << 6) | (l1 << 3);
-            const int ibeg = s.off[kb | b0lo], iend = s.off[(kb | b0hi) + 1];
-            got |= ibeg < iend;
-            const int k1 = Rec::W1 + rb - l1;  // row rb + q reads the axis-1 weight k1 + q
-            for (int i = ibeg; i < iend; ++i) {
-              const float *rec = recs + i * F2;
-              const float w02 = rec[pa] * w2c[i * F2];
-              float2 w[ROWS];
-#pragma unroll
-              for (int q = 0; q < ROWS; ++q) {
-                const float wq = w02 * rec[k1 + q];
-                w[q] = make_float2(wq, wq);
-              }
-              const float2 *vp = s_val + i * PS + hv * HS;
-              float2 v[CH];
-#pragma unroll
-              for (int ch = 0; ch + 1 < CH; ch += 2) {
-                const float4 x = *reinterpret_cast<const float4 *>(vp + ch);
-                v[ch] = make_float2(x.x, x.y);
-                v[ch + 1] = make_float2(x.z, x.w);
-              }
-              if (CH & 1) v[CH - 1] = vp[CH - 1];
-#pragma unroll
-              for (int q = 0; q < ROWS; ++q)
-#pragma unroll
-                for (int ch = 0; ch < CH; ++ch) part[q][ch] = __ffma2_rn(w[q], v[ch], part[q][ch]);
-            }
-          }
-          if (!got) continue;
-#pragma unroll
-          for (int q = 0; q < ROWS; ++q)
-#pragma unroll
-            for (int ch = 0; ch < CH; ++ch) {
-              if (!COMP) hi[q][ch] = __fadd2_rn(hi[q][ch], part[q][ch]);
-              else two_sum2(hi[q][ch], lo[q][ch], part[q][ch]);
-            }
-        }
-        // the columns no later corner pair reaches go to the grid
-        const int col = 2 * sl + j;
-        if (lane_live && (sl == NS - 1 || j < 2) && pa < T) {
-          const int co = s.coloff[col];
-          if (co >= 0) {
-#pragma unroll
-            for (int q = 0; q < ROWS; ++q) {
-              if (rb + q >= T) break;
-              const long long ro = s.rowoff[pa * T + rb + q];
-              if (ro < 0) continue;
-              float2 *dst = a.grid + (ro + co) * a.cs + (int64_t)(a.ch0 + p0 + hv * CH) * a.chs;
-#pragma unroll
-              for (int ch = 0; ch < CH; ++ch) {
-                const float2 x = COMP ? __fadd2_rn(hi[q][ch], lo[q][ch]) : hi[q][ch];
-                if (p0 + hv * CH + ch < a.nch && (x.x != 0.0f || x.y != 0.0f)) atomicAdd(dst + ch * a.chs, x);
-              }
-            }
-          }
-        }
-        if (sl == NS - 1) break;
-        // slide the window two columns to the right
-        const bool keep = j + 2 < WIN;
-#pragma unroll
-        for (int q = 0; q < ROWS; ++q)
-#pragma unroll
-          for (int ch = 0; ch < CH; ++ch) {
-            const float2 h2 = make_float2(__shfl_down_sync(0xffffffffu, hi[q][ch].x, 2),
-                                          __shfl_down_sync(0xffffffffu, hi[q][ch].y, 2));
-            const float2 l2 = make_float2(__shfl_down_sync(0xffffffffu, lo[q][ch].x, 2),
-                                          __shfl_down_sync(0xffffffffu, lo[q][ch].y, 2));
-            hi[q][ch] = keep ? h2 : make_float2(0.f, 0.f);
-            lo[q][ch] = keep ? l2 : make_float2(0.f, 0.f);
-          }
-      }
-    }
-  }
-}
-
 constexpr int kRowGroupCH = 5;  // channels per lane half (row-group tasks)
 constexpr int kRows = 3;        // tile rows per lane (row-group tasks; 2 measured 12 % slower)
 
@@ -736,11 +558,6 @@ int launch_wc(SpreadParams a, int nchan, int64_t max_blocks, cudaStream_t st) {
     constexpr int PS = 2 * ((kRowGroupCH + 1) / 2 * 2);
     const size_t smem = (size_t)a.max_sub * PS * sizeof(float2) +
                         stage_bytes(a.max_sub, T, PointRec<W, kRows>::F2, sizeof(float));
-    if constexpr (KT == COV3D_KERNEL_ES && 4 * (W + 1) <= 32) {
-      if (!spread_pairs_disabled())
-        return launch_spread_kernel(spread_pairs_kernel<W, kRowGroupCH, kRows, COMP>, "spread_pairs_kernel", smem, a,
-                                    max_blocks, st);
-    }
     return launch_spread_kernel(spread_rows_kernel<KT, W, kRowGroupCH, kRows, COMP>, "spread_rows_kernel", smem, a,
                                 max_blocks, st);
   }

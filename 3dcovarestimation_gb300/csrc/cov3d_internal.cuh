@@ -127,6 +127,8 @@ struct cov3d_plan {
   cov3d::DevBuf cgw;           // mean / CG workspace (state, vectors, shell sums)
   cov3d::DevBuf xbf, gsum;     // BF16 Gram operands and real Gram sums
   cov3d::DevBuf ctfc;          // per-image CTF coefficients (CtfCoef) from CTF parameters
+  cov3d::DevBuf lsw;           // least-squares regulariser: X, K X (r n^3 complex each) and K (n^2)
+  void *blas = nullptr;        // cuBLAS handle of the least-squares regulariser (created on first use)
   cov3d::DevBuf fftw;          // twiddles exp(-2 pi i j / fftw_n) of the fused axis-0 CG transform
   int fftw_n = 0;
   double *h_acc = nullptr;     // pinned host mirror of acc (64 doubles)
@@ -232,6 +234,9 @@ int launch_ml_reg(cov3d_plan *p, const void *grid, void *ggrid, const float *fr,
                   double *cost_acc, int init);
 int launch_gc_volume(const cov3d_plan *p, float *out);
 int launch_zero(cov3d_plan *p, void *ptr, int64_t bytes);
+int launch_ls_reg(cov3d_plan *p, const void *grid, void *ggrid, const float *fr, int64_t fr_stride, int r, double s,
+                  double *cost_acc);
+void release_blas(cov3d_plan *p);
 
 // gram_solve.cu
 int launch_gram_bf16(cov3d_plan *p, cudaStream_t st, int B, int P, int r, const void *q, int64_t is, int64_t ps,

@@ -628,10 +628,6 @@ int covar_cost_grad(cov3d_plan *p, const cov3d_cost_args *a, double *h_cost, dou
     set_error("points for L=%d images must be set before the cost", p->L);
     return COV3D_ESTATE;
   }
-  if (a->objective != 0 && a->d_fourier_reg) {
-    set_error("the least-squares Fourier regulariser is evaluated by the caller");
-    return COV3D_EINVAL;
-  }
   if (!(a->noise_var > 0.0)) {
     set_error("noise_var must be positive");
     return COV3D_EINVAL;
@@ -670,6 +666,8 @@ int covar_cost_grad(cov3d_plan *p, const cov3d_cost_args *a, double *h_cost, dou
   const bool lines_inv = pruned && line_transforms_apply(p);
   const bool lines_fwd = lines_inv && p->n <= 256;
   const bool with_reg = a->d_fourier_reg && a->reg_scale != 0.0;
+  const bool ml_reg = with_reg && a->objective == 0;  // sum fr |G|^2: fused into the transforms
+  const bool ls_reg = with_reg && a->objective != 0;  // |X X^H|^2: GEMMs before the spread (ls_reg.cu)
   const int64_t fr_stride = a->fourier_reg_per_channel ? n3 : 0;
   const float *gcp = a->use_grid_correction ? p->gc1d.as<float>() : nullptr;
   cufftHandle fft = 0, fplanes = 0, faxis0 = 0;
@@ -686,7 +684,7 @@ int covar_cost_grad(cov3d_plan *p, const cov3d_cost_args *a, double *h_cost, dou
   if (lines_fwd) {
     PhaseScope ps(p, kPhaseFftFwd);
     COV3D_TRY(step_forward_lines(p, a->d_vectors, a->d_log_sqrt, gcp, r, p->fine2.as<float2>(), p->fine.as<float2>(),
-                                 with_reg ? a->d_fourier_reg : nullptr, fr_stride, a->reg_scale / (2.0 * a->noise_var),
+                                 ml_reg ? a->d_fourier_reg : nullptr, fr_stride, a->reg_scale / (2.0 * a->noise_var),
                                  acc + 1));
   } else {
     PhaseScope ps(p, kPhasePack);
@@ -740,10 +738,16 @@ int covar_cost_grad(cov3d_plan *p, const cov3d_cost_args *a, double *h_cost, dou
   }
   // 7'. the regulariser (value and gradient coef * fr * G) initialises the gradient grid, so the
   // spread adds onto it and no zeroing pass is needed; without one, the grid is zeroed
-  if (with_reg && !lines_fwd) {
+  if (ml_reg && !lines_fwd) {
     PhaseScope ps(p, kPhaseReg);
     COV3D_TRY(launch_ml_reg(p, p->fine.ptr, p->fine2.ptr, a->d_fourier_reg, fr_stride, r,
                             a->reg_scale / (2.0 * a->noise_var), acc + 1, 1));
+  }
+  if (ls_reg) {  // value and derivative, onto the gradient grid (zero after the line transforms)
+    PhaseScope ps(p, kPhaseReg);
+    if (!lines_fwd) COV3D_TRY(launch_zero(p, p->fine2.ptr, n3 * r * 8));
+    COV3D_TRY(launch_ls_reg(p, p->fine.ptr, p->fine2.ptr, a->d_fourier_reg, fr_stride, r, a->reg_scale / L4,
+                            acc + 1));
   }
   {
     PhaseScope ps(p, kPhaseSpread);

@@ -346,8 +346,9 @@ int cov3d_plan_destroy(cov3d_plan *p) {
   }
   DevBuf *bufs[] = {&p->gc1d, &p->pts, &p->rot, &p->bin_count, &p->bin_off, &p->sub_off, &p->pt_bin, &p->pt_rank,
                     &p->sorted, &p->sub_bin, &p->sub_first, &p->sub_count, &p->nsub, &p->fine, &p->fine2, &p->q,
-                    &p->small, &p->acc, &p->cgw, &p->xbf, &p->gsum, &p->fftw, &p->ctfc};
+                    &p->small, &p->acc, &p->cgw, &p->xbf, &p->gsum, &p->fftw, &p->ctfc, &p->lsw};
   for (DevBuf *b : bufs) release(*b);
+  release_blas(p);
   if (p->h_acc) cudaFreeHost(p->h_acc);
   if (p->ev_pool) {
     for (cudaEvent_t e : *p->ev_pool) cudaEventDestroy(e);

@@ -574,8 +574,10 @@ def run_gb300(args):
     # roofline of the dominant kernel (interp or spread), per step = per launch group
     M = B * L * L
     n3 = n**3
-    alg = {"interp": r * n3 * 8 + r * M * 8 + B * 9 * 4 + M * 4,
-           "spread": r * M * 8 + 2 * r * n3 * 8 + M * 4}
+    # grid, samples, rotations (36 B) and CTF parameters (32 B) per image: the CTF itself is
+    # evaluated in the kernels
+    alg = {"interp": r * n3 * 8 + r * M * 8 + B * (9 * 4 + 8 * 4),
+           "spread": r * M * 8 + 2 * r * n3 * 8 + B * (9 * 4 + 8 * 4)}
     dom = max(("interp", "spread"), key=lambda k: phases[k][0])
     dom_ms = phases[dom][0] / max(1, args.steps)
     peak, peak_kind = load_peaks()

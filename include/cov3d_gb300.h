@@ -203,8 +203,11 @@ typedef struct {
   const float *d_ctf;       /* (B, L^2) float32 or NULL */
   double noise_var;         /* Fourier-domain noise variance (dataset noise_var * L^2) */
   double reg_scale;         /* reg / N (covar_sgd.py:357) */
-  const float *d_fourier_reg; /* (n^3) float32 centered, or NULL (ML regulariser :1373-1376); one array
-                                 per eigenvolume, (r, n^3), with fourier_reg_per_channel */
+  const float *d_fourier_reg; /* (n^3) float32 centered, or NULL; one array per eigenvolume, (r, n^3),
+                                 with fourier_reg_per_channel.  ML: reg_scale sum fr |G|^2 / (2 noise_var)
+                                 (:1373-1376); LS: reg_scale |X X^H|_F^2 / L^4 with X the (n, r n^2)
+                                 reshape of sqrt(fr) G, as the reference reshapes it (:1308-1313; two
+                                 FP32 cuBLAS GEMMs over r n^2, workspace 2 r n^3 complex on first use) */
   int use_grid_correction;  /* divide by the kernel's deapodisation factors (init_grid_correction) */
   double *d_cost;           /* optional device scalar receiving the cost (no host sync needed) */
   int gram_bf16;            /* 1: per-image Gram contractions in BF16 on the tensor cores (FP32

@@ -48,8 +48,6 @@ def test_dropin_cost_matches_reference(pkg, dev, objective, with_reg):
 @pytest.mark.parametrize("objective", ["ml", "ls"])
 @pytest.mark.parametrize("with_reg", [False, True])
 def test_fused_step_matches_reference(pkg, dev, objective, with_reg):
-    if objective == "ls" and with_reg:
-        pytest.skip("the LS regulariser is evaluated outside the fused step")
     c = load_golden("cost_L10_r3.npz")
     L, r, us = int(c["L"]), int(c["r"]), int(c["us"])
     step = pkg.FusedCovarStep(L, r, "bilinear", us, device=dev)
@@ -66,6 +64,41 @@ def test_fused_step_matches_reference(pkg, dev, objective, with_reg):
     assert rel(val, c[tag + "_cost"]) < TOL_COST
     assert rel(gv, c[tag + "_grad_vectors"]) < TOL_GRAD
     assert rel(gl, c[tag + "_grad_logsqrt"]) < TOL_GRAD
+
+
+@pytest.mark.parametrize("per_channel", [False, True])
+def test_fused_ls_regulariser_matches_dropin(pkg, dev, per_channel):
+    """The least-squares cost with its Fourier regulariser (the |X X^H|^2 term of the
+    reshape to (n, r n^2), r = 5 not dividing n = 128) in the fused step (line transforms, GEMMs
+    before the spread) against the drop-in cost through torch autograd, with one regulariser
+    for all eigenvolumes or one each; reg_scale makes the regulariser as large as the data term."""
+    L, r, B = 64, 5, 8
+    n = 2 * L
+    g = torch.Generator(device=dev).manual_seed(5)
+    covar = pkg.Covar(L, r, upsampling_factor=2).to(dev)
+    covar.init_grid_correction("bilinear")
+    R = torch.linalg.qr(torch.randn((B, 3, 3), device=dev, generator=g))[0].contiguous()
+    imgs = torch.randn((B, L, L), device=dev, generator=g, dtype=torch.complex64) * 50
+    ctf = torch.rand((B, L, L), device=dev, generator=g) + 0.2
+    shape = (r, n, n, n) if per_channel else (n, n, n)
+    fr = torch.rand(shape, device=dev, generator=g) + 0.5
+    plan = pkg.NufftPlanDiscretized((L,) * 3, upsample_factor=2, mode="bilinear")
+    plan.setrot(R)
+    with torch.no_grad():
+        vols = covar.get_vectors_fourier_domain()
+        c0 = pkg.cost_fourier_domain(vols, imgs, plan, ctf, 300.0).item()
+        c1 = pkg.cost_fourier_domain(vols, imgs, plan, ctf, 300.0, reg_scale=1.0, fourier_reg=fr).item()
+    reg_scale = abs(c0) / abs(c1 - c0)
+    val = pkg.cost_fourier_domain(covar.get_vectors_fourier_domain(), imgs, plan, ctf, 300.0, reg_scale=reg_scale,
+                                  fourier_reg=fr)
+    val.backward()
+    step = pkg.FusedCovarStep(L, r, "bilinear", 2, device=dev)
+    step.set_rotations(R)
+    v2, gv, gl = step(covar.vectors.detach(), covar.log_sqrt_eigenvals.detach(), imgs.reshape(B, -1),
+                      ctf.reshape(B, -1), 300.0, reg_scale=reg_scale, fourier_reg=fr, objective=1, sync_cost=True)
+    assert rel(v2, val.item()) < 1e-5
+    assert rel(gv, covar.vectors.grad) < 1e-4
+    assert rel(gl, covar.log_sqrt_eigenvals.grad) < 1e-4
 
 
 # r = 10 takes the staged Gram and per-pixel W-pass kernels, r = 20 two channel groups of the

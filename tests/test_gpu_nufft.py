@@ -45,6 +45,27 @@ def test_discretized_plan_matches_reference(pkg, dev, path):
         assert rel(plan.execute_adjoint_unaggregated(sig), d["adj_unagg"]) < TOL_FP32
 
 
+@pytest.mark.parametrize("mode", ["bilinear", "nearest"])
+@pytest.mark.parametrize("C", [1, 3, 5, 7, 10, 16, 33, 40])
+def test_discretized_channel_passes_match_oracle(pkg, dev, mode, C):
+    """Interpolation and spreading with every channel-pass shape of the narrow windows
+    (several points per warp, tiles of 3, 4, 5, 8 and 16 channel pairs, two passes) against
+    the float64 grid_sample restatement; 40 images so block point counts are ragged."""
+    L, us, N = 12, 2, 40
+    n = L * us
+    rng = np.random.default_rng(100 + C)
+    q, _ = np.linalg.qr(rng.standard_normal((N, 3, 3)))
+    pts = np.ascontiguousarray(O.rotated_points(q, L, wrap=False))
+    grid = (rng.standard_normal((C, n, n, n)) + 1j * rng.standard_normal((C, n, n, n))).astype(np.complex64)
+    sig = (rng.standard_normal((C, N, L * L)) + 1j * rng.standard_normal((C, N, L * L))).astype(np.complex64)
+    plan = pkg.NufftPlanDiscretized((L,) * 3, upsample_factor=us, mode=mode)
+    plan.setpts(T(pts, dev, torch.float32))
+    got = plan._plan.interp(T(grid, dev))
+    assert rel(got.reshape(C, N, -1), O.interp_discretized(grid, pts, mode)) < TOL_FP32
+    back = plan._plan.spread(T(sig.reshape(C, -1), dev))
+    assert rel(back, O.spread_discretized(sig, pts, n, mode)) < TOL_FP32
+
+
 @pytest.mark.parametrize("width,tol", [(6, 5e-5), (7, 5e-6)])
 @pytest.mark.parametrize("L", [10, 15, 16])
 def test_es_nufft_matches_direct_sum(pkg, dev, width, tol, L):

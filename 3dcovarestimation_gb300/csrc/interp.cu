@@ -43,10 +43,11 @@ struct InterpCP {
 
 // One block per subproblem.  The block stages the bin's tile (bin + (W-1)-cell halo) of 2*CP
 // channels in shared memory as [cell][channel] complex, then each warp takes one point at a
-// time (32 / (W*CP) points for the narrow bilinear and nearest windows): lane (j, q) reads the two channels 2q, 2q+1 of tile[row][corner2 + j] for the W*W
-// window rows -- W*CP contiguous 16-byte values per row, no bank conflicts -- and accumulates
-// weight * value; the W partial sums of each pair are combined through shared memory and the
-// epilogue (Nyquist zeroing, CTF, scale) is applied.
+// time (32 / (W*CP) points for the narrow bilinear and nearest windows): lane (j, q) reads the
+// two channels 2q, 2q+1 of tile[row][corner2 + j] for the W*W window rows -- W*CP contiguous
+// 16-byte values per row, no bank conflicts -- and accumulates weight * value; the W partial
+// sums of each pair are combined through shared memory and the epilogue (Nyquist zeroing,
+// CTF, scale) is applied.
 template <int KT, int W, int CP>
 __global__ void __launch_bounds__(kInterpWarps * 32) interp_kernel(const InterpParams a) {
   constexpr int T = kBin + W - 1;
@@ -115,17 +116,28 @@ __global__ void __launch_bounds__(kInterpWarps * 32) interp_kernel(const InterpP
   }
   const float2 *gbase = a.grid + (int64_t)a.ch0 * a.chs;
   // asynchronous copies global -> shared (8 bytes each, zero-filled outside the grid / past the
-  // pass's channels), all in flight before one wait
-  for (int e = tid; e < CH * T * T * T; e += blockDim.x) {
-    const int c2 = e % T;
-    const int rowi = (e / T) % (T * T);
-    const int ch = e / (T * T * T);
-    const long long ro = s_rowoff[rowi];
-    const int co = s_coloff[c2];
-    const bool ok = ch < a.nch && ro >= 0 && co >= 0;
-    const float2 *src = ok ? gbase + ro + (int64_t)co * a.cs + (int64_t)ch * a.chs : gbase;
-    const unsigned dst = (unsigned)__cvta_generic_to_shared(tile + (rowi * T + c2) * CH + ch);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(dst), "l"(src), "r"(ok ? 8 : 0) : "memory");
+  // pass's channels), all in flight before one wait.  A warp copies RPW tile rows (channel,
+  // plane, row) at a time, lane (s, c2) cell c2 of its row s: the column offset is fixed per
+  // lane, and only the row index is decomposed per copy
+  {
+    constexpr int RPW = 32 / T;
+    const int lane = tid & 31, s = lane / T, c2 = lane - (lane / T) * T;
+    if (s < RPW) {
+      const int co = s_coloff[c2];
+      const int64_t co_cs = co >= 0 ? (int64_t)co * a.cs : 0;
+      const float2 *src0 = gbase + co_cs;
+      const unsigned dst0 = (unsigned)__cvta_generic_to_shared(tile + c2 * CH);
+      const int step = (int)(blockDim.x >> 5) * RPW;
+      for (int row = (tid >> 5) * RPW + s; row < CH * T * T; row += step) {
+        const int ch = row / (T * T);
+        const int rowi = row - ch * (T * T);
+        const long long ro = s_rowoff[rowi];
+        const bool ok = ch < a.nch && ro >= 0 && co >= 0;
+        const float2 *src = ok ? src0 + ro + (int64_t)ch * a.chs : gbase;
+        const unsigned dst = dst0 + (unsigned)((rowi * T * CH + ch) * sizeof(float2));
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(dst), "l"(src), "r"(ok ? 8 : 0) : "memory");
+      }
+    }
   }
   asm volatile("cp.async.commit_group;\n" ::: "memory");
   asm volatile("cp.async.wait_group 0;\n" ::: "memory");

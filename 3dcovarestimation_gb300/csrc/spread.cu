@@ -544,8 +544,9 @@ int launch_spread_kernel(Kernel kernel, const char *name, size_t smem, const Spr
 }
 
 // One launch for all channels: the block sorts and stages its points once.  With three or more
-// channel pairs, row-group tasks over two lane halves of kRowGroupCH channels (groups of
-// 2 * kRowGroupCH channels); otherwise row tasks with the (at most two, G >= 2) pairs spread
+// channel pairs, narrow windows (W <= 2) take row tasks with two channel pairs per lane group
+// and wider ones take row-group tasks over two lane halves of kRowGroupCH channels (groups of
+// 2 * kRowGroupCH channels), otherwise row tasks with the (at most two, G >= 2) pairs spread
 // over the lane groups.
 template <int KT, int W, bool COMP>
 int launch_wc(SpreadParams a, int nchan, int64_t max_blocks, cudaStream_t st) {
@@ -554,6 +555,18 @@ int launch_wc(SpreadParams a, int nchan, int64_t max_blocks, cudaStream_t st) {
   a.ch0 = 0;
   a.nch = nchan;
   const int npairs = (nchan + 1) / 2;
+  if constexpr (W <= 2) {
+    // narrow windows: one-row tasks with two pairs per lane group (G * 2 pairs per channel group),
+    // small registers and shared memory, two blocks per SM; the row-group kernel's three-row
+    // tasks multiply by zero for all but two of a lane's columns (bilinear step: 4.6 against
+    // 7.4 ms)
+    if (npairs >= 3) {
+      constexpr int CPL = 2;
+      const size_t smem = (size_t)a.max_sub * G * CPL * sizeof(float4) +
+                          stage_bytes(a.max_sub, T, PointRec<W, 1>::F2, sizeof(float2));
+      return launch_spread_kernel(spread_kernel<KT, W, CPL, COMP>, "spread_kernel", smem, a, max_blocks, st);
+    }
+  }
   if (npairs >= 3) {
     constexpr int PS = 2 * ((kRowGroupCH + 1) / 2 * 2);
     const size_t smem = (size_t)a.max_sub * PS * sizeof(float2) +

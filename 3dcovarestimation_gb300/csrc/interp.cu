@@ -211,6 +211,29 @@ __global__ void __launch_bounds__(kInterpWarps * 32) interp_kernel(const InterpP
         a23 = __ffma2_rn(ww0, p23, a23);
       }
     }
+#ifdef COV3D_EXP_SHFLRED
+    // the W partial sums of each pair by a shuffle tree over the window cells j (lanes j*CP + q
+    // of the slot): at each level cell j adds cell j + h, h = ceil(width / 2)
+    float4 s = make_float4(a01.x, a01.y, a23.x, a23.y);
+#pragma unroll
+    for (int lvl = 0; lvl < 3; ++lvl) {
+      const int wc = lvl == 0 ? W : lvl == 1 ? (W + 1) / 2 : ((W + 1) / 2 + 1) / 2;
+      if (wc <= 1) break;
+      const int h = (wc + 1) / 2;
+      float4 t;
+      t.x = __shfl_down_sync(0xffffffffu, s.x, h * CP);
+      t.y = __shfl_down_sync(0xffffffffu, s.y, h * CP);
+      t.z = __shfl_down_sync(0xffffffffu, s.z, h * CP);
+      t.w = __shfl_down_sync(0xffffffffu, s.w, h * CP);
+      if (j + h < wc) {
+        s.x += t.x;
+        s.y += t.y;
+        s.z += t.z;
+        s.w += t.w;
+      }
+    }
+    if (pt_ok && sl < CP) {
+#else
     wred[lane] = make_float4(a01.x, a01.y, a23.x, a23.y);
     __syncwarp();
     if (pt_ok && sl < CP) {
@@ -223,6 +246,7 @@ __global__ void __launch_bounds__(kInterpWarps * 32) interp_kernel(const InterpP
         s.z += x.z;
         s.w += x.w;
       }
+#endif
       // epilogue: vol_forward's Nyquist zeroing, CTF multiply and 1/L (projection_funcs.py:355-370)
       const int64_t id = sp_id(sp.idf);
       const float sc = s_sc[k];
@@ -230,7 +254,9 @@ __global__ void __launch_bounds__(kInterpWarps * 32) interp_kernel(const InterpP
       if (2 * sl < a.nch) o[0] = make_float2(s.x * sc, s.y * sc);
       if (2 * sl + 1 < a.nch) o[a.ocs] = make_float2(s.z * sc, s.w * sc);
     }
+#ifndef COV3D_EXP_SHFLRED
     __syncwarp();
+#endif
   }
 }
 

@@ -10,6 +10,11 @@ namespace {
 
 constexpr int kBin = 8;
 constexpr int kSpreadWarps = 16;
+// Row-group kernel: two blocks of 8 warps per SM (125 registers), so one block's staging
+// (sort, records, values) overlaps the other's tasks; one block of 16 warps measured 20.1
+// against 18.0 ms at the cov-SGD workload
+constexpr int kRowsWarps = 8;
+constexpr int kRowsBlocks = 2;
 
 struct SpreadParams {
   PointGeom g;
@@ -402,7 +407,7 @@ __global__ void __launch_bounds__(kSpreadWarps * 32, W < 8 ? 2 : 1) spread_kerne
 // groups of kFoldRanges ranges, TwoSum folds with COMP) and the atomics are those of
 // spread_kernel.
 template <int KT, int W, int CH, int ROWS, bool COMP>
-__global__ void __launch_bounds__(kSpreadWarps * 32, 1) spread_rows_kernel(const SpreadParams a) {
+__global__ void __launch_bounds__(kRowsWarps * 32, kRowsBlocks) spread_rows_kernel(const SpreadParams a) {
   constexpr int T = kBin + W - 1;
   static_assert(2 * T <= 32, "two lane halves of T columns per warp");
   constexpr int HS = (CH + 1) / 2 * 2;       // float2 per half of a point's values (even)
@@ -530,7 +535,7 @@ constexpr int kRows = 3;        // tile rows per lane (row-group tasks; 2 measur
 
 template <typename Kernel>
 int launch_spread_kernel(Kernel kernel, const char *name, size_t smem, const SpreadParams &a, int64_t max_blocks,
-                         cudaStream_t st) {
+                         cudaStream_t st, int warps = kSpreadWarps) {
   if (smem > 227 * 1024) {
     set_error("spreading stage of %zu bytes exceeds shared memory", smem);
     return COV3D_EINVAL;
@@ -539,7 +544,7 @@ int launch_spread_kernel(Kernel kernel, const char *name, size_t smem, const Spr
     cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return check_cuda(e, "cudaFuncSetAttribute(spread)");
   }
-  kernel<<<(unsigned)max_blocks, kSpreadWarps * 32, smem, st>>>(a);
+  kernel<<<(unsigned)max_blocks, warps * 32, smem, st>>>(a);
   return launched(name);
 }
 
@@ -567,12 +572,14 @@ int launch_wc(SpreadParams a, int nchan, int64_t max_blocks, cudaStream_t st) {
       return launch_spread_kernel(spread_kernel<KT, W, CPL, COMP>, "spread_kernel", smem, a, max_blocks, st);
     }
   }
-  if (npairs >= 3) {
-    constexpr int PS = 2 * ((kRowGroupCH + 1) / 2 * 2);
-    const size_t smem = (size_t)a.max_sub * PS * sizeof(float2) +
-                        stage_bytes(a.max_sub, T, PointRec<W, kRows>::F2, sizeof(float));
-    return launch_spread_kernel(spread_rows_kernel<KT, W, kRowGroupCH, kRows, COMP>, "spread_rows_kernel", smem, a,
-                                max_blocks, st);
+  if constexpr (W > 2) {
+    if (npairs >= 3) {
+      constexpr int PS = 2 * ((kRowGroupCH + 1) / 2 * 2);
+      const size_t smem = (size_t)a.max_sub * PS * sizeof(float2) +
+                          stage_bytes(a.max_sub, T, PointRec<W, kRows>::F2, sizeof(float));
+      return launch_spread_kernel(spread_rows_kernel<KT, W, kRowGroupCH, kRows, COMP>, "spread_rows_kernel", smem,
+                                  a, max_blocks, st, kRowsWarps);
+    }
   }
   static_assert(2 * G >= 2, "at most two channel pairs spread over the lane groups");
   const size_t smem =

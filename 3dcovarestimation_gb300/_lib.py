@@ -64,6 +64,7 @@ _SIGNATURES = {
     "cov3d_spread_unaggregated": (c_int, [c_void_p, c_void_p, c_int64, c_void_p, c_int, c_float, c_void_p]),
     "cov3d_execute_type2": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
     "cov3d_execute_type1": (c_int, [c_void_p, c_void_p, c_int, c_void_p]),
+    "cov3d_fine_grid": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
     "cov3d_project": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_int64, c_int64, c_void_p, c_int,
                               c_float]),
     "cov3d_backproject": (c_int, [c_void_p, c_void_p, c_int64, c_int64, c_int, c_void_p, c_int, c_float, c_void_p]),

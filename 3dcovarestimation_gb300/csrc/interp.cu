@@ -46,7 +46,7 @@ struct InterpCP {
 // time (32 / (W*CP) points for the narrow bilinear and nearest windows): lane (j, q) reads the
 // two channels 2q, 2q+1 of tile[row][corner2 + j] for the W*W window rows -- W*CP contiguous
 // 16-byte values per row, no bank conflicts -- and accumulates weight * value; the W partial
-// sums of each pair are combined through shared memory and the epilogue (Nyquist zeroing,
+// sums of each pair are combined by a warp-shuffle tree and the epilogue (Nyquist zeroing,
 // CTF, scale) is applied.
 template <int KT, int W, int CP>
 __global__ void __launch_bounds__(kInterpWarps * 32) interp_kernel(const InterpParams a) {
@@ -56,10 +56,9 @@ __global__ void __launch_bounds__(kInterpWarps * 32) interp_kernel(const InterpP
   // points per warp iteration: several when a point's W*CP lanes (and its 3W weights) fit more
   // than once into the warp, as for the bilinear and nearest kernels
   constexpr int PPW = (LANES >= 3 * W && 32 / LANES > 1) ? 32 / LANES : 1;
-  extern __shared__ float4 tile4[];  // T^3 * CP float4 (= 2 complex), then kInterpWarps * 32 float4
+  extern __shared__ float4 tile4[];  // T^3 * CP float4 (= 2 complex), then the point records
   float2 *tile = reinterpret_cast<float2 *>(tile4);
-  float4 *red = tile4 + T * T * T * CP;
-  SortedPoint *s_sp = reinterpret_cast<SortedPoint *>(red + kInterpWarps * 32);  // max_sub
+  SortedPoint *s_sp = reinterpret_cast<SortedPoint *>(tile4 + T * T * T * CP);  // max_sub
   float *s_sc = reinterpret_cast<float *>(s_sp + a.max_sub);                     // epilogue factor
   const int sub = blockIdx.x;
   if (sub >= *a.nsub) return;
@@ -149,7 +148,6 @@ __global__ void __launch_bounds__(kInterpWarps * 32) interp_kernel(const InterpP
   const int j = sl / CP, q = sl - (sl / CP) * CP;
   const int lane0 = (pp < PPW ? pp : 0) * LANES;  // first lane of this lane's point slot
   const int wl = PPW == 1 ? lane : sl;             // this lane's tap among the point's 3W weights
-  float4 *wred = red + warp * 32;
   for (int k0 = warp * PPW; k0 < cnt; k0 += kInterpWarps * PPW) {
     const int k = k0 + pp;
     const bool pt_ok = pp < PPW && k < cnt;
@@ -211,7 +209,6 @@ __global__ void __launch_bounds__(kInterpWarps * 32) interp_kernel(const InterpP
         a23 = __ffma2_rn(ww0, p23, a23);
       }
     }
-#ifdef COV3D_EXP_SHFLRED
     // the W partial sums of each pair by a shuffle tree over the window cells j (lanes j*CP + q
     // of the slot): at each level cell j adds cell j + h, h = ceil(width / 2)
     float4 s = make_float4(a01.x, a01.y, a23.x, a23.y);
@@ -233,20 +230,6 @@ __global__ void __launch_bounds__(kInterpWarps * 32) interp_kernel(const InterpP
       }
     }
     if (pt_ok && sl < CP) {
-#else
-    wred[lane] = make_float4(a01.x, a01.y, a23.x, a23.y);
-    __syncwarp();
-    if (pt_ok && sl < CP) {
-      float4 s = wred[lane];
-#pragma unroll
-      for (int r = 1; r < W; ++r) {
-        const float4 x = wred[lane + r * CP];
-        s.x += x.x;
-        s.y += x.y;
-        s.z += x.z;
-        s.w += x.w;
-      }
-#endif
       // epilogue: vol_forward's Nyquist zeroing, CTF multiply and 1/L (projection_funcs.py:355-370)
       const int64_t id = sp_id(sp.idf);
       const float sc = s_sc[k];
@@ -254,9 +237,6 @@ __global__ void __launch_bounds__(kInterpWarps * 32) interp_kernel(const InterpP
       if (2 * sl < a.nch) o[0] = make_float2(s.x * sc, s.y * sc);
       if (2 * sl + 1 < a.nch) o[a.ocs] = make_float2(s.z * sc, s.w * sc);
     }
-#ifndef COV3D_EXP_SHFLRED
-    __syncwarp();
-#endif
   }
 }
 
@@ -274,7 +254,7 @@ template <int KT, int W, int CP>
 int launch_cp(const InterpParams &a, int64_t max_blocks, cudaStream_t st) {
   constexpr int T = kBin + W - 1;
   const size_t smem =
-      ((size_t)T * T * T * CP + kInterpWarps * 32) * sizeof(float4) + (size_t)a.max_sub * (sizeof(SortedPoint) + 4);
+      (size_t)T * T * T * CP * sizeof(float4) + (size_t)a.max_sub * (sizeof(SortedPoint) + 4);
   if (smem > 32 * 1024) {  // static shared arrays come on top of the dynamic size
     cudaError_t e = cudaFuncSetAttribute(interp_kernel<KT, W, CP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);

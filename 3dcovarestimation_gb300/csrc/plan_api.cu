@@ -508,6 +508,19 @@ static int type2(cov3d_plan *p, const float *d_vol_real, const void *d_vol_compl
   return launch_interp(p, g, nchan, d_out, ops, ocs, e);
 }
 
+int cov3d_fine_grid(cov3d_plan *p, const float *d_vol_real, const void *d_vol_complex, int nchan, void *d_grid) {
+  if (!valid(p) || (!d_vol_real && !d_vol_complex) || !d_grid || nchan < 1 || nchan > p->n_trans) {
+    set_error("invalid fine-grid arguments (nchan must be in 1..n_trans)");
+    return COV3D_EINVAL;
+  }
+  COV3D_TRY(launch_pack(p, d_vol_real, d_vol_complex, nullptr, 1, nchan, d_grid));
+  cufftHandle fft;
+  COV3D_TRY(get_fft(p, nchan, &fft));
+  return check_cufft(cufftExecC2C(fft, static_cast<cufftComplex *>(d_grid), static_cast<cufftComplex *>(d_grid),
+                                  CUFFT_FORWARD),
+                     "cufftExecC2C(forward)");
+}
+
 int cov3d_execute_type2(cov3d_plan *p, const float *d_vol_real, const void *d_vol_complex, int nchan, void *d_out) {
   EpilogueArgs e{nullptr, 0, 1.0f};
   return type2(p, d_vol_real, d_vol_complex, nchan, d_out, 1, p ? p->n_points : 0, e);

@@ -196,6 +196,32 @@ class _Plan:
                           _lib.ptr(ctf_t), fl, float(scale))
         return out
 
+    def fine_grid(self, vol):
+        """Deapodised, zero-padded FFT of (C, L, L, L) volumes (cov3d_fine_grid): (C, n, n, n)
+        complex64 in FFT-native order, for :meth:`interp_native` over many batches of points."""
+        C = vol.shape[0]
+        grid = torch.empty((C, self.n, self.n, self.n), dtype=torch.complex64, device=self.device)
+        with torch.cuda.device(self.device):
+            if vol.is_complex():
+                v = vol.to(torch.complex64).contiguous()
+                _lib.call("cov3d_fine_grid", self.bind(), None, _lib.ptr(v), C, _lib.ptr(grid))
+            else:
+                v = vol.to(torch.float32).contiguous()
+                _lib.call("cov3d_fine_grid", self.bind(), _lib.ptr(v), None, C, _lib.ptr(grid))
+        return grid
+
+    def interp_native(self, grid, ctf=None, flags=0, scale=1.0):
+        """Interpolation of a :meth:`fine_grid` result with the projection epilogue, written
+        point-major: returns (n_points, C) complex64."""
+        C = grid.shape[0]
+        out = torch.empty((self.n_points, C), dtype=torch.complex64, device=self.device)
+        layout = _lib.GridLayout(order=_lib.GRID_FFT_NATIVE, cell_stride=1, chan_stride=self.n**3)
+        ctf_t = None if ctf is None else ctf.detach().to(device=self.device, dtype=torch.float32).contiguous()
+        with torch.cuda.device(self.device):
+            _lib.call("cov3d_interp", self.bind(), _lib.ptr(grid), _lib.ctypes.byref(layout), C, _lib.ptr(out), C, 1,
+                      _lib.ptr(ctf_t), flags | (_lib.APPLY_CTF if ctf_t is not None else 0), float(scale))
+        return out
+
     def backproject(self, values, ctf=None, flags=0, scale=1.0):
         """Type 1 with im_backward's prologue fused (cov3d_backproject): (C, n_points) -> (C, L, L, L)."""
         C = values.shape[0]

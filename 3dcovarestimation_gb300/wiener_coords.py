@@ -14,7 +14,7 @@ import torch
 
 from . import _lib
 from .nufft_plan import NufftPlan, NufftPlanDiscretized
-from .projection_funcs import _set_pose, centered_fft3, vol_forward
+from .projection_funcs import _set_pose, centered_fft3, centered_ifft2, vol_forward
 
 
 def compute_latentMAP_batch(images: torch.Tensor, eigen_forward: torch.Tensor, noise_var: float,
@@ -103,6 +103,28 @@ def wiener_coords(dataset, eigenvecs: torch.Tensor, eigenvals: torch.Tensor, bat
     return (coords, fwd) if return_eigen_forward else coords
 
 
+class _EigenProjector:
+    """Projections of fixed eigenvolumes on an exact plan for many batches of poses, as
+    ``vol_forward`` gives them (Nyquist zeroing, CTF, 1/L): the fine grid is transformed once
+    (``cov3d_fine_grid``) and each batch only interpolates it (``cov3d_interp``), written
+    point-major so the Gram contractions read it directly."""
+
+    def __init__(self, plan: NufftPlan, vols: torch.Tensor):
+        self.plan, self.vols, self.grid = plan, vols, None
+
+    def __call__(self, filters: Optional[torch.Tensor], fourier_domain: bool = False) -> torch.Tensor:
+        """(n, r, L, L) projections of the current batch, Fourier domain (point-major storage) or,
+        like ``vol_forward``'s default, the real part of their centered inverse 2D FFT."""
+        p = self.plan._plan
+        if self.grid is None:
+            self.grid = p.fine_grid(self.vols)
+        L = self.vols.shape[-1]
+        ctf = None if filters is None else filters.reshape(p.n_images, -1)
+        out = p.interp_native(self.grid, ctf, _lib.APPLY_NYQUIST, 1.0 / L)
+        q = out.view(p.n_images, L * L, -1).permute(0, 2, 1).reshape(p.n_images, -1, L, L)
+        return q if fourier_domain else centered_ifft2(q).real
+
+
 def latentMAP(dataset, eigenvecs: torch.Tensor, eigenvals: torch.Tensor, batch_size: int = 1024,
               start_ind: Optional[int] = None, end_ind: Optional[int] = None, return_coords_covar: bool = False,
               nufft_plan: type = NufftPlan, **nufft_plan_kwargs: Any):
@@ -128,13 +150,17 @@ def latentMAP(dataset, eigenvecs: torch.Tensor, eigenvals: torch.Tensor, batch_s
     count = end_ind - start_ind
     coords = torch.zeros((count, rank), device=device)
     covar_inv = torch.zeros((count, rank, rank), dtype=dtype) if return_coords_covar else None
+    project = _EigenProjector(plan, vols) if nufft_plan == NufftPlan else None
     for i in range(0, count, batch_size):
         images, pts_rot, filters, _ = dataset[start_ind + i: min(start_ind + i + batch_size, end_ind)]
         images, pts_rot, filters = images.to(device), pts_rot.to(device), filters.to(device)
         _set_pose(plan, pts_rot)
-        eig_fwd = vol_forward(vols, plan, filters)
-        if eig_fwd.ndim == 3:
-            eig_fwd = eig_fwd.unsqueeze(0)
+        if project is not None:  # the eigenvolumes are transformed once, not per batch
+            eig_fwd = project(filters)
+        else:
+            eig_fwd = vol_forward(vols, plan, filters)
+            if eig_fwd.ndim == 3:
+                eig_fwd = eig_fwd.unsqueeze(0)
         z, m, _ = compute_latentMAP_batch(images, eig_fwd, dataset.noise_var, eigenvals_inv)
         coords[i: i + batch_size] = z.squeeze(-1).real.to(coords.dtype)
         if return_coords_covar:

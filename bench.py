@@ -74,6 +74,8 @@ def parse():
     ap.add_argument("--no-bf16", action="store_true", help="skip the BF16-Gram variant of the step")
     ap.add_argument("--no-wiener", action="store_true", help="skip the Wiener-coordinate measurement")
     ap.add_argument("--no-bilinear", action="store_true", help="skip the bilinear-interpolation step")
+    ap.add_argument("--ragged-L", type=int, default=256, help="volume size of the ragged Wiener measurement")
+    ap.add_argument("--no-ragged", action="store_true", help="skip the ragged-batch Wiener measurement")
     return ap.parse_args()
 
 
@@ -234,6 +236,55 @@ def make_dataset(pkg, args, dev, n_images):
     noise_var = signal_var / 0.05
     images += torch.randn(images.shape, generator=g, device=dev, dtype=torch.complex64) * (noise_var ** 0.5)
     return images, rot, prm, noise_var
+
+
+def run_wiener_ragged(pkg, args, dev):
+    """Wiener / latent-MAP coordinates at the full-pipeline size: L = args.ragged_L, r = 10,
+    batches of 256 .. 4096 images in a fixed ragged sequence over a resident pool of 4096
+    Fourier-domain images (the solve's cost does not depend on the image values), uniform
+    SO(3) poses, CTF from per-image parameters, the eigenvolumes' fine grid transformed once.
+    Returns images/s over the sequence (CUDA events)."""
+    import torch
+
+    from importlib import import_module
+
+    syn = import_module("3dcovarestimation_gb300.synthetic")
+    wc = import_module("3dcovarestimation_gb300.wiener_coords")
+    L, r = args.ragged_L, 10
+    g = torch.Generator(device=dev).manual_seed(args.seed + 5)
+    eig = syn.gaussian_blob_volumes(r, L, generator=g, device=dev)
+    eig = syn.orthonormalize(eig.reshape(r, -1)).reshape(r, L, L, L)
+    lam = torch.linspace(4.0, 0.5, r, device=dev, dtype=torch.float64)
+    linv = torch.diag(1.0 / lam)
+    pool = 4096
+    images = torch.randn((pool, L, L), device=dev, generator=g, dtype=torch.complex64) * 10
+    rot = syn.uniform_rotations(pool, generator=g, device=dev)
+    df = torch.rand((pool,), device=dev, generator=g) * 2 + 1
+    prm = syn.ctf_params(df, 1.0, device=dev)
+    sizes = [256, 1000, 4096, 3000, 512, 2048, 1500, 4096, 768, 3500]
+    plan = pkg.NufftPlan((L,) * 3, batch_size=r, device=dev, width=args.width)
+    project = wc._EigenProjector(plan, eig)
+
+    def batch(nimg, off):
+        idx = slice(off, off + nimg)
+        plan.setrot(rot[idx])
+        q = project(syn.ctf_from_params(prm[idx], L), fourier_domain=True)
+        return wc.compute_latentMAP_batch(images[idx], q, 1.0e4, linv)[0]
+
+    batch(sizes[0], 0)  # warm-up: plan, fine grid, kernels
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    total = 0
+    for k, nimg in enumerate(sizes):
+        batch(nimg, (k * 331) % (pool - nimg + 1))
+        total += nimg
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    return {"images_per_s": total / (ms / 1e3), "images": total, "L": L, "rank": r, "batch_sizes": sizes,
+            "note": "ragged batches of 256..4096 images (full-pipeline configuration's sizes, L=256): ES "
+                    "interpolation of the eigenvolumes' fine grid, FP32 Gram, FP64 Cholesky per image"}
 
 
 def run_mean_cg(pkg, args, dev):
@@ -545,10 +596,11 @@ def run_gb300(args):
         lam = torch.exp(2 * covar.log_sqrt_eigenvals.detach()).to(torch.float64)
         linv = torch.diag(1.0 / (lam + 1e-6))
         wplan = pkg.NufftPlan((L,) * 3, batch_size=r, device=dev, width=args.width)
+        project = wc._EigenProjector(wplan, eigv)  # as latentMAP: the eigenvolumes' grid once
 
         def wbatch(b):
             wplan.setrot(rot[b])
-            q = pkg.vol_forward(eigv, wplan, syn.ctf_from_params(prm[b], L), fourier_domain=True)
+            q = project(syn.ctf_from_params(prm[b], L), fourier_domain=True)
             return wc.compute_latentMAP_batch(images[b], q, noise_var, linv)[0]
 
         wbatch(0)
@@ -561,8 +613,9 @@ def run_gb300(args):
         barrier()
         wms = w0.elapsed_time(w1)
         wiener = {"images_per_s": nb * B / (wms / 1e3), "images": nb * B, "batch": B,
-                  "note": "per batch: ES type-2 projections of the r eigenvolumes with CTF, FP32 Gram, FP64 "
-                          "Cholesky solve per image (Fourier-domain images)"}
+                  "note": "per batch: ES interpolation of the r eigenvolumes' fine grid (transformed once, as "
+                          "latentMAP does) with CTF, FP32 Gram, FP64 Cholesky solve per image (Fourier-domain "
+                          "images)"}
 
     if rank != 0:
         if world > 1:
@@ -608,6 +661,8 @@ def run_gb300(args):
         line["bf16_gram"] = bf16
     if wiener is not None:
         line["wiener_coords"] = wiener
+    if not args.no_wiener and not args.no_ragged:
+        line["wiener_ragged"] = run_wiener_ragged(pkg, args, dev)
     if not args.no_mean:
         line["mean_cg"] = run_mean_cg(pkg, args, dev)
     if bilinear is not None:

@@ -175,6 +175,13 @@ int cov3d_ctf_images(void *stream, const float *d_params, int64_t n_images, int 
 int cov3d_project(cov3d_plan *plan, const float *d_vol_real, const void *d_vol_complex, int nchan, void *d_out,
                   int64_t out_point_stride, int64_t out_chan_stride, const float *d_ctf, int flags, float scale);
 
+/* The first half of cov3d_execute_type2 alone: deapodise + zero-pad + FFT of nchan volumes into
+ * the caller's (nchan, n^3) complex64 buffer in FFT-native order (cov3d_grid_layout
+ * {COV3D_GRID_FFT_NATIVE, 1, n^3}), so that a loop over batches of points with fixed volumes
+ * transforms them once and calls cov3d_interp per batch; the reference's latentMAP re-executes
+ * its plan on the same eigenvolumes for every batch (wiener_coords.py:131-139). */
+int cov3d_fine_grid(cov3d_plan *plan, const float *d_vol_real, const void *d_vol_complex, int nchan, void *d_grid);
+
 /* Its exact adjoint: cov3d_execute_type1 with im_backward's prologue fused into the spreading
  * (projection_funcs.py:373-399); (point, channel) input at d_values[point*in_point_stride +
  * ch*in_chan_stride], (nchan, L^3) complex64 output. */

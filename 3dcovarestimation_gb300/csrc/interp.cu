@@ -16,6 +16,7 @@ struct InterpParams {
   const int *sub_bin;
   const int *sub_first;
   const int *sub_count;
+  const int *bin_off;  // first sorted point of each bin (exclusive scan of the bin counts)
   const int *nsub;
   const float2 *grid;
   int64_t cs, chs;
@@ -64,7 +65,15 @@ __global__ void __launch_bounds__(kInterpWarps * 32) interp_kernel(const InterpP
   if (sub >= *a.nsub) return;
   const int bin = a.sub_bin[sub];
   const int first = a.sub_first[sub];
-  const int cnt = a.sub_count[sub];
+#ifdef COV3D_EXP_BINBLOCK
+  // one block per bin: the block of the bin's first subproblem takes all of the bin's points,
+  // max_sub at a time, so the tile is staged once per bin
+  if (first != a.bin_off[bin]) return;
+  const int last = a.bin_off[bin + 1];
+#else
+  const int last = first + a.sub_count[sub];
+#endif
+  int cnt = min(a.max_sub, last - first);
   const int nb12 = a.bins.nb[1] * a.bins.nb[2];
   const int ts0 = (bin / nb12) * kBin;
   const int ts1 = ((bin / a.bins.nb[2]) % a.bins.nb[1]) * kBin;
@@ -148,95 +157,109 @@ __global__ void __launch_bounds__(kInterpWarps * 32) interp_kernel(const InterpP
   const int j = sl / CP, q = sl - (sl / CP) * CP;
   const int lane0 = (pp < PPW ? pp : 0) * LANES;  // first lane of this lane's point slot
   const int wl = PPW == 1 ? lane : sl;             // this lane's tap among the point's 3W weights
-  for (int k0 = warp * PPW; k0 < cnt; k0 += kInterpWarps * PPW) {
-    const int k = k0 + pp;
-    const bool pt_ok = pp < PPW && k < cnt;
-    const SortedPoint sp = s_sp[pt_ok ? k : k0];
-    int c0[3];
-    c0[0] = first_cell<KT, W>(sp.t0);
-    c0[1] = first_cell<KT, W>(sp.t1);
-    c0[2] = first_cell<KT, W>(sp.t2);
-    // one kernel weight per lane wl < 3W, then shared through the warp
-    float myw = 0.0f;
-    if (wl < 3 * W) {
-      const int d = wl / W, tq = wl - (wl / W) * W;
-      const float td = d == 0 ? sp.t0 : d == 1 ? sp.t1 : sp.t2;
-      myw = tap_weight<KT, W>(td, tq, a.k.beta);
-    }
-    float w0[W], w1[W];
-#pragma unroll
-    for (int r = 0; r < W; ++r) {
-      w0[r] = __shfl_sync(0xffffffffu, myw, lane0 + r);
-      w1[r] = __shfl_sync(0xffffffffu, myw, lane0 + W + r);
-    }
-    const float wj = __shfl_sync(0xffffffffu, myw, lane0 + 2 * W + (j < W ? j : 0));
-    int l0 = c0[0], l1 = c0[1], l2 = c0[2];
-    if (KT == COV3D_KERNEL_ES) {
-      l0 = wrap1(l0, n);
-      l1 = wrap1(l1, n);
-      l2 = wrap1(l2, n);
-    }
-    l0 -= ts0;
-    l1 -= ts1;
-    l2 -= ts2;
-    const int cell2 = l2 + j;
-    const bool lane_ok = pt_ok && cell2 >= 0;
-    const float4 *base = tile4 + cell2 * CP + q;
-    // two packed FP32 accumulators (FFMA2: one instruction per channel pair of values; the
-    // same rounding as two fmaf); each window plane is summed over its rows with the axis-1
-    // weights first, then added with its axis-0 weight times this lane's axis-2 weight
-    float2 a01 = make_float2(0.f, 0.f), a23 = make_float2(0.f, 0.f);
-    if (lane_ok) {
-      float2 ww1[W];
-#pragma unroll
-      for (int i1 = 0; i1 < W; ++i1) ww1[i1] = make_float2(w1[i1], w1[i1]);
-#pragma unroll
-      for (int i0 = 0; i0 < W; ++i0) {
-        const int r0 = l0 + i0;
-        if (KT != COV3D_KERNEL_ES && r0 < 0) continue;
-        float2 p01 = make_float2(0.f, 0.f), p23 = make_float2(0.f, 0.f);
-#pragma unroll
-        for (int i1 = 0; i1 < W; ++i1) {
-          const int r1 = l1 + i1;
-          if (KT != COV3D_KERNEL_ES && r1 < 0) continue;
-          const float4 v = base[(r0 * T + r1) * T * CP];
-          p01 = __ffma2_rn(ww1[i1], make_float2(v.x, v.y), p01);
-          p23 = __ffma2_rn(ww1[i1], make_float2(v.z, v.w), p23);
+  for (int base = first;;) {
+    for (int k0 = warp * PPW; k0 < cnt; k0 += kInterpWarps * PPW) {
+      const int k = k0 + pp;
+      const bool pt_ok = pp < PPW && k < cnt;
+      const SortedPoint sp = s_sp[pt_ok ? k : k0];
+      int c0[3];
+      c0[0] = first_cell<KT, W>(sp.t0);
+      c0[1] = first_cell<KT, W>(sp.t1);
+      c0[2] = first_cell<KT, W>(sp.t2);
+      // one kernel weight per lane wl < 3W, then shared through the warp
+      float myw = 0.0f;
+      if (wl < 3 * W) {
+        const int d = wl / W, tq = wl - (wl / W) * W;
+        const float td = d == 0 ? sp.t0 : d == 1 ? sp.t1 : sp.t2;
+        myw = tap_weight<KT, W>(td, tq, a.k.beta);
+      }
+      float w0[W], w1[W];
+  #pragma unroll
+      for (int r = 0; r < W; ++r) {
+        w0[r] = __shfl_sync(0xffffffffu, myw, lane0 + r);
+        w1[r] = __shfl_sync(0xffffffffu, myw, lane0 + W + r);
+      }
+      const float wj = __shfl_sync(0xffffffffu, myw, lane0 + 2 * W + (j < W ? j : 0));
+      int l0 = c0[0], l1 = c0[1], l2 = c0[2];
+      if (KT == COV3D_KERNEL_ES) {
+        l0 = wrap1(l0, n);
+        l1 = wrap1(l1, n);
+        l2 = wrap1(l2, n);
+      }
+      l0 -= ts0;
+      l1 -= ts1;
+      l2 -= ts2;
+      const int cell2 = l2 + j;
+      const bool lane_ok = pt_ok && cell2 >= 0;
+      const float4 *base = tile4 + cell2 * CP + q;
+      // two packed FP32 accumulators (FFMA2: one instruction per channel pair of values; the
+      // same rounding as two fmaf); each window plane is summed over its rows with the axis-1
+      // weights first, then added with its axis-0 weight times this lane's axis-2 weight
+      float2 a01 = make_float2(0.f, 0.f), a23 = make_float2(0.f, 0.f);
+      if (lane_ok) {
+        float2 ww1[W];
+  #pragma unroll
+        for (int i1 = 0; i1 < W; ++i1) ww1[i1] = make_float2(w1[i1], w1[i1]);
+  #pragma unroll
+        for (int i0 = 0; i0 < W; ++i0) {
+          const int r0 = l0 + i0;
+          if (KT != COV3D_KERNEL_ES && r0 < 0) continue;
+          float2 p01 = make_float2(0.f, 0.f), p23 = make_float2(0.f, 0.f);
+  #pragma unroll
+          for (int i1 = 0; i1 < W; ++i1) {
+            const int r1 = l1 + i1;
+            if (KT != COV3D_KERNEL_ES && r1 < 0) continue;
+            const float4 v = base[(r0 * T + r1) * T * CP];
+            p01 = __ffma2_rn(ww1[i1], make_float2(v.x, v.y), p01);
+            p23 = __ffma2_rn(ww1[i1], make_float2(v.z, v.w), p23);
+          }
+          const float w0j = w0[i0] * wj;
+          const float2 ww0 = make_float2(w0j, w0j);
+          a01 = __ffma2_rn(ww0, p01, a01);
+          a23 = __ffma2_rn(ww0, p23, a23);
         }
-        const float w0j = w0[i0] * wj;
-        const float2 ww0 = make_float2(w0j, w0j);
-        a01 = __ffma2_rn(ww0, p01, a01);
-        a23 = __ffma2_rn(ww0, p23, a23);
+      }
+      // the W partial sums of each pair by a shuffle tree over the window cells j (lanes j*CP + q
+      // of the slot): at each level cell j adds cell j + h, h = ceil(width / 2)
+      float4 s = make_float4(a01.x, a01.y, a23.x, a23.y);
+  #pragma unroll
+      for (int lvl = 0; lvl < 3; ++lvl) {
+        const int wc = lvl == 0 ? W : lvl == 1 ? (W + 1) / 2 : ((W + 1) / 2 + 1) / 2;
+        if (wc <= 1) break;
+        const int h = (wc + 1) / 2;
+        float4 t;
+        t.x = __shfl_down_sync(0xffffffffu, s.x, h * CP);
+        t.y = __shfl_down_sync(0xffffffffu, s.y, h * CP);
+        t.z = __shfl_down_sync(0xffffffffu, s.z, h * CP);
+        t.w = __shfl_down_sync(0xffffffffu, s.w, h * CP);
+        if (j + h < wc) {
+          s.x += t.x;
+          s.y += t.y;
+          s.z += t.z;
+          s.w += t.w;
+        }
+      }
+      if (pt_ok && sl < CP) {
+        // epilogue: vol_forward's Nyquist zeroing, CTF multiply and 1/L (projection_funcs.py:355-370)
+        const int64_t id = sp_id(sp.idf);
+        const float sc = s_sc[k];
+        float2 *o = a.out + id * a.ops + (int64_t)(a.ch0 + 2 * sl) * a.ocs;
+        if (2 * sl < a.nch) o[0] = make_float2(s.x * sc, s.y * sc);
+        if (2 * sl + 1 < a.nch) o[a.ocs] = make_float2(s.z * sc, s.w * sc);
       }
     }
-    // the W partial sums of each pair by a shuffle tree over the window cells j (lanes j*CP + q
-    // of the slot): at each level cell j adds cell j + h, h = ceil(width / 2)
-    float4 s = make_float4(a01.x, a01.y, a23.x, a23.y);
-#pragma unroll
-    for (int lvl = 0; lvl < 3; ++lvl) {
-      const int wc = lvl == 0 ? W : lvl == 1 ? (W + 1) / 2 : ((W + 1) / 2 + 1) / 2;
-      if (wc <= 1) break;
-      const int h = (wc + 1) / 2;
-      float4 t;
-      t.x = __shfl_down_sync(0xffffffffu, s.x, h * CP);
-      t.y = __shfl_down_sync(0xffffffffu, s.y, h * CP);
-      t.z = __shfl_down_sync(0xffffffffu, s.z, h * CP);
-      t.w = __shfl_down_sync(0xffffffffu, s.w, h * CP);
-      if (j + h < wc) {
-        s.x += t.x;
-        s.y += t.y;
-        s.z += t.z;
-        s.w += t.w;
-      }
+    base += a.max_sub;
+    if (base >= last) break;
+    cnt = min(a.max_sub, last - base);
+    __syncthreads();  // every warp is done with the previous points
+    for (int k = tid; k < cnt; k += blockDim.x) {
+      const SortedPoint sp = a.pts[base + k];
+      s_sp[k] = sp;
+      float sc = (a.nyquist && sp_nyquist(sp.idf)) ? 0.0f : a.scale;
+      sc *= ctf_factor(a.ctf, a.ctfc, a.g, sp_id(sp.idf));
+      s_sc[k] = sc;
     }
-    if (pt_ok && sl < CP) {
-      // epilogue: vol_forward's Nyquist zeroing, CTF multiply and 1/L (projection_funcs.py:355-370)
-      const int64_t id = sp_id(sp.idf);
-      const float sc = s_sc[k];
-      float2 *o = a.out + id * a.ops + (int64_t)(a.ch0 + 2 * sl) * a.ocs;
-      if (2 * sl < a.nch) o[0] = make_float2(s.x * sc, s.y * sc);
-      if (2 * sl + 1 < a.nch) o[a.ocs] = make_float2(s.z * sc, s.w * sc);
-    }
+    __syncthreads();
   }
 }
 
@@ -318,6 +341,7 @@ int launch_interp(cov3d_plan *p, const GridArgs &ga, int nchan, void *out, int64
   a.sub_bin = p->sub_bin.as<int>();
   a.sub_first = p->sub_first.as<int>();
   a.sub_count = p->sub_count.as<int>();
+  a.bin_off = p->bin_off.as<int>();
   a.nsub = p->nsub.as<int>();
   a.grid = static_cast<const float2 *>(ga.grid);
   a.cs = ga.cell_stride;

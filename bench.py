@@ -76,6 +76,8 @@ def parse():
     ap.add_argument("--no-bilinear", action="store_true", help="skip the bilinear-interpolation step")
     ap.add_argument("--ragged-L", type=int, default=256, help="volume size of the ragged Wiener measurement")
     ap.add_argument("--no-ragged", action="store_true", help="skip the ragged-batch Wiener measurement")
+    ap.add_argument("--no-rank20", action="store_true", help="skip the rank-20 step")
+    ap.add_argument("--no-small-epoch", action="store_true", help="skip the L=32 one-epoch measurement")
     return ap.parse_args()
 
 
@@ -285,6 +287,63 @@ def run_wiener_ragged(pkg, args, dev):
     return {"images_per_s": total / (ms / 1e3), "images": total, "L": L, "rank": r, "batch_sizes": sizes,
             "note": "ragged batches of 256..4096 images (full-pipeline configuration's sizes, L=256): ES "
                     "interpolation of the eigenvolumes' fine grid, FP32 Gram, FP64 Cholesky per image"}
+
+
+def run_small_epoch(pkg, args, dev, with_reference):
+    """The CPU-runnable configuration's training part: one epoch of covariance SGD at L = 32,
+    r = 5 over 2 000 images in batches of 256 (the last one 208), on bilinear plans, timed as
+    the wall time of the whole epoch on the GPU (host-resident images copied in per batch,
+    the cost read back per batch) and, when the reference is installed, the reference's own
+    run_batch for the same batches on the host cores."""
+    import torch
+
+    from importlib import import_module
+
+    syn = import_module("3dcovarestimation_gb300.synthetic")
+    L, r, N, B = 32, 5, 2000, 256
+    g = torch.Generator(device=dev).manual_seed(args.seed + 7)
+    images = (torch.randn((N, L * L), device=dev, generator=g, dtype=torch.complex64) * 10).cpu().pin_memory()
+    rot = syn.uniform_rotations(N, generator=g, device=dev).cpu().pin_memory()
+    prm = syn.ctf_params(torch.rand((N,), device=dev, generator=g) * 2 + 1, 3.0, device=dev).cpu().pin_memory()
+    covar = pkg.Covar(L, r, upsampling_factor=2).to(dev)
+    covar.vectors.grad = torch.zeros_like(covar.vectors)
+    covar.log_sqrt_eigenvals.grad = torch.zeros_like(covar.log_sqrt_eigenvals)
+    opt = torch.optim.Adam([{"params": covar.vectors, "lr": 1e-6 * B}, {"params": covar.log_sqrt_eigenvals,
+                                                                        "lr": 1e-4 * B}])
+    step = pkg.FusedCovarStep(L, r, "bilinear", 2, device=dev, max_batch=B)
+
+    def epoch():
+        costs = []
+        for i in range(0, N, B):
+            j = min(N, i + B)
+            step.set_rotations(rot[i:j].to(dev, non_blocking=True))
+            c, _, _ = step(covar.vectors.detach(), covar.log_sqrt_eigenvals.detach(),
+                           images[i:j].to(dev, non_blocking=True), None, 1.0e4, 0.0, None,
+                           grad_vectors=covar.vectors.grad, grad_log_sqrt=covar.log_sqrt_eigenvals.grad,
+                           ctf_params=prm[i:j].to(dev, non_blocking=True))
+            opt.step()
+            costs.append(float(c))
+        return costs
+
+    epoch()  # warm-up: plans, kernels
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    epoch()
+    torch.cuda.synchronize()
+    gpu_s = time.perf_counter() - t0
+    out = {"L": L, "rank": r, "images": N, "batch": B, "gpu_epoch_s": gpu_s, "gpu_images_per_s": N / gpu_s,
+           "note": "one epoch of the fused step on bilinear plans, host images copied in and the cost read back "
+                   "per batch; mean CG not included"}
+    if with_reference:
+        from oracle import ref_step
+
+        if ref_step.available():
+            ips, det = ref_step.time_steps(L, r, B, 8, 1, seed=args.seed, budget_s=60.0)
+            out["reference_images_per_s"] = ips
+            out["reference_epoch_s_estimate"] = N / ips
+            out["reference_sample"] = (f"{det['steps']} whole run_batch step(s) of {B} images after {det['warmup']} "
+                                       f"warm-up, torch CPU threads={det['threads']}")
+    return out
 
 
 def run_mean_cg(pkg, args, dev):
@@ -531,6 +590,43 @@ def run_gb300(args):
                 "note": "Gram contractions in BF16 with FP32 accumulation (tcgen05); projections, spreading, "
                         "solve and update unchanged (FP32 / FP64)"}
 
+    # the precision configuration's rank: r = 20 at the same L and batch, FP32 and BF16 Gram
+    rank20 = None
+    if not args.no_rank20:
+        r2 = 20
+        covar20 = pkg.Covar(L, r2, upsampling_factor=2).to(dev)
+        gv20 = torch.zeros_like(covar20.vectors)
+        gl20 = torch.zeros_like(covar20.log_sqrt_eigenvals)
+        rank20 = {"L": L, "rank": r2, "batch": B}
+        for prec in ("fp32", "bf16"):
+            st20 = pkg.FusedCovarStep(L, r2, "nufft", 2, width=args.width, device=dev,
+                                      compensated=not args.uncompensated, gram_precision=prec, max_batch=B)
+
+            def step20(k):
+                b = (k * world + rank) % nb
+                st20.set_rotations(rot[b])
+                st20(covar20.vectors.detach(), covar20.log_sqrt_eigenvals.detach(), images[b], None, noise_var,
+                     reg_scale, fourier_reg, grad_vectors=gv20, grad_log_sqrt=gl20, ctf_params=prm[b])
+
+            for k in range(2):
+                step20(k)
+            barrier()
+            st20.plan.timing(True)
+            t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            n20 = max(3, args.steps // 4)
+            t0.record(stream)
+            for k in range(n20):
+                step20(k)
+            t1.record(stream)
+            barrier()
+            ph20 = st20.plan.timing_read()
+            st20.plan.timing(False)
+            ms20 = t0.elapsed_time(t1) / n20
+            rank20[prec] = {"images_per_s": world * B / (ms20 / 1e3), "ms_per_step": ms20, "steps": n20,
+                            "phases_ms_per_step": {k: v[0] / n20 for k, v in ph20.items() if v[1]}}
+            del st20
+        torch.cuda.empty_cache()
+
     # the same step on the reference's default interpolation (NufftPlanDiscretized bilinear,
     # grid_sample semantics): the like-for-like comparison with the reference's CPU arm
     bilinear = None
@@ -659,10 +755,14 @@ def run_gb300(args):
     }
     if bf16 is not None:
         line["bf16_gram"] = bf16
+    if rank20 is not None:
+        line["rank20_step"] = rank20
     if wiener is not None:
         line["wiener_coords"] = wiener
     if not args.no_wiener and not args.no_ragged:
         line["wiener_ragged"] = run_wiener_ragged(pkg, args, dev)
+    if not args.no_small_epoch:
+        line["small_epoch"] = run_small_epoch(pkg, args, dev, with_reference=not args.no_cpu_baseline)
     if not args.no_mean:
         line["mean_cg"] = run_mean_cg(pkg, args, dev)
     if bilinear is not None:

@@ -1,7 +1,7 @@
 // Interpolation ("type-2" half of the NUFFT, and the reference's grid_sample forward) over
-// bin-sorted points: each subproblem's tile of the fine grid is read from HBM once into shared
-// memory and reused by all its points; the projection epilogue (Nyquist zeroing, CTF
-// multiply, 1/L) is fused.
+// bin-sorted points: each bin's tile of the fine grid is read from HBM once into shared memory
+// and reused by all its points; the projection epilogue (Nyquist zeroing, CTF multiply, 1/L)
+// is fused.
 #include "cov3d_device.cuh"
 
 namespace cov3d {
@@ -15,7 +15,6 @@ struct InterpParams {
   const SortedPoint *pts;
   const int *sub_bin;
   const int *sub_first;
-  const int *sub_count;
   const int *bin_off;  // first sorted point of each bin (exclusive scan of the bin counts)
   const int *nsub;
   const float2 *grid;
@@ -23,7 +22,6 @@ struct InterpParams {
   int shift;
   int ch0;
   int nch;  // channels in this pass (<= 2 * CP)
-  int max_sub;
   float2 *out;
   int64_t ops, ocs;
   const float *ctf;
@@ -33,7 +31,8 @@ struct InterpParams {
 };
 
 constexpr int kBin = 8;
-constexpr int kInterpWarps = 24;  // 56 registers: 24 warps next to the one 190 KB tile per SM
+constexpr int kInterpWarps = 24;    // 24 warps next to the one 176 KB tile per SM (ES, 10 channels)
+constexpr int kInterpChunk = 1024;  // points staged at a time (20 KB of records and epilogue factors)
 
 // Channel pairs per pass: lanes are (window cell, channel pair) pairs, so W * CP <= 32, and the
 // tile (bin + halo) of 2*CP complex channels must fit in shared memory.
@@ -42,7 +41,7 @@ struct InterpCP {
   static constexpr int value = W <= 2 ? 16 : 32 / W;
 };
 
-// One block per subproblem.  The block stages the bin's tile (bin + (W-1)-cell halo) of 2*CP
+// One block per bin (see the kernel's first lines).  The block stages the bin's tile (bin + (W-1)-cell halo) of 2*CP
 // channels in shared memory as [cell][channel] complex, then each warp takes one point at a
 // time (32 / (W*CP) points for the narrow bilinear and nearest windows): lane (j, q) reads the
 // two channels 2q, 2q+1 of tile[row][corner2 + j] for the W*W window rows -- W*CP contiguous
@@ -59,21 +58,18 @@ __global__ void __launch_bounds__(kInterpWarps * 32) interp_kernel(const InterpP
   constexpr int PPW = (LANES >= 3 * W && 32 / LANES > 1) ? 32 / LANES : 1;
   extern __shared__ float4 tile4[];  // T^3 * CP float4 (= 2 complex), then the point records
   float2 *tile = reinterpret_cast<float2 *>(tile4);
-  SortedPoint *s_sp = reinterpret_cast<SortedPoint *>(tile4 + T * T * T * CP);  // max_sub
-  float *s_sc = reinterpret_cast<float *>(s_sp + a.max_sub);                     // epilogue factor
+  SortedPoint *s_sp = reinterpret_cast<SortedPoint *>(tile4 + T * T * T * CP);  // kInterpChunk
+  float *s_sc = reinterpret_cast<float *>(s_sp + kInterpChunk);                  // epilogue factor
   const int sub = blockIdx.x;
   if (sub >= *a.nsub) return;
   const int bin = a.sub_bin[sub];
   const int first = a.sub_first[sub];
-#ifdef COV3D_EXP_BINBLOCK
   // one block per bin: the block of the bin's first subproblem takes all of the bin's points,
-  // max_sub at a time, so the tile is staged once per bin
+  // kInterpChunk at a time, so the tile is staged once per bin (a bin holds 2.8 subproblems on
+  // average at the cov-SGD workload; 14.1 -> 12.6 ms)
   if (first != a.bin_off[bin]) return;
   const int last = a.bin_off[bin + 1];
-#else
-  const int last = first + a.sub_count[sub];
-#endif
-  int cnt = min(a.max_sub, last - first);
+  int cnt = min(kInterpChunk, last - first);
   const int nb12 = a.bins.nb[1] * a.bins.nb[2];
   const int ts0 = (bin / nb12) * kBin;
   const int ts1 = ((bin / a.bins.nb[2]) % a.bins.nb[1]) * kBin;
@@ -248,9 +244,9 @@ __global__ void __launch_bounds__(kInterpWarps * 32) interp_kernel(const InterpP
         if (2 * sl + 1 < a.nch) o[a.ocs] = make_float2(s.z * sc, s.w * sc);
       }
     }
-    base += a.max_sub;
+    base += kInterpChunk;
     if (base >= last) break;
-    cnt = min(a.max_sub, last - base);
+    cnt = min(kInterpChunk, last - base);
     __syncthreads();  // every warp is done with the previous points
     for (int k = tid; k < cnt; k += blockDim.x) {
       const SortedPoint sp = a.pts[base + k];
@@ -277,7 +273,7 @@ template <int KT, int W, int CP>
 int launch_cp(const InterpParams &a, int64_t max_blocks, cudaStream_t st) {
   constexpr int T = kBin + W - 1;
   const size_t smem =
-      (size_t)T * T * T * CP * sizeof(float4) + (size_t)a.max_sub * (sizeof(SortedPoint) + 4);
+      (size_t)T * T * T * CP * sizeof(float4) + (size_t)kInterpChunk * (sizeof(SortedPoint) + 4);
   if (smem > 32 * 1024) {  // static shared arrays come on top of the dynamic size
     cudaError_t e = cudaFuncSetAttribute(interp_kernel<KT, W, CP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
@@ -337,10 +333,8 @@ int launch_interp(cov3d_plan *p, const GridArgs &ga, int nchan, void *out, int64
   a.k = make_kernel(p);
   a.bins = p->bins;
   a.pts = p->sorted.as<SortedPoint>();
-  a.max_sub = p->max_sub;
   a.sub_bin = p->sub_bin.as<int>();
   a.sub_first = p->sub_first.as<int>();
-  a.sub_count = p->sub_count.as<int>();
   a.bin_off = p->bin_off.as<int>();
   a.nsub = p->nsub.as<int>();
   a.grid = static_cast<const float2 *>(ga.grid);

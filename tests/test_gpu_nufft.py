@@ -85,6 +85,30 @@ def test_es_nufft_matches_direct_sum(pkg, dev, width, tol, L):
     assert rel(out, O.es_type2(vol, pts.astype(np.float64), 2, width).reshape(out.shape)) < 3e-6
 
 
+@pytest.mark.parametrize("kind", ["nufft", "bilinear"])
+def test_crowded_bins_match_oracle(pkg, dev, kind):
+    """512 images at L = 16: every slice passes through the centre, so the central bins hold
+    thousands of points and the interpolation takes them in several chunks of one block."""
+    L, B, C = 16, 512, 3
+    rng = np.random.default_rng(9)
+    R = O.rotvec_to_rotmat(rng.standard_normal((B, 3)))
+    if kind == "nufft":
+        pts = O.rotated_points(R, L).astype(np.float32)
+        vol = rng.standard_normal((C, L, L, L)).astype(np.float32)
+        plan = pkg.NufftPlan((L,) * 3, batch_size=C, device=dev, width=6)
+        plan.setpts(T(pts, dev))
+        out = plan.execute_forward(T(vol, dev))
+        assert rel(out, O.es_type2(vol, pts.astype(np.float64), 2, 6).reshape(out.shape)) < 3e-6
+    else:
+        pts = np.ascontiguousarray(O.rotated_points(R, L, wrap=False))
+        n = 2 * L
+        grid = (rng.standard_normal((C, n, n, n)) + 1j * rng.standard_normal((C, n, n, n))).astype(np.complex64)
+        plan = pkg.NufftPlanDiscretized((L,) * 3, upsample_factor=2, mode="bilinear")
+        plan.setpts(T(pts, dev, torch.float32))
+        out = plan._plan.interp(T(grid, dev))
+        assert rel(out.reshape(C, B, -1), O.interp_discretized(grid, pts, "bilinear")) < TOL_FP32
+
+
 def test_es_adjointness_and_known_slice(pkg, dev):
     rng = np.random.default_rng(5)
     L = 15

@@ -172,6 +172,26 @@ def test_latent_map_ragged_batches(pkg, dev, batch):
     assert rel(c, d["z"]) < 1e-4
 
 
+def test_fine_grid_reuse_equals_vol_forward(pkg, dev):
+    """The eigenvolumes transformed once (cov3d_fine_grid) and interpolated per batch give the
+    projections vol_forward gives with the full type 2 per batch, in both domains, over two
+    batches of different poses and sizes."""
+    L, r = 24, 6
+    g = torch.Generator(device=dev).manual_seed(21)
+    vols = torch.randn((r, L, L, L), device=dev, generator=g)
+    plan = pkg.NufftPlan((L,) * 3, batch_size=r, device=dev)
+    project = pkg.wiener_coords._EigenProjector(plan, vols)
+    for n in (7, 13):
+        R = torch.linalg.qr(torch.randn((n, 3, 3), device=dev, generator=g))[0].contiguous()
+        ctf = torch.rand((n, L, L), device=dev, generator=g) + 0.2
+        plan.setrot(R)
+        for fourier in (True, False):
+            want = pkg.vol_forward(vols, plan, ctf, fourier_domain=fourier)
+            got = project(ctf, fourier_domain=fourier)
+            assert got.shape == want.shape
+            assert rel(got, want) < 1e-6
+
+
 @pytest.mark.parametrize("masked,fourier", [(False, False), (True, False), (True, True)])
 def test_preprocess_image_batch_matches_reference(pkg, dev, masked, fourier):
     g = load_golden("preprocess_L10.npz")

@@ -32,6 +32,15 @@ struct InterpParams {
 
 constexpr int kBin = 8;
 constexpr int kInterpWarps = 24;    // 24 warps next to the one 176 KB tile per SM (ES, 10 channels)
+// warps per block: more for the wide windows' large tiles (one block per SM)
+template <int W, int CP>
+struct InterpWarps {
+#ifdef COV3D_EXP_IW32
+  static constexpr int value = (W > 2 && CP >= 3) ? 32 : kInterpWarps;
+#else
+  static constexpr int value = kInterpWarps;
+#endif
+};
 constexpr int kInterpChunk = 1024;  // points staged at a time (20 KB; 2048 measured slightly slower)
 
 // Channel pairs per pass: lanes are (window cell, channel pair) pairs, so W * CP <= 32, and the
@@ -49,7 +58,7 @@ struct InterpCP {
 // weight * value; the W partial sums of each pair are combined by a warp-shuffle tree and the
 // epilogue (Nyquist zeroing, CTF, scale) is applied.
 template <int KT, int W, int CP>
-__global__ void __launch_bounds__(kInterpWarps * 32) interp_kernel(const InterpParams a) {
+__global__ void __launch_bounds__(InterpWarps<W, CP>::value * 32) interp_kernel(const InterpParams a) {
   constexpr int T = kBin + W - 1;
   constexpr int CH = 2 * CP;
   constexpr int LANES = W * CP;
@@ -154,7 +163,7 @@ __global__ void __launch_bounds__(kInterpWarps * 32) interp_kernel(const InterpP
   const int lane0 = (pp < PPW ? pp : 0) * LANES;  // first lane of this lane's point slot
   const int wl = PPW == 1 ? lane : sl;             // this lane's tap among the point's 3W weights
   for (int base = first;;) {
-    for (int k0 = warp * PPW; k0 < cnt; k0 += kInterpWarps * PPW) {
+    for (int k0 = warp * PPW; k0 < cnt; k0 += InterpWarps<W, CP>::value * PPW) {
       const int k = k0 + pp;
       const bool pt_ok = pp < PPW && k < cnt;
       const SortedPoint sp = s_sp[pt_ok ? k : k0];
@@ -279,7 +288,7 @@ int launch_cp(const InterpParams &a, int64_t max_blocks, cudaStream_t st) {
                                          (int)smem);
     if (e != cudaSuccess) return check_cuda(e, "cudaFuncSetAttribute(interp_kernel)");
   }
-  interp_kernel<KT, W, CP><<<(unsigned)max_blocks, kInterpWarps * 32, smem, st>>>(a);
+  interp_kernel<KT, W, CP><<<(unsigned)max_blocks, InterpWarps<W, CP>::value * 32, smem, st>>>(a);
   return launched("interp_kernel");
 }
 

@@ -31,15 +31,12 @@ struct InterpParams {
 };
 
 constexpr int kBin = 8;
-constexpr int kInterpWarps = 24;    // 24 warps next to the one 176 KB tile per SM (ES, 10 channels)
-// warps per block: more for the wide windows' large tiles (one block per SM)
+constexpr int kInterpWarps = 24;    // warps per block of the small tiles (two blocks per SM)
+// Warps per block: 32 next to the wide windows' large tiles, one block per SM (ES, 10 channels:
+// 11.9 against 12.0 ms with 24; the narrow tiles measured slower with 32)
 template <int W, int CP>
 struct InterpWarps {
-#ifdef COV3D_EXP_IW32
   static constexpr int value = (W > 2 && CP >= 3) ? 32 : kInterpWarps;
-#else
-  static constexpr int value = kInterpWarps;
-#endif
 };
 constexpr int kInterpChunk = 1024;  // points staged at a time (20 KB; 2048 measured slightly slower)
 

@@ -38,6 +38,24 @@ def test_exact_inputs_match_bit_for_bit(pkg, dev, n, r, P):
         assert torch.equal(a, b)
 
 
+@pytest.mark.parametrize("n,P", [(7, 4096), (11, 1000), (5, 16384)])
+def test_point_major_r10_matches_bit_for_bit(pkg, dev, n, P):
+    """The fused step's layout (Q point-major, r = 10, the staged FP32 Gram's fast path on the
+    other side): bit for bit against the FP32 Gram with BF16-exact inputs, including a pixel
+    count that is not a multiple of the 128-pixel stage."""
+    r = 10
+    g = torch.Generator(device=dev).manual_seed(n + P)
+    q = torch.randint(-32, 33, (n, P, r, 2), generator=g, device=dev).float() / 4
+    yv = torch.randint(-32, 33, (n, P, 2), generator=g, device=dev).float() / 4
+    Q = torch.view_as_complex(q.contiguous()).permute(0, 2, 1)  # (n, r, P), point stride r
+    y = torch.view_as_complex(yv.contiguous())
+    ref = fp32_gram(pkg, Q, y)
+    out = pkg.covar_sgd.gram_bf16(Q, y)
+    torch.cuda.synchronize()
+    for a, b in zip(out, ref):
+        assert torch.equal(a, b)
+
+
 def test_general_inputs_within_bf16_rounding(pkg, dev):
     g = torch.Generator(device=dev).manual_seed(5)
     n, r, P = 40, 10, 16384

@@ -31,6 +31,8 @@ int check_cufft(cufftResult r, const char *what);
 #define COV3D_CUDA(expr) COV3D_TRY(::cov3d::check_cuda((expr), #expr))
 // Counts one kernel launch of this library and checks the launch error.
 int launched(const char *name);
+// adds n kernel launches to the library's count (each replay of a captured CUDA graph)
+void count_launches(long long n);
 #define COV3D_LAUNCHED(name) COV3D_TRY(::cov3d::launched(name))
 
 // ----------------------------------------------------------------------------- geometry

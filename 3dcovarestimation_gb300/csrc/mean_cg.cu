@@ -669,7 +669,8 @@ int cg_solve(cov3d_plan *p, const float *d_lhs, const void *d_b, void *d_x, doub
     return COV3D_OK;
   }
 
-  for (int it = 0; it < maxiter; ++it) {
+  // one iteration: every kernel is a no-op once the device state says done
+  auto iteration = [&]() -> int {
     COV3D_TRY(apply_A(pv, ap, pv, st));
     update_kernel<<<capped(nb(L3)), 256, 0, s>>>(x, r, pv, ap, L3, st);
     COV3D_LAUNCHED("update_kernel");
@@ -685,13 +686,51 @@ int cg_solve(cov3d_plan *p, const float *d_lhs, const void *d_b, void *d_x, doub
     direction_kernel<<<capped(nb(L3)), 256, 0, s>>>(pv, zz, L3, st);
     COV3D_LAUNCHED("direction_kernel");
     roll_kernel<<<1, 1, 0, s>>>(st);
-    COV3D_LAUNCHED("roll_kernel");
-    if ((it + 1) % poll_every == 0 || it + 1 == maxiter) {
-      COV3D_CUDA(cudaMemcpyAsync(&hs, st, sizeof(CgState), cudaMemcpyDeviceToHost, s));
-      COV3D_CUDA(cudaStreamSynchronize(s));
-      if (hs.done) break;
+    return launched("roll_kernel");
+  };
+  // poll_every iterations captured once as a CUDA graph on a side stream (a capture cannot run
+  // on the legacy default stream), then replayed on the plan's stream until the state says done:
+  // one launch per poll_every iterations instead of about 14 per iteration (learned-PC solve at
+  // L = 128: 0.221 -> 0.194 s, plain CG 1.39 -> 1.25 s)
+  {
+    const cudaStream_t s0 = s;
+    cudaStream_t cs = nullptr;
+    COV3D_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    const cufftHandle hs_all[] = {h, hc, hp, h0, hcp};
+    auto set_streams = [&](cudaStream_t to) -> int {
+      p->stream = to;
+      s = to;
+      for (cufftHandle hh : hs_all)
+        if (hh) COV3D_TRY(check_cufft(cufftSetStream(hh, to), "cufftSetStream"));
+      return COV3D_OK;
+    };
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    const long long l0 = cov3d_launch_count();
+    int rc = set_streams(cs);
+    if (rc == COV3D_OK) rc = check_cuda(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "capture");
+    if (rc == COV3D_OK) {
+      for (int k = 0; k < poll_every && rc == COV3D_OK; ++k) rc = iteration();
+      const int rc2 = check_cuda(cudaStreamEndCapture(cs, &graph), "end capture");
+      if (rc == COV3D_OK) rc = rc2;
     }
+    const long long per_replay = cov3d_launch_count() - l0;
+    const int rc3 = set_streams(s0);
+    if (rc == COV3D_OK) rc = rc3;
+    if (rc == COV3D_OK) rc = check_cuda(cudaGraphInstantiate(&exec, graph, 0), "graph instantiate");
+    for (int it = 0; rc == COV3D_OK && it < maxiter; it += poll_every) {
+      rc = check_cuda(cudaGraphLaunch(exec, s0), "graph launch");
+      count_launches(per_replay);
+      if (rc == COV3D_OK) rc = check_cuda(cudaMemcpyAsync(&hs, st, sizeof(CgState), cudaMemcpyDeviceToHost, s0), "poll");
+      if (rc == COV3D_OK) rc = check_cuda(cudaStreamSynchronize(s0), "poll sync");
+      if (rc == COV3D_OK && hs.done) break;
+    }
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    cudaStreamDestroy(cs);
+    if (rc != COV3D_OK) return rc;
   }
+
   COV3D_CUDA(cudaMemcpyAsync(&hs, st, sizeof(CgState), cudaMemcpyDeviceToHost, s));
   COV3D_CUDA(cudaStreamSynchronize(s));
   const double rel = sqrt(hs.rr_new / hs.b2);

@@ -27,6 +27,8 @@ int launched(const char *name) {
   return check_cuda(cudaGetLastError(), name);
 }
 
+void count_launches(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
 PhaseScope::PhaseScope(cov3d_plan *p, int phase) : p_(p) {
   if (!p->timing) return;
   auto &pool = *p->ev_pool;

@@ -311,7 +311,10 @@ int cov3d_circulant_symbol(cov3d_plan *plan, const float *d_reg_lhs, float *d_sy
  * in the L^3 Fourier domain.  *iters receives the loop index at which it stopped (the
  * reference's num_iter), *relres ||r|| / ||b||; d_history (maxiter + 1 doubles, may be NULL)
  * the relative residual before the loop and after each iteration.  Returns COV3D_EMAXITER
- * (with d_x holding the last iterate) when the tolerance was not reached. */
+ * (with d_x holding the last iterate) when the tolerance was not reached.  The iterations run as
+ * replays of a CUDA graph of 8 iterations that the call captures on its own side stream and
+ * launches on the plan's stream; the host reads the state between replays, so the call
+ * synchronises the plan's stream and cannot itself run inside a caller's stream capture. */
 int cov3d_cg_solve(cov3d_plan *plan, const float *d_reg_lhs, const void *d_b, void *d_x, double rtol, int maxiter,
                    int precond, const float *d_symbol, int *iters, double *relres, double *d_history);
 

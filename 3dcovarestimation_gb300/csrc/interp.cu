@@ -159,6 +159,9 @@ __global__ void __launch_bounds__(InterpWarps<W, CP>::value * 32) interp_kernel(
   const int j = sl / CP, q = sl - (sl / CP) * CP;
   const int lane0 = (pp < PPW ? pp : 0) * LANES;  // first lane of this lane's point slot
   const int wl = PPW == 1 ? lane : sl;             // this lane's tap among the point's 3W weights
+  // the point slots' taps, per warp and double-buffered by iteration (see below)
+  __shared__ __align__(16) float s_w[InterpWarps<W, CP>::value * 2 * PPW * 24];
+  int wbuf = 0;
   for (int base = first;;) {
     for (int k0 = warp * PPW; k0 < cnt; k0 += InterpWarps<W, CP>::value * PPW) {
       const int k = k0 + pp;
@@ -175,13 +178,21 @@ __global__ void __launch_bounds__(InterpWarps<W, CP>::value * 32) interp_kernel(
         const float td = d == 0 ? sp.t0 : d == 1 ? sp.t1 : sp.t2;
         myw = tap_weight<KT, W>(td, tq, a.k.beta);
       }
-      float w0[W], w1[W];
-  #pragma unroll
-      for (int r = 0; r < W; ++r) {
-        w0[r] = __shfl_sync(0xffffffffu, myw, lane0 + r);
-        w1[r] = __shfl_sync(0xffffffffu, myw, lane0 + W + r);
+      // through the warp's slot in shared memory (double-buffered by iteration): axis-0 taps at
+      // 0, axis-1 at 8, axis-2 at 16, read back as broadcast 16-byte loads -- five loads and a
+      // store instead of 13 shuffles in the queue the tile loads use (11.9 -> 11.5 ms)
+      float *ws = s_w + ((warp * 2 + wbuf) * PPW + lane0 / LANES) * 24;
+      if (wl < 3 * W) ws[(wl / W) * 8 + wl - (wl / W) * W] = myw;
+      __syncwarp();
+      float w0[8], w1[8];
+      {
+        const float4 a0 = *reinterpret_cast<const float4 *>(ws), a1 = *reinterpret_cast<const float4 *>(ws + 4);
+        const float4 b0 = *reinterpret_cast<const float4 *>(ws + 8), b1 = *reinterpret_cast<const float4 *>(ws + 12);
+        w0[0] = a0.x; w0[1] = a0.y; w0[2] = a0.z; w0[3] = a0.w; w0[4] = a1.x; w0[5] = a1.y; w0[6] = a1.z; w0[7] = a1.w;
+        w1[0] = b0.x; w1[1] = b0.y; w1[2] = b0.z; w1[3] = b0.w; w1[4] = b1.x; w1[5] = b1.y; w1[6] = b1.z; w1[7] = b1.w;
       }
-      const float wj = __shfl_sync(0xffffffffu, myw, lane0 + 2 * W + (j < W ? j : 0));
+      const float wj = ws[16 + (j < W ? j : 0)];
+      wbuf ^= 1;
       int l0 = c0[0], l1 = c0[1], l2 = c0[2];
       if (KT == COV3D_KERNEL_ES) {
         l0 = wrap1(l0, n);

@@ -409,11 +409,13 @@ def run_mean_cg(pkg, args, dev):
         pcn = lp.LearnedPreconditioner(device=dev)
         pcn.symbol(reg, L)  # warm
         torch.cuda.synchronize()
+        torch.cuda.nvtx.range_push("mean_cg_learned_pc")
         t0 = time.perf_counter()
         sym = pcn.symbol(reg, L)  # features + network + upsampling, inside the timed solve
         x, info = mean.cg_solve(reg, b, x0, L, rtol=args.mean_rtol, maxiter=args.mean_maxiter, precond=sym)
         torch.cuda.synchronize()
         sec = time.perf_counter() - t0
+        torch.cuda.nvtx.range_pop()
         out["learned_pc"] = {"seconds": sec, "iters": info.iters, "relres": info.relres, "converged": info.converged,
                              "ms_per_iter": 1e3 * sec / max(1, info.iters + 1)}
         out["learned_vs_diagonal_pc_time"] = sec / out["diagonal_pc"]["seconds"]

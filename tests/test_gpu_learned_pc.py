@@ -63,7 +63,7 @@ def test_committed_network_beats_the_circulant_preconditioner(pkg, dev):
                                                     "3dcovarestimation_gb300", "learned_pc_weights.npz")),
                     reason="no trained weights")
 def test_committed_network_against_the_diagonal_preconditioner(pkg, dev):
-    """The fallback the learned preconditioner is judged against: the Fourier-diagonal 1/reg_lhs
+    """The fallback the learned preconditioner is measured against: the Fourier-diagonal 1/reg_lhs
     on the fine grid.  Same problem, same rtol, both converge; the learned symbol (features +
     network + the L^3 symbol, timed inside the solve) takes less wall time than the diagonal
     preconditioner, whose every iteration costs a second fine-grid transform pair."""

@@ -25,7 +25,7 @@ APPLY_NYQUIST, APPLY_CTF, APPLY_CTF_PARAMS = 1, 2, 4
 # phase shift)
 CTF_NPARAMS = 8
 # cov3d_plan_reserve flags
-RESERVE_POINTS, RESERVE_GRAM_BF16 = 1, 2
+RESERVE_POINTS, RESERVE_GRAM_BF16, RESERVE_LS_REG = 1, 2, 4
 
 c_int, c_int64, c_double, c_float, c_void_p = ctypes.c_int, ctypes.c_int64, ctypes.c_double, ctypes.c_float, ctypes.c_void_p
 

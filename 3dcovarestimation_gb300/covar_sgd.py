@@ -171,10 +171,13 @@ class FusedCovarStep:
     ``noise_var`` is the Fourier-domain variance (spatial variance * L**2), exactly as the
     reference trainer holds them after ``dataset.to_fourier_domain()`` (``dataset.py:426-433``);
     by Parseval the resulting cost equals the reference's spatial-domain cost for "nufft".
+    ``max_batch`` sizes every workspace at construction (later steps of up to that many images
+    allocate nothing); ``ls_regulariser`` also sizes the least-squares Fourier regulariser's.
     """
 
     def __init__(self, resolution, rank, nufft_disc="nufft", upsampling_factor=2, width=6, eps=1e-6,
-                 compensated=True, device=None, bin_size=0, gram_precision="fp32", max_batch=None):
+                 compensated=True, device=None, bin_size=0, gram_precision="fp32", max_batch=None,
+                 ls_regulariser=False):
         kernel = {"nufft": _lib.KERNEL_ES, "bilinear": _lib.KERNEL_LINEAR, "nearest": _lib.KERNEL_NEAREST}[nufft_disc]
         if gram_precision not in ("fp32", "bf16"):
             raise ValueError("gram_precision must be 'fp32' or 'bf16'")
@@ -185,7 +188,8 @@ class FusedCovarStep:
         self.L, self.rank, self.nufft_disc = resolution, rank, nufft_disc
         self.device = self.plan.device
         if max_batch:  # every workspace sized now: steps of up to max_batch images allocate nothing
-            self.plan.reserve(max_batch, resolution, rank, points=True, gram_bf16=self.gram_bf16)
+            self.plan.reserve(max_batch, resolution, rank, points=True, gram_bf16=self.gram_bf16,
+                              ls_reg=ls_regulariser)
         self.d_cost = torch.zeros((1,), dtype=torch.float64, device=self.device)
 
     def set_rotations(self, rotmats):
@@ -406,7 +410,8 @@ class CovarTrainer:
             ds.to_fourier_domain() if self.optimize_in_fourier_domain else ds.to_spatial_domain()
         self.step_fn = FusedCovarStep(self.covar.resolution, self.covar.rank, nufft_disc, self.covar.upsampling_factor,
                                       width=width, compensated=compensated, device=self.device,
-                                      gram_precision=gram_precision, max_batch=self.batch_size)
+                                      gram_precision=gram_precision, max_batch=self.batch_size,
+                                      ls_regulariser=self.objective == OBJECTIVE_LS and reg != 0)
         if nufft_disc == "nufft":
             self.covar.grid_correction = self.step_fn.plan.grid_correction().to(self.device)
         else:

@@ -239,6 +239,7 @@ int launch_zero(cov3d_plan *p, void *ptr, int64_t bytes);
 int launch_ls_reg(cov3d_plan *p, const void *grid, void *ggrid, const float *fr, int64_t fr_stride, int r, double s,
                   double *cost_acc);
 void release_blas(cov3d_plan *p);
+int reserve_ls_reg(cov3d_plan *p, int r);
 
 // gram_solve.cu
 int launch_gram_bf16(cov3d_plan *p, cudaStream_t st, int B, int P, int r, const void *q, int64_t is, int64_t ps,

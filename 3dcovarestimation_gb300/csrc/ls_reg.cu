@@ -101,6 +101,20 @@ void release_blas(cov3d_plan *p) {
   p->blas = nullptr;
 }
 
+// The regulariser's workspace (X, K X and K: 2 r n^3 + n^2 complex) and the cuBLAS handle,
+// created once; later calls at the same or a smaller rank allocate nothing.
+int reserve_ls_reg(cov3d_plan *p, int r) {
+  const int64_t n = p->n;
+  COV3D_TRY(grow(p->lsw, (2 * r * n * n * n + n * n) * 8));
+  if (!p->blas) {
+    cublasHandle_t h = nullptr;
+    COV3D_TRY(check_blas(cublasCreate(&h), "cublasCreate"));
+    p->blas = h;
+    COV3D_TRY(check_blas(cublasSetMathMode(h, CUBLAS_DEFAULT_MATH), "cublasSetMathMode"));  // FP32, no TF32
+  }
+  return COV3D_OK;
+}
+
 int launch_ls_reg(cov3d_plan *p, const void *grid, void *ggrid, const float *fr, int64_t fr_stride, int r, double s,
                   double *cost_acc) {
   const int n = p->n;
@@ -110,16 +124,10 @@ int launch_ls_reg(cov3d_plan *p, const void *grid, void *ggrid, const float *fr,
     set_error("least-squares regulariser: r * n^2 = %lld exceeds the GEMM's int range", (long long)kdim);
     return COV3D_EINVAL;
   }
-  COV3D_TRY(grow(p->lsw, (2 * r * n3 + (int64_t)n * n) * 8));
+  COV3D_TRY(reserve_ls_reg(p, r));
   float2 *x = p->lsw.as<float2>();
   float2 *y = x + r * n3;
   float2 *kmat = y + r * n3;
-  if (!p->blas) {
-    cublasHandle_t h = nullptr;
-    COV3D_TRY(check_blas(cublasCreate(&h), "cublasCreate"));
-    p->blas = h;
-    COV3D_TRY(check_blas(cublasSetMathMode(h, CUBLAS_DEFAULT_MATH), "cublasSetMathMode"));  // FP32, no TF32
-  }
   cublasHandle_t h = static_cast<cublasHandle_t>(p->blas);
   COV3D_TRY(check_blas(cublasSetStream(h, p->stream), "cublasSetStream"));
   const unsigned rows = (unsigned)(r * (int64_t)n * n < 4864 ? r * (int64_t)n * n : 4864);

@@ -343,7 +343,19 @@ int cov3d_plan_reserve(cov3d_plan *p, int64_t max_images, int points_L, int ncha
   COV3D_TRY(grow(p->small, max_images * (nchan * nchan * 8 * 2 + nchan * 8 * 2 + 8 + 8) + 64));
   COV3D_TRY(grow(p->ctfc, max_images * (int64_t)sizeof(CtfCoef)));
   if (line_transforms_apply(p)) COV3D_TRY(ensure_twiddles(p, p->n));
+  // the cuFFT plans (and their work areas) of the step's transforms where the line DFTs do not
+  // apply: the pruned 2D + axis-0 pair for even L, the full 3D transform of nchan channels else
+  cufftHandle h = 0;
+  if (prunable(p)) {
+    if (!(line_transforms_apply(p) && p->n <= 256)) {
+      COV3D_TRY(get_fft_planes(p, &h));
+      COV3D_TRY(get_fft_axis0(p, &h));
+    }
+  } else {
+    COV3D_TRY(get_fft(p, nchan, &h));
+  }
   if (flags & COV3D_RESERVE_GRAM_BF16) COV3D_TRY(reserve_gram_bf16(p, (int)max_images, (int)P, nchan));
+  if (flags & COV3D_RESERVE_LS_REG) COV3D_TRY(reserve_ls_reg(p, nchan));
   return check_cuda(cudaStreamSynchronize(p->stream), "reserve");
 }
 

@@ -99,10 +99,12 @@ class _Plan:
             _lib.call("cov3d_setrot", h, _lib.ptr(rot), rot.shape[0], int(points_L))
         self.n_images, self.points_L = rot.shape[0], int(points_L)
 
-    def reserve(self, max_images, points_L, nchan, points=False, gram_bf16=False):
+    def reserve(self, max_images, points_L, nchan, points=False, gram_bf16=False, ls_reg=False):
         """Size the plan's workspaces at set-up (``cov3d_plan_reserve``) so that later calls on
-        up to ``max_images`` images allocate nothing."""
-        flags = (_lib.RESERVE_POINTS if points else 0) | (_lib.RESERVE_GRAM_BF16 if gram_bf16 else 0)
+        up to ``max_images`` images allocate nothing (``ls_reg``: also the least-squares
+        Fourier regulariser's workspace and cuBLAS handle)."""
+        flags = ((_lib.RESERVE_POINTS if points else 0) | (_lib.RESERVE_GRAM_BF16 if gram_bf16 else 0) |
+                 (_lib.RESERVE_LS_REG if ls_reg else 0))
         with torch.cuda.device(self.device):
             _lib.call("cov3d_plan_reserve", self.bind(), int(max_images), int(points_L), int(nchan), flags)
 

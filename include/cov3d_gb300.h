@@ -107,12 +107,16 @@ int cov3d_plan_destroy(cov3d_plan *plan);
 
 /* Size every workspace of the plan for batches of up to max_images images of points_L^2 points
  * and nchan channels (the covariance step at rank nchan, the sort, the rotations, the in-kernel
- * CTF coefficients, the line-DFT twiddles), so that later calls within those sizes allocate
- * nothing (cuFINUFFT sizes its plan at construction, nufft_plan.py:288-316).  Without it the
- * plan grows its buffers on first use.  flags: COV3D_RESERVE_POINTS also sizes the copy of
- * explicit points (setpts), COV3D_RESERVE_GRAM_BF16 the BF16 Gram's operands. */
+ * CTF coefficients, the line-DFT twiddles or, where those do not apply, the cuFFT plans), so
+ * that later calls within those sizes allocate nothing (cuFINUFFT sizes its plan at
+ * construction, nufft_plan.py:288-316).  Without it the plan grows its buffers on first
+ * use.  flags: COV3D_RESERVE_POINTS also sizes the copy of
+ * explicit points (setpts), COV3D_RESERVE_GRAM_BF16 the BF16 Gram's operands,
+ * COV3D_RESERVE_LS_REG the least-squares Fourier regulariser's workspace (2 nchan n^3 + n^2
+ * complex) and its cuBLAS handle. */
 #define COV3D_RESERVE_POINTS 1
 #define COV3D_RESERVE_GRAM_BF16 2
+#define COV3D_RESERVE_LS_REG 4
 int cov3d_plan_reserve(cov3d_plan *plan, int64_t max_images, int points_L, int nchan, int flags);
 int cov3d_plan_set_stream(cov3d_plan *plan, void *stream);
 /* Reports n (fine grid edge), width and beta actually used. */

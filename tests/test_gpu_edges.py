@@ -117,3 +117,41 @@ def test_single_image_batch(pkg, dev):
     assert rel(v2, val.item()) < 1e-5
     assert rel(gv, covar.vectors.grad) < 1e-4
     assert rel(gl, covar.log_sqrt_eigenvals.grad) < 1e-4
+
+
+@pytest.mark.parametrize("L", [32, 16])
+def test_reserved_step_allocates_nothing(pkg, dev, L):
+    """A step built with ``max_batch`` (and ``ls_regulariser`` for the least-squares objective
+    with its Fourier regulariser) allocates no device memory in its calls: the workspaces, the
+    transforms' cuFFT plans (n = 64, 32: outside the line DFTs) and the cuBLAS handle are made
+    at construction.  A step built without ``ls_regulariser`` grows the regulariser's 2 r n^3
+    complex workspace on its first such call (the control that the measurement sees it)."""
+    r, B, n = 3, 8, 2 * L
+    g = torch.Generator(device=dev).manual_seed(5)
+    vec = (torch.randn((r, L, L, L), device=dev, generator=g) / L**1.5).contiguous()
+    ls = torch.zeros((r,), device=dev)
+    imgs = torch.randn((B, L * L), dtype=torch.complex64, device=dev, generator=g)
+    ctf = torch.rand((B, L * L), device=dev, generator=g) + 0.2
+    R = torch.linalg.qr(torch.randn((B, 3, 3), device=dev, generator=g))[0].contiguous()
+    fr = torch.rand((n, n, n), device=dev, generator=g) + 0.1
+    gv, gl = torch.empty_like(vec), torch.empty_like(ls)
+
+    def run(step):
+        step.set_rotations(R)
+        step(vec, ls, imgs, ctf, 5.0, reg_scale=0.1, fourier_reg=fr, objective=1, grad_vectors=gv, grad_log_sqrt=gl)
+        torch.cuda.synchronize(dev)
+
+    run(pkg.FusedCovarStep(L, r, "nufft", 2, device=dev, max_batch=B, ls_regulariser=True))  # loads the kernels
+    free = {}
+    for flag in (True, False):
+        step = pkg.FusedCovarStep(L, r, "nufft", 2, device=dev, max_batch=B, ls_regulariser=flag)
+        torch.cuda.synchronize(dev)
+        before, _ = torch.cuda.mem_get_info(dev)
+        run(step)
+        run(step)
+        after, _ = torch.cuda.mem_get_info(dev)
+        free[flag] = before - after
+        del step
+    assert free[True] == 0
+    if L == 32:  # a 12.6 MB workspace: new pages whatever the allocator keeps
+        assert free[False] >= 2 * r * n**3 * 8

@@ -50,6 +50,9 @@ __device__ __forceinline__ float prologue(const PointGeom &g, int64_t id, const 
 constexpr int kLMin = -8;   // window corners relative to the bin lie in [kLMin, kLMin + 16)
 constexpr int kKeys = 256;  // sort key (l1 - kLMin) * 16 + (l0 - kLMin)
 constexpr int kFoldRanges = 3;  // window-corner rows l1 summed in FP32 between compensated folds
+// spread_rows_kernel: a task's W + ROWS - 1 = 8 ranges (w = 6) in two groups of four, two
+// compensated folds instead of three (16.3 against 16.6 ms per cov-SGD step)
+constexpr int kRowsFold = 4;
 
 // Per-point record staged once per block, in elements of float2 (each weight twice, the operand
 // of a packed multiply: spread_kernel) or float (each weight once, splatted in a register:
@@ -404,7 +407,7 @@ __global__ void __launch_bounds__(kSpreadWarps * 32, W < 8 ? 2 : 1) spread_kerne
 // average).  Shared memory returns per point and lane 40 bytes of values where lanes owning all
 // channels of one cell would take 80: the loads, not the multiply-adds, bound this kernel.  The
 // task's ranges are those of the corners l1 in [b - W + 1, b + ROWS - 1]; the summation (FP32
-// groups of kFoldRanges ranges, TwoSum folds with COMP) and the atomics are those of
+// groups of kRowsFold ranges, TwoSum folds with COMP) and the atomics are those of
 // spread_kernel.
 template <int KT, int W, int CH, int ROWS, bool COMP>
 __global__ void __launch_bounds__(kRowsWarps * 32, kRowsBlocks) spread_rows_kernel(const SpreadParams a) {
@@ -461,7 +464,7 @@ __global__ void __launch_bounds__(kRowsWarps * 32, kRowsBlocks) spread_rows_kern
 #pragma unroll
         for (int ch = 0; ch < CH; ++ch) hi[q][ch] = lo[q][ch] = make_float2(0.f, 0.f);
       bool any = false;
-      for (int l1g = rb + ROWS - 1; l1g > rb - W; l1g -= kFoldRanges) {
+      for (int l1g = rb + ROWS - 1; l1g > rb - W; l1g -= kRowsFold) {
         float2 part[ROWS][CH];  // packed FP32 (FFMA2), same rounding as fmaf
 #pragma unroll
         for (int q = 0; q < ROWS; ++q)
@@ -469,7 +472,7 @@ __global__ void __launch_bounds__(kRowsWarps * 32, kRowsBlocks) spread_rows_kern
           for (int ch = 0; ch < CH; ++ch) part[q][ch] = make_float2(0.f, 0.f);
         bool got = false;
 #pragma unroll
-        for (int sr = 0; sr < kFoldRanges; ++sr) {
+        for (int sr = 0; sr < kRowsFold; ++sr) {
           const int l1 = l1g - sr;
           const int b1 = l1 - kLMin;
           if (l1 <= rb - W || b1 < 0 || b1 > 15 || b0lo > b0hi) continue;

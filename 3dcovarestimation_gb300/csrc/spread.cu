@@ -367,17 +367,25 @@ __global__ void __launch_bounds__(kSpreadWarps * 32, W < 8 ? 2 : 1) spread_kerne
           }
         }
         if (!in) continue;
-        any = true;
+        if (!any) {  // the first group: its fold, TwoSum(0, sum), is (sum, 0) exactly
 #pragma unroll
-        for (int u = 0; u < CPL; ++u) {
-          if (!COMP) {
-            hi01[u] = __fadd2_rn(hi01[u], part01[u]);
-            hi23[u] = __fadd2_rn(hi23[u], part23[u]);
-          } else {
-            two_sum2(hi01[u], lo01[u], part01[u]);
-            two_sum2(hi23[u], lo23[u], part23[u]);
+          for (int u = 0; u < CPL; ++u) {
+            hi01[u] = part01[u];
+            hi23[u] = part23[u];
+          }
+        } else {
+#pragma unroll
+          for (int u = 0; u < CPL; ++u) {
+            if (!COMP) {
+              hi01[u] = __fadd2_rn(hi01[u], part01[u]);
+              hi23[u] = __fadd2_rn(hi23[u], part23[u]);
+            } else {
+              two_sum2(hi01[u], lo01[u], part01[u]);
+              two_sum2(hi23[u], lo23[u], part23[u]);
+            }
           }
         }
+        any = true;
       }
       // the finished cell goes to the global grid
       if (!any) continue;
@@ -463,15 +471,11 @@ __global__ void __launch_bounds__(kRowsWarps * 32, kRowsBlocks) spread_rows_kern
       for (int q = 0; q < ROWS; ++q)
 #pragma unroll
         for (int ch = 0; ch < CH; ++ch) hi[q][ch] = lo[q][ch] = make_float2(0.f, 0.f);
-      bool any = false;
-      for (int l1g = rb + ROWS - 1; l1g > rb - W; l1g -= kRowsFold) {
-        float2 part[ROWS][CH];  // packed FP32 (FFMA2), same rounding as fmaf
-#pragma unroll
-        for (int q = 0; q < ROWS; ++q)
-#pragma unroll
-          for (int ch = 0; ch < CH; ++ch) part[q][ch] = make_float2(0.f, 0.f);
+      // the points of the task's ranges l1g, l1g - 1, ... (kRowsFold of them) multiplied into acc
+      // (packed FP32, FFMA2: the same rounding as fmaf); true if any range held a point
+      auto group = [&](const int l1g, float2(&acc)[ROWS][CH]) {
         bool got = false;
-#pragma unroll  // 128 registers and 12 bytes of spills; not unrolled (126, none): 16.5 against 16.3 ms
+#pragma unroll  // 128 registers, 8 bytes of spills; not unrolled (126, none): 16.5 against 16.3 ms
         for (int sr = 0; sr < kRowsFold; ++sr) {
           const int l1 = l1g - sr;
           const int b1 = l1 - kLMin;
@@ -501,10 +505,21 @@ __global__ void __launch_bounds__(kRowsWarps * 32, kRowsBlocks) spread_rows_kern
 #pragma unroll
             for (int q = 0; q < ROWS; ++q)
 #pragma unroll
-              for (int ch = 0; ch < CH; ++ch) part[q][ch] = __ffma2_rn(w[q], v[ch], part[q][ch]);
+              for (int ch = 0; ch < CH; ++ch) acc[q][ch] = __ffma2_rn(w[q], v[ch], acc[q][ch]);
           }
         }
-        if (!got) continue;
+        return got;
+      };
+      // the first group straight into the cell sums (its fold, TwoSum(0, sum), is (sum, 0)
+      // exactly), each later one summed apart and folded in
+      bool any = group(rb + ROWS - 1, hi);
+      for (int l1g = rb + ROWS - 1 - kRowsFold; l1g > rb - W; l1g -= kRowsFold) {
+        float2 part[ROWS][CH];
+#pragma unroll
+        for (int q = 0; q < ROWS; ++q)
+#pragma unroll
+          for (int ch = 0; ch < CH; ++ch) part[q][ch] = make_float2(0.f, 0.f);
+        if (!group(l1g, part)) continue;
         any = true;
 #pragma unroll
         for (int q = 0; q < ROWS; ++q)

@@ -21,6 +21,16 @@ def load_golden(name):
     return np.load(os.path.join(GOLDEN, name))
 
 
+def cost_scale(total, per_image):
+    """What the FP32 error of a mean ML cost scales with: the larger of the mean and the mean
+    magnitude of its per-image terms, which take either sign and can cancel in the mean (a
+    relative test of a near-zero mean would fail on rounding alone)."""
+    import numpy as np
+
+    per = per_image.detach().abs().mean().item() if hasattr(per_image, "detach") else float(np.mean(np.abs(per_image)))
+    return max(abs(float(total)), per)
+
+
 @pytest.fixture(scope="session")
 def pkg():
     """The product package, with its CUDA library built in-tree (no fallback)."""

@@ -5,13 +5,13 @@ import numpy as np
 import pytest
 import torch
 
-from conftest import load_golden
+from conftest import cost_scale, load_golden
 from oracle import nufft_oracle as O
 
 pytestmark = pytest.mark.gpu
 
 TOL_COST = 1e-5   # FP32 path vs FP64 reference, relative
-TOL_GRAD = 1e-4   # gradient vs FP64, relative (spec bound)
+TOL_GRAD = 1e-4   # gradient vs FP64, relative (the stated gradient bound)
 
 
 def rel(a, b):
@@ -75,6 +75,7 @@ def test_fused_ls_regulariser_matches_dropin(pkg, dev, per_channel):
     L, r, B = 64, 5, 8
     n = 2 * L
     g = torch.Generator(device=dev).manual_seed(5)
+    torch.manual_seed(5)  # the Covar's random initial eigenvolumes
     covar = pkg.Covar(L, r, upsampling_factor=2).to(dev)
     covar.init_grid_correction("bilinear")
     R = torch.linalg.qr(torch.randn((B, 3, 3), device=dev, generator=g))[0].contiguous()
@@ -133,6 +134,7 @@ def test_fused_step_equals_dropin_autograd_full_size(pkg, dev, L, r, B):
     pack and unpack fused; n = 128 and 512) and the drop-in cost (torch's FFT of the volumes,
     vol_forward + ProjectedCost autograd) on the same discretized plan."""
     g = torch.Generator(device=dev).manual_seed(1)
+    torch.manual_seed(1)  # the Covar's random initial eigenvolumes
     covar = pkg.Covar(L, r, upsampling_factor=2).to(dev)
     covar.init_grid_correction("bilinear")
     R = torch.linalg.qr(torch.randn((B, 3, 3), device=dev, generator=g))[0].contiguous()
@@ -142,11 +144,14 @@ def test_fused_step_equals_dropin_autograd_full_size(pkg, dev, L, r, B):
     plan.setrot(R)
     val = pkg.cost_maximum_liklihood_fourier_domain(covar.get_vectors_fourier_domain(), imgs, plan, ctf, 300.0)
     val.backward()
+    with torch.no_grad():
+        per_image = pkg.cost_maximum_liklihood_fourier_domain(covar.get_vectors_fourier_domain(), imgs, plan, ctf,
+                                                              300.0, mean_aggregate=False)
     step = pkg.FusedCovarStep(L, r, "bilinear", 2, device=dev)
     step.set_rotations(R)
     v2, gv, gl = step(covar.vectors.detach(), covar.log_sqrt_eigenvals.detach(), imgs.reshape(B, -1),
                       ctf.reshape(B, -1), 300.0, sync_cost=True)
-    assert rel(v2, val.item()) < 1e-5
+    assert abs(v2 - val.item()) < 1e-5 * cost_scale(val.item(), per_image)
     assert rel(gv, covar.vectors.grad) < 1e-4
     assert rel(gl, covar.log_sqrt_eigenvals.grad) < 1e-4
 

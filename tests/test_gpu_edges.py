@@ -101,6 +101,7 @@ def test_single_image_batch(pkg, dev):
     drop-in cost (the reference squeezes only the volume axis of a single volume)."""
     L, r = 16, 3
     g = torch.Generator(device=dev).manual_seed(4)
+    torch.manual_seed(4)  # the Covar's random initial eigenvolumes
     covar = pkg.Covar(L, r, upsampling_factor=2).to(dev)
     covar.init_grid_correction("bilinear")
     R = torch.linalg.qr(torch.randn((1, 3, 3), device=dev, generator=g))[0].contiguous()
@@ -114,7 +115,7 @@ def test_single_image_batch(pkg, dev):
     step.set_rotations(R)
     v2, gv, gl = step(covar.vectors.detach(), covar.log_sqrt_eigenvals.detach(), imgs.reshape(1, -1),
                       ctf.reshape(1, -1), 300.0, sync_cost=True)
-    assert rel(v2, val.item()) < 1e-5
+    assert rel(v2, val.item()) < 1e-5 or abs(v2 - val.item()) < 1e-6  # one term: relative unless near zero
     assert rel(gv, covar.vectors.grad) < 1e-4
     assert rel(gl, covar.log_sqrt_eigenvals.grad) < 1e-4
 

@@ -782,6 +782,9 @@ def run_gb300(args):
 
 def main():
     args = parse()
+    import torch
+
+    torch.manual_seed(args.seed)  # the Covar's random initial eigenvolumes (the data have their own generators)
     if args.impl == "reference":
         run_reference(args)
     else:

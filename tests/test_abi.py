@@ -53,3 +53,31 @@ def test_host_side_validation(pkg):
         assert "invalid argument" in str(e)
     else:
         raise AssertionError("check() did not raise")
+
+
+def _header_text():
+    text = "".join(open(h).read() for h in sorted(glob.glob(os.path.join(ROOT, "include", "*.h"))))
+    return re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+
+
+def test_binding_matches_every_prototype(pkg):
+    """The ctypes table (_lib._SIGNATURES) gives every prototype of the header the same number of
+    arguments, so a parameter added on one side only fails here rather than on the GPU."""
+    protos = re.findall(r"\b(cov3d_\w+)\s*\(([^;{}]*?)\)\s*;", _header_text(), flags=re.S)
+    assert len(protos) >= 15
+    sigs = pkg._lib._SIGNATURES
+    for name, params in protos:
+        p = params.strip()
+        n = 0 if p in ("", "void") else p.count(",") + 1
+        assert name in sigs, name
+        assert len(sigs[name][1]) == n, (name, n, len(sigs[name][1]))
+
+
+def test_binding_structs_match_the_header(pkg):
+    """cov3d_opts and cov3d_cost_args: the same fields in the same order on both sides."""
+    text = _header_text()
+    for sname, cls in (("cov3d_opts", pkg._lib.Opts), ("cov3d_cost_args", pkg._lib.CostArgs)):
+        m = re.search(r"typedef struct\s*\w*\s*\{([^{}]*)\}\s*" + sname + r"\s*;", text)
+        assert m, sname
+        fields = [re.findall(r"(\w+)\s*$", f.strip())[0] for f in m.group(1).split(";") if f.strip()]
+        assert fields == [f[0] for f in cls._fields_], sname
